@@ -1,0 +1,215 @@
+"""Procedural scenes and environment maps for the benchmark configurations.
+
+Scenes are built as the reference's host arrays (src/cl/scene/CMesh.java:339-357):
+points float4 (w = 0), uvs float2, normals float4, faces 10 x int32 with
+`mat = group << 16 | material`, materials 144 B each. Synthetic throughout; the
+generators are seeded so every run sees the same scene.
+
+  box_room      the box room (36 triangles, 256 x 256, depth 4)
+  soup          uniform triangle soup (1M triangles) in [-1, 1]^3
+  stadium       ground plane of 2M triangles plus a displaced icosphere
+  sky_env       zenith-to-horizon gradient plus a Gaussian sun, lat-long FP32 RGB
+
+Material conventions (stated because the reference leaves them open): GGX
+"roughness r" is the alpha of the GGX lobe, glossy_param.y = glossy_param.z = r
+(no squaring); F0 0.04 is glossy_color = 0.04 with glossy scale 1. Per-triangle
+roughness/albedo draws are quantised to a 64 x 64 palette because the reference
+encodes the material index in 16 bits (src/cl/kernel/Util.cl:11-14).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .layout import FACE, MATERIAL, default_material, make_camera
+
+
+@dataclass
+class Scene:
+    points: np.ndarray            # float32 [V, 4]
+    faces: np.ndarray             # FACE [N]
+    materials: np.ndarray         # MATERIAL [M]
+    uvs: np.ndarray = field(default_factory=lambda: np.zeros((1, 2), np.float32))
+    normals: np.ndarray = field(default_factory=lambda: np.zeros((1, 4), np.float32))
+    camera: np.ndarray | None = None
+    name: str = ""
+
+    @property
+    def ntri(self) -> int:
+        return int(self.faces.shape[0])
+
+
+def _faces(tri_idx: np.ndarray, mat: np.ndarray) -> np.ndarray:
+    f = np.zeros(tri_idx.shape[0], dtype=FACE)
+    f["vx"], f["vy"], f["vz"] = tri_idx[:, 0], tri_idx[:, 1], tri_idx[:, 2]
+    f["uvx"] = f["uvy"] = f["uvz"] = -1
+    f["nx"] = f["ny"] = f["nz"] = -1
+    f["mat"] = mat.astype(np.int32)
+    return f
+
+
+def _points(p: np.ndarray) -> np.ndarray:
+    out = np.zeros((p.shape[0], 4), np.float32)
+    out[:, :3] = p
+    return out
+
+
+def _material(diffuse=(0.75, 0.75, 0.75), glossy=None, alpha=0.0, emission=None, power=0.0):
+    m = default_material()
+    m["diffuse_color"] = (*diffuse, 1.0)
+    m["diffuse_param"] = (1.0, 0.0, 0.0, 0.0)
+    if glossy is not None:
+        m["glossy_color"] = (glossy, glossy, glossy, 1.0)
+        m["glossy_param"] = (1.0, alpha, alpha, 0.0)
+    if emission is not None:
+        m["emission_color"] = (*emission, 1.0)
+        m["emission_param"] = (1.0, power, 0.0, 0.0)
+    return m
+
+
+def _quad(p0, p1, p2, p3):
+    return [(p0, p1, p2), (p0, p2, p3)]
+
+
+def _box(center, size, height, angle_deg):
+    cx, cz = center
+    h = size / 2.0
+    a = math.radians(angle_deg)
+    ca, sa = math.cos(a), math.sin(a)
+
+    def pt(x, y, z):
+        return (cx + ca * x + sa * z, y, cz - sa * x + ca * z)
+
+    c = [pt(-h, 0, -h), pt(h, 0, -h), pt(h, 0, h), pt(-h, 0, h),
+         pt(-h, height, -h), pt(h, height, -h), pt(h, height, h), pt(-h, height, h)]
+    tris = []
+    tris += _quad(c[0], c[1], c[2], c[3])  # bottom
+    tris += _quad(c[4], c[7], c[6], c[5])  # top
+    tris += _quad(c[0], c[4], c[5], c[1])  # sides
+    tris += _quad(c[1], c[5], c[6], c[2])
+    tris += _quad(c[2], c[6], c[7], c[3])
+    tris += _quad(c[3], c[7], c[4], c[0])
+    return tris
+
+
+def box_room(width=256, height=256) -> Scene:
+    """Unit-cube room: 5 quads (grey 0.75, red left wall, green right wall), two
+    boxes of side 0.3 and 0.6 rotated +15 / -18 degrees about y (GGX r 0.3,
+    F0 0.04 over a 0.75 grey base), a 0.25 x 0.25 ceiling emitter of radiance 15.
+    36 triangles. Pinhole camera, vertical fov 40 degrees."""
+    tris, mats = [], []
+    room = [
+        (_quad((0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0)), 0),      # floor
+        (_quad((0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1)), 0),      # ceiling
+        (_quad((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0)), 0),      # back
+        (_quad((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1)), 1),      # left (red)
+        (_quad((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0)), 2),      # right (green)
+    ]
+    for quad, m in room:
+        for t in quad:
+            tris.append(t)
+            mats.append(m)
+    for t in _box((0.68, 0.62), 0.3, 0.3, 15.0):
+        tris.append(t)
+        mats.append(3)
+    for t in _box((0.33, 0.36), 0.6 * 0.5, 0.6, -18.0):
+        tris.append(t)
+        mats.append(3)
+    e0, e1 = 0.5 - 0.125, 0.5 + 0.125
+    y = 0.999
+    for t in _quad((e0, y, e0), (e1, y, e0), (e1, y, e1), (e0, y, e1)):
+        tris.append(t)
+        mats.append(4)
+    pts = np.array([v for t in tris for v in t], np.float32)
+    idx = np.arange(pts.shape[0], dtype=np.int32).reshape(-1, 3)
+    materials = np.stack([
+        _material((0.75, 0.75, 0.75)),
+        _material((0.75, 0.1, 0.1)),
+        _material((0.1, 0.75, 0.1)),
+        _material((0.75, 0.75, 0.75), glossy=0.04, alpha=0.3),
+        _material((0.75, 0.75, 0.75), emission=(1.0, 1.0, 1.0), power=15.0),
+    ])
+    cam = make_camera((0.5, 0.5, 2.35), (0.5, 0.5, 0.0), (0.0, 1.0, 0.0), 40.0, width, height)
+    return Scene(points=_points(pts), faces=_faces(idx, np.array(mats)), materials=materials,
+                 camera=cam, name="box_room")
+
+
+def _palette_materials(levels=64, glossy_fraction=1.0):
+    """64 x 64 palette: roughness r in [0.05, 0.8] x albedo a in [0.2, 0.9]."""
+    mats = []
+    for ri in range(levels):
+        r = 0.05 + 0.75 * (ri + 0.5) / levels
+        for ai in range(levels):
+            a = 0.2 + 0.7 * (ai + 0.5) / levels
+            mats.append(_material((a, a, a), glossy=0.04, alpha=r))
+    return np.stack(mats)
+
+
+def soup(ntri=1_000_000, seed=1, width=1920, height=1080) -> Scene:
+    """Triangle soup: centroids U[-1,1]^3, edge vectors i.i.d. N(0, 0.005^2) per
+    axis, per-triangle GGX roughness U[0.05, 0.8] and albedo U[0.2, 0.9]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    c = rng.uniform(-1.0, 1.0, size=(ntri, 3))
+    e1 = rng.normal(0.0, 0.005, size=(ntri, 3))
+    e2 = rng.normal(0.0, 0.005, size=(ntri, 3))
+    p1 = c - (e1 + e2) / 3.0
+    pts = np.empty((ntri * 3, 3), np.float64)
+    pts[0::3] = p1
+    pts[1::3] = p1 + e1
+    pts[2::3] = p1 + e2
+    ri = rng.integers(0, 64, size=ntri)
+    ai = rng.integers(0, 64, size=ntri)
+    idx = np.arange(ntri * 3, dtype=np.int32).reshape(-1, 3)
+    cam = make_camera((0.0, 0.5, 3.2), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, width, height)
+    return Scene(points=_points(pts.astype(np.float32)), faces=_faces(idx, ri * 64 + ai),
+                 materials=_palette_materials(), camera=cam, name=f"soup{ntri}")
+
+
+def sky_env(width=2048, height=1024, sun_elev_deg=30.0, sun_azim_deg=40.0, sun_sigma_deg=0.5,
+            sun_peak=5.0e4) -> np.ndarray:
+    """FP32 RGB lat-long map (float4 texels, w = 1) in the reference's mapping
+    (src/cl/kernel/Util.cl:397-439: u -> theta = 2 pi u, v -> phi = pi v, y up):
+    zenith-to-horizon gradient plus a Gaussian sun lobe of the given peak."""
+    u = (np.arange(width, dtype=np.float64) + 0.5) / width
+    v = (np.arange(height, dtype=np.float64) + 0.5) / height
+    theta = 2.0 * np.pi * u[None, :]
+    phi = np.pi * v[:, None]
+    dx = -np.sin(phi) * np.cos(theta)
+    dy = np.cos(phi) * np.ones_like(theta)
+    dz = np.sin(phi) * np.sin(theta)
+    up = np.clip(dy, 0.0, 1.0)
+    zenith = np.array([0.25, 0.45, 1.0])
+    horizon = np.array([1.0, 0.95, 0.9])
+    ground = np.array([0.25, 0.22, 0.2])
+    t = np.sqrt(up)[..., None]
+    sky = horizon * (1.0 - t) + zenith * t
+    sky = np.where((dy < 0.0)[..., None], ground, sky)
+    el, az = math.radians(sun_elev_deg), math.radians(sun_azim_deg)
+    sdir = np.array([math.cos(el) * math.cos(az), math.sin(el), math.cos(el) * math.sin(az)])
+    cosang = np.clip(dx * sdir[0] + dy * sdir[1] + dz * sdir[2], -1.0, 1.0)
+    ang = np.arccos(cosang)
+    sig = math.radians(sun_sigma_deg)
+    sun = sun_peak * np.exp(-0.5 * (ang / sig) ** 2)
+    rgb = sky + sun[..., None] * np.array([1.0, 0.95, 0.85])
+    out = np.ones((height, width, 4), np.float32)
+    out[..., :3] = rgb
+    return out.reshape(-1, 4)
+
+
+def random_rays(scene: Scene, n: int, seed: int = 7, inside: bool = True):
+    """Synthetic ray set for traversal parity: origins inside the scene bound
+    (or on a sphere around it), directions uniform on the sphere."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = scene.points[:, :3]
+    lo, hi = p.min(0), p.max(0)
+    if inside:
+        o = rng.uniform(lo, hi, size=(n, 3))
+    else:
+        ctr, rad = (lo + hi) / 2, float(np.linalg.norm(hi - lo)) * 0.75
+        w = rng.normal(size=(n, 3))
+        o = ctr + rad * w / np.linalg.norm(w, axis=1, keepdims=True)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return o.astype(np.float32), d.astype(np.float32)
