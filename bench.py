@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""Benchmark: Mrays/s of the wavefront GI path on the 1M-triangle soup with the
+HDR environment at 1920x1080 (1 spp per step, max depth 8, Russian roulette
+from bounce 3), one GB300 per rank.
+
+A step is one GI frame (one pass of every pixel). `value` counts primary,
+extension and shadow rays traced on the device, over the timed frames, divided
+by the device time (CUDA events on the library's stream); inputs are resident.
+`e2e` is the same metric through the C-ABI with host buffers: every step
+uploads the camera from pinned host memory, renders, and reads the film back
+into pinned host memory.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) each rank renders its own frames of the same job
+(weak scaling: per-GPU work fixed), with no collective on the data path.
+The reference arm times the reference algorithm on the host cores: the
+restatement in oracle/ (the reference's OpenCL C cannot run on the GPU host,
+which has neither an OpenCL runtime nor the reference sources).
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W_DEFAULT, H_DEFAULT, DEPTH, RR = 1920, 1080, 8, 3
+NTRI = 1_000_000
+ENV_W, ENV_H = 2048, 1024
+METRIC = "Mrays/s (primary + extension + shadow rays traced, device-counted)"
+WORKLOAD = "soup1M_1920x1080_depth8_rr3_env2048x1024"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def config_dict(width, height, ntri, world):
+    return {
+        "workload": WORKLOAD if (width, height, ntri) == (W_DEFAULT, H_DEFAULT, NTRI) else
+        f"soup{ntri}_{width}x{height}_depth{DEPTH}_rr{RR}_env{ENV_W}x{ENV_H}",
+        "scene": f"{ntri}-triangle soup, centroids U[-1,1]^3, edges N(0,0.005^2), GGX r U[0.05,0.8], albedo U[0.2,0.9]",
+        "environment": f"{ENV_W}x{ENV_H} FP32 lat-long sky gradient + 0.5 deg Gaussian sun (peak 5e4); SAT built in FP64",
+        "resolution": f"{width}x{height}", "spp_per_step": 1, "max_depth": DEPTH, "rr_from_bounce": RR,
+        "rng": "per-pixel seed pixel ^ 0x9E3779B9 into the reference WangHash chain",
+        "film": "FP32 Kahan-compensated", "launch": "CUDA graph per frame",
+        "l2": "no flush: per-step working set (path state + queues ~420 MB, BVH+triangles 112 MB) exceeds the 129 MB L2",
+        "parallelism": f"replicas x{world} (pixels/frames independent, no collective)",
+    }
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU side
+def cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, seconds, threads):
+    """Oracle frames (benchmark semantics) rendered in parallel threads for about
+    `seconds`; returns (rays, wall seconds, frames)."""
+    from oracle.oracle import ptr
+    cam = sc.camera.copy()
+    stop = time.perf_counter() + seconds
+    lock = threading.Lock()
+    total = {"rays": 0, "frames": 0}
+
+    def worker(tid):
+        f = 0
+        while time.perf_counter() < stop or f == 0:
+            acc = np.zeros((width * height, 4), np.float32)
+            c = np.zeros(DEPTH, np.int32)
+            rc = np.zeros(3, np.int64)
+            orc.lib.or_render_frame(ptr(cam), width, height, DEPTH, 1, RR, None, float(1 + tid + 1000 * f),
+                                    ptr(sc.points), ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces), sc.ntri,
+                                    ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(env), ptr(lum), ptr(sat), ENV_W,
+                                    ENV_H, 1, 0, ptr(acc), ptr(c), ptr(rc))
+            with lock:
+                total["rays"] += int(rc.sum())
+                total["frames"] += 1
+            f += 1
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(worker, range(threads)))
+    return total["rays"], time.perf_counter() - t0, total["frames"]
+
+
+def cpu_scene(orc, ntri):
+    from mambatracer_gb300 import scenes
+    from oracle.oracle import bvh_build, ptr
+    sc = scenes.soup(ntri, seed=1)
+    nodes, bounds, _, _ = bvh_build(orc, sc)
+    env = scenes.sky_env(ENV_W, ENV_H)
+    lum = np.zeros(ENV_W * ENV_H, np.float32)
+    sat = np.zeros(ENV_W * ENV_H, np.float32)
+    orc.lib.or_env_lum_sat(ptr(env), ENV_W, ENV_H, ptr(lum), ptr(sat))
+    return sc, nodes, bounds, env, lum, sat
+
+
+def algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_count, threads):
+    """Per-launch algorithmic bytes of the primary-ray closest-hit launch:
+    sum over rays of 32 (ray in) + 16 (hit out) + 64 per interior visit + 48 per
+    triangle test, the visit counts taken from the FP32 oracle traversal of the
+    same rays (benchmark-semantics raygen of this frame)."""
+    from mambatracer_gb300 import layout
+    from oracle.oracle import ptr
+    n = width * height
+    rays = np.zeros(n, layout.RAY)
+    cam = cam.copy()
+    cam["dimension"] = (width, height)
+    orc.lib.or_raygen(ptr(cam), ptr(rays), None, float(frame_count), n, 1)
+    chunks = np.array_split(np.arange(n), threads * 4)
+    res = np.zeros((n, 2), np.int64)
+
+    def work(idx):
+        r = np.ascontiguousarray(rays[idx])
+        t = np.zeros(len(idx), np.float32)
+        p = np.zeros(len(idx), np.int32)
+        c = np.zeros((len(idx), 2), np.int64)
+        orc.lib.or_trace_closest(ptr(r), len(idx), ptr(sc.points), ptr(sc.faces), sc.ntri, ptr(nodes), ptr(bounds),
+                                 ptr(t), ptr(p), ptr(c))
+        res[idx] = c
+
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(work, [c for c in chunks if len(c)]))
+    v_int, tri = res[:, 0].sum(), res[:, 1].sum()
+    return int(n * 48 + 64 * v_int + 48 * tri), float(v_int) / n, float(tri) / n
+
+
+# ------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from mambatracer_gb300 import api, build, scenes
+    build.build()
+
+    width, height, ntri = (640, 360, 200_000) if args.small else (W_DEFAULT, H_DEFAULT, NTRI)
+    sc = scenes.soup(ntri, seed=1, width=width, height=height)
+    env = scenes.sky_env(ENV_W, ENV_H)
+    ctx = api.Context(local)
+    S = api.Scene(ctx, sc)
+    nodes, bounds = S.build_bvh()
+    S.set_env(env, ENV_W, ENV_H)
+    job = api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, use_graph=1)
+    cam = sc.camera.copy()
+    job.set_camera(cam)
+
+    def frame_no(step):
+        return float(1 + step * world + rank)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for i in range(args.warmup):
+        job.render(None, frame_no(i))
+    ctx.finish()
+    job.clear()
+    barrier()
+    ctx.finish()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ctx.record(0)
+    for i in range(args.steps):
+        job.render(None, frame_no(args.warmup + i))
+    ctx.record(1)
+    ctx.finish()
+    barrier()
+    ms = ctx.elapsed_ms(0, 1)
+    clk = clocks.stop()
+    rays = job.total_rays()
+    total_rays = int(rays.sum())
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        rr = torch.tensor([total_rays], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(rr)
+        total_rays = int(rr.item())
+    value = total_rays / (ms * 1e-3) / 1e6
+
+    # e2e through the C-ABI with host buffers: camera in (pinned), film out (pinned)
+    import ctypes as C
+
+    from mambatracer_gb300._lib import check, lib
+    film_host = torch.empty((width * height, 4), dtype=torch.float32, pin_memory=True)
+    cam_host = torch.empty(64, dtype=torch.uint8, pin_memory=True)
+    cam_host.numpy()[:] = np.frombuffer(cam.tobytes(), np.uint8)
+    L = lib()
+    e2e_steps = max(3, args.steps // 2)
+    job.clear()
+    barrier()
+    ctx.finish()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        check(L.mt_job_set_camera(job.h, C.c_void_p(cam_host.data_ptr())))
+        check(L.mt_render_frame(job.h, None, frame_no(10000 + i)))
+        check(L.mt_film_read(job.h, C.c_void_p(film_host.data_ptr()), 0))
+    e2e_s = time.perf_counter() - t0
+    e2e_rays = int(job.total_rays().sum())
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+        rr = torch.tensor([e2e_rays], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(rr)
+        e2e_rays = int(rr.item())
+    e2e = {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s",
+           "h2d_bytes_per_step": 64 + 416, "d2h_bytes_per_step": width * height * 16,
+           "note": "camera (64 B) and the pass parameters (416 B) in, the float4 film out, per frame"}
+
+    out = None
+    if rank == 0:
+        # per-launch device times (profiled frames, no graph) for the roofline
+        pj = api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, profile=1)
+        pj.set_camera(cam)
+        prof_frames = 5
+        kms = []
+        for i in range(prof_frames + 1):
+            pj.render(None, frame_no(i))
+            if i:
+                kms.append(pj.kernel_ms()[0])
+        kms = np.mean(np.stack(kms), axis=0)
+        names = ["raygen"] + [f"{k}_b{b}" for b in range(1, DEPTH + 1) for k in ("trace_closest", "shade",
+                                                                                 "trace_shadow")]
+        per_kernel = {n: round(float(v), 4) for n, v in zip(names, kms)}
+        trace_total = float(sum(v for n, v in per_kernel.items() if n.startswith("trace_")))
+        frame_total = float(kms.sum())
+        pj.close()
+        from oracle.oracle import Oracle
+        orc = Oracle()
+        threads = os.cpu_count() or 1
+        t_alg = time.perf_counter()
+        alg_bytes, v_int, tri = algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_no(1), threads)
+        t_alg = time.perf_counter() - t_alg
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except OSError:
+            pass
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        t_b1 = per_kernel["trace_closest_b1"]
+        achieved = alg_bytes / (t_b1 * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "kernel": "k_trace_closest (bounce 1, primary rays)",
+                    "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                    "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                    "traffic": None,
+                    "alg_bytes_per_launch": alg_bytes, "rays_per_launch": width * height,
+                    "interior_visits_per_ray": round(v_int, 2), "triangle_tests_per_ray": round(tri, 2),
+                    "launch_ms": round(t_b1, 4),
+                    "trace_share_of_frame": round(trace_total / frame_total, 3), "per_kernel_ms": per_kernel}
+        # CPU baseline: the oracle on the host cores, a bounded sample
+        cw, ch = width // 4, height // 4
+        csc, cn, cb, cenv, clum, csat = sc, nodes, bounds, env, None, None
+        from oracle.oracle import ptr
+        clum = np.zeros(ENV_W * ENV_H, np.float32)
+        csat = np.zeros(ENV_W * ENV_H, np.float32)
+        orc.lib.or_env_lum_sat(ptr(cenv), ENV_W, ENV_H, ptr(clum), ptr(csat))
+        crays, csec, cframes = cpu_render_rate(orc, csc, cn, cb, cenv, clum, csat, cw, ch, args.cpu_seconds, threads)
+        cpu_baseline = {"value": round(crays / csec / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                        "sample": f"{cframes} frames of {cw}x{ch} (1/16 of the pixels, same scene, camera, depth, RR) "
+                                  f"in {threads} threads for {csec:.1f} s; oracle/mt_oracle.cpp (FP32)"}
+        out = {
+            "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (procedural soup and sky; no dataset)",
+            "config": config_dict(width, height, ntri, world),
+            "rays_per_step": round(total_rays / args.steps / world), "rays_split": rays.tolist(),
+            "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e,
+            "gpu_launches": args.steps * (2 + 3 * DEPTH), "clocks": clk,
+            "msamples_per_s": round(width * height * args.steps * world / (ms * 1e-3) / 1e6, 2),
+            "bvh_depth": S.depth, "alg_bytes_seconds": round(t_alg, 1),
+        }
+    job.close()
+    S.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------- reference arm
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import build as ob
+    from oracle.oracle import Oracle
+    ob.build()
+    orc = Oracle()
+    threads = os.cpu_count() or 1
+    sc, nodes, bounds, env, lum, sat = cpu_scene(orc, NTRI)
+    width, height = W_DEFAULT // 4, H_DEFAULT // 4
+    for _ in range(args.warmup):
+        cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, 0.0, threads)
+    rays = secs = frames = 0
+    for _ in range(args.steps):
+        r, s, f = cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, 0.0, threads)
+        rays, secs, frames = rays + r, secs + s, frames + f
+    value = rays / secs / 1e6
+    sample = (f"each step: {threads} frames of {width}x{height} (1/16 of the 1080p pixels) rendered in parallel, "
+              f"one per host thread; oracle/mt_oracle.cpp, the FP32 restatement pinned bit-exact to the reference kernels")
+    out = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (procedural soup and sky; no dataset)",
+        "config": config_dict(W_DEFAULT, H_DEFAULT, NTRI, world),
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("the reference's OpenCL kernels need an OpenCL runtime (none on this host: no ICD, no PoCL) and "
+                 "its sources are not on the GPU host; its algorithm runs as the oracle restatement"),
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="mambatracer", choices=["mambatracer", "reference"])
+    ap.add_argument("--small", action="store_true", help="small case for profiler captures")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

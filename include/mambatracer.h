@@ -1,0 +1,206 @@
+/*
+ * mambatracer.h - C-ABI of the GB300 wavefront GI path tracer.
+ *
+ * Drop-in boundary for MambaTracer's render path: the Java host
+ * (src/cl/device/CDeviceGI.java and the classes it drives) reaches these entry
+ * points through Panama FFM or JNI in place of JOCL. Plain pointers and sizes
+ * only. Every struct that crosses this boundary keeps the reference's OpenCL
+ * byte layout:
+ *   points    float4 per vertex (w = 0)            src/cl/scene/CMesh.java:339-357
+ *   uvs       float2 per uv
+ *   normals   float4 per normal
+ *   faces     Face, 10 x int32 (40 B)              src/cl/kernel/Util.cl:95-102
+ *   materials Material, 144 B                      src/cl/kernel/Bsdf.cl:24-50
+ *   nodes     BVHNode, 7 x int32 (28 B)            src/cl/kernel/NormalBVH.cl:1-11
+ *   bounds    BoundingBox, 2 x float4 (32 B)       src/cl/kernel/Util.cl:116-121
+ *   rays      Ray (80 B)                           src/cl/kernel/Util.cl:129-138
+ *   camera    CameraStruct (64 B)                  src/cl/kernel/Util.cl:78-85
+ *
+ * Errors: every call returns 0 (MT_OK) or a negative MT_ERR_* code; the
+ * message of the last failure on the calling thread is mt_last_error(). This
+ * replaces the CLException JOCL throws (src/cl/ui/fx/main/TracerAPI.java:79).
+ * Device-side failures (a bounded wait that ran out) are latched in the
+ * context and returned by the next call that synchronises (MT_ERR_DEVICE).
+ *
+ * Threading: one CUDA stream per context, calls on one context are serialised
+ * by an internal mutex (the reference serialises on one in-order OpenCL queue,
+ * src/cl/device/CDeviceGI.java:200-203). Only calls that return data to the
+ * host wait for the device.
+ */
+#ifndef MAMBATRACER_H
+#define MAMBATRACER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MT_OK 0
+#define MT_ERR_INVALID -1   /* bad argument, malformed array, unknown name */
+#define MT_ERR_CUDA -2      /* a CUDA runtime call failed */
+#define MT_ERR_NOMEM -3     /* device allocation failed / over budget */
+#define MT_ERR_DEPTH -4     /* BVH deeper than the 64-level traversal stack */
+#define MT_ERR_DEVICE -5    /* a kernel latched an error (bounded wait expired) */
+#define MT_ERR_BUSY -6      /* served mode: admission refused, retry later */
+
+typedef struct mt_context mt_context;
+typedef struct mt_buffer mt_buffer;
+typedef struct mt_kernel mt_kernel;
+typedef struct mt_scene mt_scene;
+typedef struct mt_job mt_job;
+
+/* ------------------------------------------------------------ context */
+
+/* OpenCLConfiguration.getDefault (src/cl/ui/fx/main/TracerAPI.java:86-90). */
+int mt_ctx_create(int device, mt_context** out);
+int mt_ctx_destroy(mt_context* ctx);
+/* OpenCLConfiguration.finish (src/cl/device/CDeviceGI.java:428). */
+int mt_finish(mt_context* ctx);
+const char* mt_last_error(void);
+/* Library build string (arch, parity flags). */
+const char* mt_version(void);
+
+/* ---------------------------------------- low level: buffers (CMemory) */
+
+/* OpenCLConfiguration.createBufferB/I/F (e.g. src/cl/device/CDeviceGI.java:152-162). */
+int mt_buf_alloc(mt_context* ctx, size_t bytes, mt_buffer** out);
+/* createFromI/F (e.g. src/cl/scene/CMesh.java:341-345): allocate and upload. */
+int mt_buf_create_from(mt_context* ctx, const void* host, size_t bytes, mt_buffer** out);
+/* CMemory.transferToDevice / setCL (src/cl/algorithms/CCompact.java:81). */
+int mt_buf_write(mt_buffer* buf, size_t offset, const void* host, size_t bytes);
+/* CMemory.transferFromDevice / getCL (src/cl/device/CDeviceGI.java:357). */
+int mt_buf_read(mt_buffer* buf, size_t offset, void* host, size_t bytes);
+/* Fill with a repeated 4-byte pattern (the Init*Data kernels' job). */
+int mt_buf_fill32(mt_buffer* buf, uint32_t pattern, size_t offset, size_t bytes);
+size_t mt_buf_size(const mt_buffer* buf);
+/* CResourceFactory.releaseMemory (src/cl/scene/CNormalBVH.java:56). */
+int mt_buf_free(mt_buffer* buf);
+
+/* ----------------------------- low level: kernels by name (CKernel) */
+
+/* OpenCLConfiguration.createKernel(name, args...) (e.g. src/cl/device/CDeviceGI.java:168-178).
+ * Names are the reference's __kernel names; the argument list is the
+ * reference's (buffers in the reference layouts). Supported: the plain
+ * wavefront set listed by mt_kernel_names(). */
+int mt_kernel_create(mt_context* ctx, const char* name, mt_kernel** out);
+const char* mt_kernel_names(void);
+/* CKernel.putArg(i, mem) (src/cl/device/CDeviceGI.java:301). */
+int mt_kernel_set_arg_buf(mt_kernel* k, int index, mt_buffer* buf);
+/* __local scratch arguments (CLocalMemory.LOCALINT/LOCALFLOAT): size only. */
+int mt_kernel_set_arg_local(mt_kernel* k, int index, size_t bytes);
+/* OpenCLConfiguration.execute1DKernel(k, global, local): local is a hint;
+ * work-items >= global are not launched. */
+int mt_launch_1d(mt_kernel* k, size_t global, size_t local);
+int mt_kernel_destroy(mt_kernel* k);
+
+/* --------------------------------------------------- scene and BVH */
+
+/* Mesh arrays (CMesh.initCLBuffers, src/cl/scene/CMesh.java:339-357). uvs and
+ * normals may be NULL when no face references them (uvx/nx = -1). */
+int mt_scene_create(mt_context* ctx, const float* points, int npoints, const float* uvs, int nuvs,
+                    const float* normals, int nnormals, const int32_t* faces, int nfaces,
+                    const void* materials, int nmaterials, mt_scene** out);
+/* CNormalBVH.build (src/cl/scene/CNormalBVH.java:45-148) on the host, same
+ * node layout; optional copies of nodes (7*(2N-1) ints) and bounds (8*(2N-1)
+ * floats) are returned. depth_out: the BVH depth. */
+int mt_bvh_build(mt_scene* scene, int32_t* nodes_out, float* bounds_out, int* depth_out);
+/* The same build on host arrays only (no device work, no context): fills
+ * nodes_out (7*(2N-1) ints) and bounds_out (8*(2N-1) floats) as the Java
+ * CNormalBVH fills its CMemory<CNode>/CMemory<CBound> (CNormalBVH.java:59-79). */
+int mt_bvh_build_host(const float* points, int npoints, const int32_t* faces, int nfaces, int32_t* nodes_out,
+                      float* bounds_out, int* depth_out);
+/* Use a BVH built elsewhere (the Java builder's nodes/bounds buffers). */
+int mt_bvh_import(mt_scene* scene, const int32_t* nodes, const float* bounds, int nnodes);
+/* Traversal precision: 0 = FP32 child boxes (default), 1 = 8-bit child boxes
+ * quantised relative to the parent and rounded outward. */
+int mt_scene_set_bvh_precision(mt_scene* scene, int precision);
+/* Replace the material table (TracerAPI material edits, src/cl/ui/fx/main/TracerAPI.java:371). */
+int mt_scene_set_materials(mt_scene* scene, const void* materials, int nmaterials);
+int mt_scene_light_count(const mt_scene* scene);
+int mt_scene_destroy(mt_scene* scene);
+
+/* ------------------------------------------------ environment light */
+
+/* CEnvironment.setEnvironmentMap (src/cl/algorithms/CEnvironment.java:46-60):
+ * rgb is float4 per texel (lat-long, width x height). The luminance and the
+ * inclusive SAT are built on the GPU in FP64 (stored FP32 for sampling). */
+int mt_env_set(mt_scene* scene, const float* rgb, int width, int height);
+/* Same, with the luminance and SAT given (e.g. the host SAT of the reference). */
+int mt_env_set_with_sat(mt_scene* scene, const float* rgb, const float* lum, const float* sat, int width,
+                        int height);
+int mt_env_clear(mt_scene* scene);
+/* Copy out the GPU-built luminance / FP64 SAT (either may be NULL). */
+int mt_env_read(mt_scene* scene, float* lum, double* sat64, float* sat32);
+
+/* Adaptive light grid (CAdaptiveEnvironment, src/cl/algorithms/CAdaptiveEnvironment.java:69-145):
+ * nu x nv grid of cells of rx x ry tiles (reference: 1600 x 1600, 16 x 32).
+ * enable = 0 turns grid-guided sampling off (full-map SAT as the reference). */
+int mt_env_grid_config(mt_scene* scene, int nu, int nv, int rx, int ry, int enable);
+/* Per-cell SAT of a given func (prefixSumRowSubgrid + prefixSumColSubgrid,
+ * src/cl/kernel/LightGrid.cl:347-400); fp64 != 0 builds it in FP64. */
+int mt_env_grid_sat(mt_context* ctx, const float* func, float* sat_out, int nu, int nv, int rx, int ry,
+                    int fp64);
+
+/* ---------------------------------------------------------- rendering */
+
+typedef struct mt_render_config {
+  int width, height;
+  int max_depth;     /* bounces per path (reference: 15, CDeviceGI.java:226) */
+  int mode;          /* 0 = reference semantics, 1 = benchmark semantics (pixel-keyed RNG, RR, Q1/Q2 fixed) */
+  int rr_depth;      /* mode 1: Russian roulette from this bounce on (0 = off) */
+  int film_kahan;    /* 1 = compensated film sums (default), 0 = plain FP32 adds as the reference */
+  int spp;           /* passes per mt_render_frame call */
+  int use_graph;     /* 1 = replay each frame's launches as a CUDA graph */
+  int profile;       /* 1 = time every kernel launch with CUDA events (no graph) */
+} mt_render_config;
+
+/* A render job: film + path state resident on the device (CDeviceGI.setup,
+ * src/cl/device/CDeviceGI.java:116-164). */
+int mt_job_create(mt_context* ctx, mt_scene* scene, const mt_render_config* cfg, mt_job** out);
+int mt_job_destroy(mt_job* job);
+/* CDeviceGI.updateCamera (src/cl/device/CDeviceGI.java:308-313). */
+int mt_job_set_camera(mt_job* job, const void* camera);
+/* One GI frame: CDeviceGI.loop (src/cl/device/CDeviceGI.java:214-271) without
+ * the texture pass. seeds: in mode 0 the State seed pair of each
+ * allocateState() call in launch order (2 * (1 + 2 * max_depth) ints per
+ * pass), NULL in mode 1. frame_count: State.frameCount of the first pass. */
+int mt_render_frame(mt_job* job, const int32_t* seeds, float frame_count);
+/* CImage film: accum (float4 per pixel). resolve != 0 divides by the frame
+ * count as averageAccum does (src/cl/kernel/Image.cl:29-67). */
+int mt_film_read(mt_job* job, float* rgba, int resolve);
+int mt_film_clear(mt_job* job);
+/* Rays traced so far: [primary, extension, shadow], and the live queue length
+ * after each bounce of the last pass (max_depth ints). */
+int mt_job_stats(mt_job* job, int64_t* rays3, int32_t* counts);
+/* Rays traced since the job was created or its film cleared: [primary,
+ * extension, shadow], counted on the device. */
+int mt_job_total_rays(mt_job* job, int64_t* rays3);
+/* Device time of the last mt_render_frame, in ms (CUDA events on the job's stream). */
+int mt_job_last_ms(mt_job* job, float* ms);
+/* Profiled jobs: device time of each launch of the last frame, in ms, pass by
+ * pass: [raygen, then per bounce trace_closest, shade, trace_shadow] =
+ * spp * (1 + 3 * max_depth) floats. */
+int mt_job_kernel_ms(mt_job* job, float* ms);
+
+/* CUDA event slots on the context's stream (0..7): record, and the device
+ * time between two recorded slots. */
+int mt_ctx_event_record(mt_context* ctx, int slot);
+int mt_ctx_event_elapsed(mt_context* ctx, int from_slot, int to_slot, float* ms);
+
+/* ------------------------------------------------------- ray queries */
+
+/* Closest hit over n rays in the reference Ray layout (80 B each, tMax is
+ * updated as IntersectPrimitives does): t_out and prim_out (-1 on a miss). */
+int mt_trace_closest(mt_scene* scene, const void* rays, int n, float* t_out, int32_t* prim_out);
+/* Any hit (testOcclusion, src/cl/kernel/NormalBVH.cl:235-317): 1 = occluded. */
+int mt_trace_any(mt_scene* scene, const void* rays, int n, int32_t* occluded_out);
+/* Device-resident variant for benchmarks: rays/outputs are mt_buffers. */
+int mt_trace_closest_dev(mt_scene* scene, mt_buffer* rays, int n, mt_buffer* t_out, mt_buffer* prim_out,
+                         float* ms_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MAMBATRACER_H */

@@ -1,0 +1,108 @@
+"""ctypes binding of libmambatracer.so (the C-ABI in include/mambatracer.h).
+
+The library is required: importing the package's runtime API without it raises,
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmambatracer.so")
+
+MT_OK = 0
+ERRORS = {-1: "MT_ERR_INVALID", -2: "MT_ERR_CUDA", -3: "MT_ERR_NOMEM", -4: "MT_ERR_DEPTH", -5: "MT_ERR_DEVICE",
+          -6: "MT_ERR_BUSY"}
+
+
+class MTError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class RenderConfig(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("max_depth", C.c_int), ("mode", C.c_int),
+                ("rr_depth", C.c_int), ("film_kahan", C.c_int), ("spp", C.c_int), ("use_graph", C.c_int),
+                ("profile", C.c_int)]
+
+
+P = C.c_void_p
+I = C.c_int
+F = C.c_float
+PI = C.POINTER(C.c_int)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "mt_ctx_create": (I, [I, C.POINTER(P)]),
+    "mt_ctx_destroy": (I, [P]),
+    "mt_finish": (I, [P]),
+    "mt_last_error": (C.c_char_p, []),
+    "mt_version": (C.c_char_p, []),
+    "mt_buf_alloc": (I, [P, C.c_size_t, C.POINTER(P)]),
+    "mt_buf_create_from": (I, [P, P, C.c_size_t, C.POINTER(P)]),
+    "mt_buf_write": (I, [P, C.c_size_t, P, C.c_size_t]),
+    "mt_buf_read": (I, [P, C.c_size_t, P, C.c_size_t]),
+    "mt_buf_fill32": (I, [P, C.c_uint32, C.c_size_t, C.c_size_t]),
+    "mt_buf_size": (C.c_size_t, [P]),
+    "mt_buf_free": (I, [P]),
+    "mt_kernel_create": (I, [P, C.c_char_p, C.POINTER(P)]),
+    "mt_kernel_names": (C.c_char_p, []),
+    "mt_kernel_set_arg_buf": (I, [P, I, P]),
+    "mt_kernel_set_arg_local": (I, [P, I, C.c_size_t]),
+    "mt_launch_1d": (I, [P, C.c_size_t, C.c_size_t]),
+    "mt_kernel_destroy": (I, [P]),
+    "mt_scene_create": (I, [P, P, I, P, I, P, I, P, I, P, I, C.POINTER(P)]),
+    "mt_bvh_build": (I, [P, P, P, PI]),
+    "mt_bvh_build_host": (I, [P, I, P, I, P, P, PI]),
+    "mt_bvh_import": (I, [P, P, P, I]),
+    "mt_scene_set_bvh_precision": (I, [P, I]),
+    "mt_scene_set_materials": (I, [P, P, I]),
+    "mt_scene_light_count": (I, [P]),
+    "mt_scene_destroy": (I, [P]),
+    "mt_env_set": (I, [P, P, I, I]),
+    "mt_env_set_with_sat": (I, [P, P, P, P, I, I]),
+    "mt_env_clear": (I, [P]),
+    "mt_env_read": (I, [P, P, P, P]),
+    "mt_env_grid_config": (I, [P, I, I, I, I, I]),
+    "mt_env_grid_sat": (I, [P, P, P, I, I, I, I, I]),
+    "mt_job_create": (I, [P, P, C.POINTER(RenderConfig), C.POINTER(P)]),
+    "mt_job_destroy": (I, [P]),
+    "mt_job_set_camera": (I, [P, P]),
+    "mt_render_frame": (I, [P, P, F]),
+    "mt_film_read": (I, [P, P, I]),
+    "mt_film_clear": (I, [P]),
+    "mt_job_stats": (I, [P, P, P]),
+    "mt_job_last_ms": (I, [P, C.POINTER(C.c_float)]),
+    "mt_job_kernel_ms": (I, [P, P]),
+    "mt_job_total_rays": (I, [P, P]),
+    "mt_ctx_event_record": (I, [P, I]),
+    "mt_ctx_event_elapsed": (I, [P, I, I, C.POINTER(C.c_float)]),
+    "mt_trace_closest": (I, [P, P, I, P, P]),
+    "mt_trace_any": (I, [P, P, I, P]),
+    "mt_trace_closest_dev": (I, [P, P, I, P, P, C.POINTER(C.c_float)]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded library; raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with mambatracer_gb300.build.build() "
+                              "(there is no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(code: int) -> None:
+    if code != MT_OK:
+        raise MTError(code, lib().mt_last_error().decode())

@@ -1,0 +1,278 @@
+"""Host API over the C-ABI, mirroring the reference's device interface.
+
+`DeviceGI` follows RayDeviceInterface / CDeviceGI (src/cl/abstracts/RayDeviceInterface.java:28-71,
+src/cl/device/CDeviceGI.java): `set(mesh, bvh)`, `setup(w, h)`, `update_camera()`,
+`execute()` (one frame), `start/pause/resume/stop` on a render thread, and
+`update_image()` returning the film. Everything runs through libmambatracer.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import numpy as np
+
+from . import layout
+from ._lib import RenderConfig, check, lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().mt_ctx_create(device, C.byref(h)))
+        self.h = h
+
+    def finish(self):
+        check(lib().mt_finish(self.h))
+
+    def record(self, slot: int):
+        check(lib().mt_ctx_event_record(self.h, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        check(lib().mt_ctx_event_elapsed(self.h, a, b, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if self.h:
+            check(lib().mt_ctx_destroy(self.h))
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Scene:
+    """Mesh arrays on the device (CMesh.initCLBuffers, src/cl/scene/CMesh.java:339-357)."""
+
+    def __init__(self, ctx: Context, sc):
+        self.ctx = ctx
+        self.src = sc
+        pts = np.ascontiguousarray(sc.points, np.float32)
+        faces = np.ascontiguousarray(sc.faces)
+        mats = np.ascontiguousarray(sc.materials)
+        uvs = np.ascontiguousarray(sc.uvs, np.float32)
+        nrm = np.ascontiguousarray(sc.normals, np.float32)
+        h = C.c_void_p()
+        check(lib().mt_scene_create(ctx.h, _p(pts), pts.shape[0], _p(uvs), uvs.shape[0], _p(nrm), nrm.shape[0],
+                                    _p(faces), faces.shape[0], _p(mats), mats.shape[0], C.byref(h)))
+        self.h = h
+        self.depth = None
+
+    def build_bvh(self):
+        """CNormalBVH.build on the host (returns nodes, bounds in the reference layout)."""
+        n = self.src.ntri
+        nodes = np.zeros((2 * n - 1, 7), np.int32)
+        bounds = np.zeros((2 * n - 1, 8), np.float32)
+        depth = C.c_int()
+        check(lib().mt_bvh_build(self.h, _p(nodes), _p(bounds), C.byref(depth)))
+        self.depth = depth.value
+        return nodes, bounds
+
+    def import_bvh(self, nodes: np.ndarray, bounds: np.ndarray):
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        bounds = np.ascontiguousarray(bounds, np.float32)
+        check(lib().mt_bvh_import(self.h, _p(nodes), _p(bounds), nodes.shape[0]))
+
+    def set_env(self, rgb: np.ndarray, w: int, h: int):
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        check(lib().mt_env_set(self.h, _p(rgb), w, h))
+
+    def set_env_with_sat(self, rgb, lum, sat, w, h):
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        lum = np.ascontiguousarray(lum, np.float32)
+        sat = np.ascontiguousarray(sat, np.float32)
+        check(lib().mt_env_set_with_sat(self.h, _p(rgb), _p(lum), _p(sat), w, h))
+
+    def env_arrays(self, w, h):
+        lum = np.zeros(w * h, np.float32)
+        sat64 = np.zeros(w * h, np.float64)
+        sat32 = np.zeros(w * h, np.float32)
+        check(lib().mt_env_read(self.h, _p(lum), _p(sat64), _p(sat32)))
+        return lum, sat64, sat32
+
+    @property
+    def light_count(self) -> int:
+        return lib().mt_scene_light_count(self.h)
+
+    def trace_closest(self, rays: np.ndarray):
+        rays = np.ascontiguousarray(rays)
+        assert rays.dtype == layout.RAY
+        t = np.zeros(rays.shape[0], np.float32)
+        prim = np.zeros(rays.shape[0], np.int32)
+        check(lib().mt_trace_closest(self.h, _p(rays), rays.shape[0], _p(t), _p(prim)))
+        return t, prim
+
+    def trace_any(self, rays: np.ndarray):
+        rays = np.ascontiguousarray(rays)
+        assert rays.dtype == layout.RAY
+        occ = np.zeros(rays.shape[0], np.int32)
+        check(lib().mt_trace_any(self.h, _p(rays), rays.shape[0], _p(occ)))
+        return occ
+
+    def close(self):
+        if self.h:
+            check(lib().mt_scene_destroy(self.h))
+            self.h = None
+
+
+class Job:
+    """Film and path state of one render job resident on the device."""
+
+    def __init__(self, ctx: Context, scene: Scene, width: int, height: int, max_depth: int = 15, mode: int = 0,
+                 rr_depth: int = 0, film_kahan: int = 1, spp: int = 1, use_graph: int = 0, profile: int = 0):
+        self.cfg = RenderConfig(width, height, max_depth, mode, rr_depth, film_kahan, spp, use_graph, profile)
+        h = C.c_void_p()
+        check(lib().mt_job_create(ctx.h, scene.h, C.byref(self.cfg), C.byref(h)))
+        self.h = h
+        self.width, self.height = width, height
+
+    def set_camera(self, cam: np.ndarray):
+        cam = np.ascontiguousarray(cam)
+        assert cam.dtype == layout.CAMERA
+        check(lib().mt_job_set_camera(self.h, _p(cam)))
+
+    def render(self, seeds: np.ndarray | None = None, frame_count: float = 1.0):
+        if seeds is not None:
+            seeds = np.ascontiguousarray(seeds, np.int32)
+        check(lib().mt_render_frame(self.h, _p(seeds), float(frame_count)))
+
+    def film(self, resolve: bool = False) -> np.ndarray:
+        out = np.zeros((self.width * self.height, 4), np.float32)
+        check(lib().mt_film_read(self.h, _p(out), int(resolve)))
+        return out
+
+    def clear(self):
+        check(lib().mt_film_clear(self.h))
+
+    def stats(self):
+        rays = np.zeros(3, np.int64)
+        counts = np.zeros(self.cfg.max_depth, np.int32)
+        check(lib().mt_job_stats(self.h, _p(rays), _p(counts)))
+        return rays, counts
+
+    def total_rays(self) -> np.ndarray:
+        out = np.zeros(3, np.int64)
+        check(lib().mt_job_total_rays(self.h, _p(out)))
+        return out
+
+    def last_ms(self) -> float:
+        ms = C.c_float()
+        check(lib().mt_job_last_ms(self.h, C.byref(ms)))
+        return ms.value
+
+    def kernel_ms(self) -> np.ndarray:
+        """Per-launch device times of the last frame (profiled jobs): spp x (1 + 3 * max_depth)."""
+        out = np.zeros(self.cfg.spp * (1 + 3 * self.cfg.max_depth), np.float32)
+        check(lib().mt_job_kernel_ms(self.h, _p(out)))
+        return out.reshape(self.cfg.spp, -1)
+
+    def close(self):
+        if self.h:
+            check(lib().mt_job_destroy(self.h))
+            self.h = None
+
+
+def bvh_build_host(sc):
+    """CNormalBVH.build on host arrays (no device needed)."""
+    n = sc.ntri
+    nodes = np.zeros((2 * n - 1, 7), np.int32)
+    bounds = np.zeros((2 * n - 1, 8), np.float32)
+    depth = C.c_int()
+    pts = np.ascontiguousarray(sc.points, np.float32)
+    faces = np.ascontiguousarray(sc.faces)
+    check(lib().mt_bvh_build_host(_p(pts), pts.shape[0], _p(faces), n, _p(nodes), _p(bounds), C.byref(depth)))
+    return nodes, bounds, depth.value
+
+
+class DeviceGI:
+    """Progressive GI device (CDeviceGI): a render thread that calls execute()
+    in a loop, with pause/resume/stop as LambdaThread offers them."""
+
+    def __init__(self, width: int, height: int, ctx: Context | None = None, **job_kw):
+        self.width, self.height = width, height
+        self.ctx = ctx or Context()
+        self.job_kw = job_kw
+        self.scene = None
+        self.job = None
+        self.camera = None
+        self.frame_count = 1.0  # CImage frame count starts at 1 (CDeviceGI.java:325-328)
+        self._thread = None
+        self._run = threading.Event()
+        self._stop = threading.Event()
+        self.seed_source = np.random.default_rng()
+
+    # RayDeviceInterface.set(mesh, bvhBuild)
+    def set(self, scene: Scene, nodes: np.ndarray | None = None, bounds: np.ndarray | None = None):
+        self.scene = scene
+        if nodes is not None:
+            scene.import_bvh(nodes, bounds)
+
+    # CDeviceGI.setup(w, h)
+    def setup(self, width: int, height: int):
+        self.width, self.height = width, height
+        if self.job:
+            self.job.close()
+        self.job = Job(self.ctx, self.scene, width, height, **self.job_kw)
+        if self.camera is not None:
+            self.job.set_camera(self.camera)
+
+    def update_camera(self, camera: np.ndarray):
+        cam = camera.copy()
+        cam["dimension"] = (self.width, self.height)
+        self.camera = cam
+        if self.job:
+            self.job.set_camera(cam)
+
+    def _seeds(self):
+        cfg = self.job.cfg
+        if cfg.mode != 0:
+            return None
+        # allocateState: two random 30-bit primes per call (CDeviceGI.java:364-376); any odd 30-bit
+        # values serve the RNG, so odd draws stand in for the primes
+        n = 2 * (1 + 2 * cfg.max_depth) * cfg.spp
+        return (self.seed_source.integers(2 ** 29, 2 ** 30, size=n) | 1).astype(np.int32)
+
+    def execute(self):
+        self.job.render(self._seeds(), self.frame_count)
+        self.frame_count += self.job.cfg.spp
+
+    def update_image(self, resolve: bool = True) -> np.ndarray:
+        return self.job.film(resolve=resolve)
+
+    def start(self):
+        self._stop.clear()
+        self._run.set()
+
+        def loop():
+            while not self._stop.is_set():
+                if not self._run.wait(timeout=0.05):
+                    continue
+                self.execute()
+                self.ctx.finish()
+
+        self._thread = threading.Thread(target=loop, daemon=True)
+        self._thread.start()
+
+    def pause(self):
+        self._run.clear()
+
+    def resume(self):
+        self._run.set()
+
+    def is_paused(self) -> bool:
+        return not self._run.is_set()
+
+    def stop(self):
+        self._stop.set()
+        self._run.set()
+        if self._thread:
+            self._thread.join()
+            self._thread = None

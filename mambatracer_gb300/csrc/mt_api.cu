@@ -1,0 +1,1220 @@
+// C-ABI of the GB300 wavefront path tracer (see include/mambatracer.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mambatracer.h"
+#include "mt_common.h"
+#include "mt_device.cuh"
+#include "mt_kernels.h"
+
+using namespace mt;
+
+// ------------------------------------------------------------------ errors
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+#define CU(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) return fail(MT_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(MT_ERR_NOMEM, "cudaMalloc(%zu B): %s", count * sizeof(T), cudaGetErrorString(e));
+  }
+  return MT_OK;
+}
+template <class T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+}  // namespace
+
+// ----------------------------------------------------------------- structs
+struct mt_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::recursive_mutex mu;
+  int* d_scratch = nullptr;  // [0] work counter, [1] error for ray queries
+  cudaEvent_t ev[8] = {};
+};
+
+struct mt_buffer {
+  mt_context* ctx;
+  void* ptr;
+  size_t bytes;
+};
+
+struct mt_scene {
+  mt_context* ctx;
+  int npoints = 0, nuvs = 0, nnormals = 0, ntri = 0, nmat = 0;
+  std::vector<float> h_points;
+  std::vector<int32_t> h_faces;
+  std::vector<uint8_t> h_materials;
+  float4* d_points = nullptr;
+  float2* d_uvs = nullptr;
+  float4* d_normals = nullptr;
+  Face* d_faces = nullptr;
+  Material* d_materials = nullptr;
+  int* d_light_faces = nullptr;
+  int nlights = 0;
+  // traversal layout
+  float4* d_nodes = nullptr;
+  float4* d_tris = nullptr;
+  int nrec = 0, root_ref = 0, depth = 0, has_bvh = 0, precision = 0;
+  // environment
+  float4* d_env_rgb = nullptr;
+  float* d_env_lum = nullptr;
+  float* d_env_sat = nullptr;
+  double* d_env_sat64 = nullptr;
+  int env_w = 0, env_h = 0, env_present = 0;
+  int grid_nu = 1600, grid_nv = 1600, grid_rx = 16, grid_ry = 32, grid_on = 0;
+
+  DevScene view() const {
+    DevScene s{};
+    s.nodes = d_nodes;
+    s.qnodes = nullptr;
+    s.tris = d_tris;
+    s.root_ref = root_ref;
+    s.ntri = ntri;
+    s.nrec = nrec;
+    s.precision = precision;
+    s.points = d_points;
+    s.uvs = d_uvs;
+    s.normals = d_normals;
+    s.faces = d_faces;
+    s.materials = d_materials;
+    s.light_faces = d_light_faces;
+    s.nlights = nlights;
+    return s;
+  }
+  DevEnv env_view() const {
+    DevEnv e{};
+    e.rgb = d_env_rgb;
+    e.lum = d_env_lum;
+    e.sat = d_env_sat;
+    e.w = env_w;
+    e.h = env_h;
+    e.present = env_present;
+    e.grid_on = 0;
+    return e;
+  }
+};
+
+struct mt_job {
+  mt_context* ctx;
+  mt_scene* scene;
+  mt_render_config cfg;
+  FrameBufs fb{};
+  Ctrl* d_ctrl = nullptr;  // one per pass
+  unsigned long long* d_status = nullptr;
+  size_t status_stride = 0;
+  PassParams* h_pp = nullptr;  // pinned, 2 sets of one per pass (alternating frames)
+  PassParams* d_pp = nullptr;  // 2 sets of one per pass
+  unsigned char camera[64];
+  int has_camera = 0;
+  double frames = 0;  // passes accumulated in the film
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t done[2] = {nullptr, nullptr};  // frame completion per parameter set
+  int slot = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  std::vector<cudaEvent_t> kev;  // profile: 2 + 3 * max_depth per pass
+  unsigned long long* d_totals = nullptr;  // running [primary, extension, shadow, error]
+  std::vector<Ctrl> h_ctrl;
+};
+
+// ------------------------------------------------------------------ context
+extern "C" const char* mt_last_error(void) { return g_err.c_str(); }
+
+extern "C" const char* mt_version(void) {
+  return "mambatracer-gb300 sm_103a fmad=false prec-div prec-sqrt";
+}
+
+extern "C" int mt_ctx_create(int device, mt_context** out) {
+  if (!out) return fail(MT_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int n = 0;
+  CU(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return fail(MT_ERR_INVALID, "device %d of %d", device, n);
+  CU(cudaSetDevice(device));
+  auto* c = new mt_context();
+  c->device = device;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(MT_ERR_CUDA, "cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+  }
+  c->num_sms = prop.multiProcessorCount;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(MT_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  if (dalloc(&c->d_scratch, 4) != MT_OK) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return MT_ERR_NOMEM;
+  }
+  for (auto& ev : c->ev) cudaEventCreate(&ev);
+  *out = c;
+  return MT_OK;
+}
+
+extern "C" int mt_ctx_destroy(mt_context* ctx) {
+  if (!ctx) return fail(MT_ERR_INVALID, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  dfree(ctx->d_scratch);
+  for (auto& ev : ctx->ev)
+    if (ev) cudaEventDestroy(ev);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return MT_OK;
+}
+
+extern "C" int mt_ctx_event_record(mt_context* ctx, int slot) {
+  if (!ctx || slot < 0 || slot >= 8) return fail(MT_ERR_INVALID, "bad event slot");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaEventRecord(ctx->ev[slot], ctx->stream));
+  return MT_OK;
+}
+
+extern "C" int mt_ctx_event_elapsed(mt_context* ctx, int a, int b, float* ms) {
+  if (!ctx || !ms || a < 0 || a >= 8 || b < 0 || b >= 8) return fail(MT_ERR_INVALID, "bad event slot");
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaEventSynchronize(ctx->ev[b]));
+  CU(cudaEventElapsedTime(ms, ctx->ev[a], ctx->ev[b]));
+  return MT_OK;
+}
+
+extern "C" int mt_finish(mt_context* ctx) {
+  if (!ctx) return fail(MT_ERR_INVALID, "ctx is NULL");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return MT_OK;
+}
+
+// ------------------------------------------------------------------ buffers
+extern "C" int mt_buf_alloc(mt_context* ctx, size_t bytes, mt_buffer** out) {
+  if (!ctx || !out) return fail(MT_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(MT_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  }
+  CU(cudaMemsetAsync(p, 0, bytes ? bytes : 1, ctx->stream));
+  *out = new mt_buffer{ctx, p, bytes};
+  return MT_OK;
+}
+
+extern "C" int mt_buf_create_from(mt_context* ctx, const void* host, size_t bytes, mt_buffer** out) {
+  int r = mt_buf_alloc(ctx, bytes, out);
+  if (r != MT_OK) return r;
+  return mt_buf_write(*out, 0, host, bytes);
+}
+
+extern "C" int mt_buf_write(mt_buffer* b, size_t off, const void* host, size_t bytes) {
+  if (!b || (!host && bytes)) return fail(MT_ERR_INVALID, "NULL argument");
+  if (off > b->bytes || bytes > b->bytes - off) return fail(MT_ERR_INVALID, "write [%zu,+%zu) past %zu B", off, bytes, b->bytes);
+  std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+  CU(cudaSetDevice(b->ctx->device));
+  CU(cudaMemcpyAsync((char*)b->ptr + off, host, bytes, cudaMemcpyHostToDevice, b->ctx->stream));
+  CU(cudaStreamSynchronize(b->ctx->stream));
+  return MT_OK;
+}
+
+extern "C" int mt_buf_read(mt_buffer* b, size_t off, void* host, size_t bytes) {
+  if (!b || (!host && bytes)) return fail(MT_ERR_INVALID, "NULL argument");
+  if (off > b->bytes || bytes > b->bytes - off) return fail(MT_ERR_INVALID, "read [%zu,+%zu) past %zu B", off, bytes, b->bytes);
+  std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+  CU(cudaSetDevice(b->ctx->device));
+  CU(cudaMemcpyAsync(host, (char*)b->ptr + off, bytes, cudaMemcpyDeviceToHost, b->ctx->stream));
+  CU(cudaStreamSynchronize(b->ctx->stream));
+  return MT_OK;
+}
+
+namespace {
+__global__ void k_fill32(uint32_t* p, uint32_t v, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+}  // namespace
+
+extern "C" int mt_buf_fill32(mt_buffer* b, uint32_t pattern, size_t off, size_t bytes) {
+  if (!b) return fail(MT_ERR_INVALID, "NULL buffer");
+  if ((off | bytes) & 3) return fail(MT_ERR_INVALID, "offset and size must be multiples of 4");
+  if (off > b->bytes || bytes > b->bytes - off) return fail(MT_ERR_INVALID, "fill past the end");
+  std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+  CU(cudaSetDevice(b->ctx->device));
+  size_t n = bytes / 4;
+  if (n) k_fill32<<<(unsigned)((n + 255) / 256), 256, 0, b->ctx->stream>>>((uint32_t*)((char*)b->ptr + off), pattern, n);
+  CU(cudaGetLastError());
+  return MT_OK;
+}
+
+extern "C" size_t mt_buf_size(const mt_buffer* b) { return b ? b->bytes : 0; }
+
+extern "C" int mt_buf_free(mt_buffer* b) {
+  if (!b) return fail(MT_ERR_INVALID, "NULL buffer");
+  {
+    std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    cudaFree(b->ptr);
+  }
+  delete b;
+  return MT_OK;
+}
+
+// ------------------------------------------------------------------- scene
+namespace {
+
+bool emitter_host(const Material& m) {
+  float s = m.emission_param.x;
+  float x = m.emission_color.x * s, y = m.emission_color.y * s, z = m.emission_color.z * s;
+  return (0.2989f * x + 0.5866f * y) + 0.1145f * z != 0.0f;
+}
+
+int upload_lights(mt_scene* s) {
+  // identifyMeshLights + prefix scan + prepareLightInfo (CLightConfiguration.java:43-87):
+  // the faces whose material emits, in face order.
+  std::vector<int> lf;
+  const Face* F = reinterpret_cast<const Face*>(s->h_faces.data());
+  const Material* M = reinterpret_cast<const Material*>(s->h_materials.data());
+  for (int i = 0; i < s->ntri; ++i) {
+    int m = F[i].mat & 0xFFFF;
+    if (emitter_host(M[m])) lf.push_back(i);
+  }
+  dfree(s->d_light_faces);
+  s->nlights = (int)lf.size();
+  int r = dalloc(&s->d_light_faces, lf.size());
+  if (r) return r;
+  if (!lf.empty()) CU(cudaMemcpy(s->d_light_faces, lf.data(), lf.size() * 4, cudaMemcpyHostToDevice));
+  return MT_OK;
+}
+
+template <class T>
+int upload(T** d, const void* h, size_t count) {
+  dfree(*d);
+  int r = dalloc(d, count);
+  if (r) return r;
+  if (h && count) CU(cudaMemcpy(*d, h, count * sizeof(T), cudaMemcpyHostToDevice));
+  return MT_OK;
+}
+
+void free_scene(mt_scene* s) {
+  dfree(s->d_points);
+  dfree(s->d_uvs);
+  dfree(s->d_normals);
+  dfree(s->d_faces);
+  dfree(s->d_materials);
+  dfree(s->d_light_faces);
+  dfree(s->d_nodes);
+  dfree(s->d_tris);
+  dfree(s->d_env_rgb);
+  dfree(s->d_env_lum);
+  dfree(s->d_env_sat);
+  dfree(s->d_env_sat64);
+}
+
+}  // namespace
+
+extern "C" int mt_scene_create(mt_context* ctx, const float* points, int npoints, const float* uvs, int nuvs,
+                               const float* normals, int nnormals, const int32_t* faces, int nfaces,
+                               const void* materials, int nmaterials, mt_scene** out) {
+  if (!ctx || !out || !points || !faces || !materials) return fail(MT_ERR_INVALID, "NULL argument");
+  if (npoints <= 0 || nfaces <= 0 || nmaterials <= 0) return fail(MT_ERR_INVALID, "empty scene");
+  if (nmaterials > 65536) return fail(MT_ERR_INVALID, "more than 65536 materials (16-bit material index)");
+  *out = nullptr;
+  const Face* F = reinterpret_cast<const Face*>(faces);
+  for (int i = 0; i < nfaces; ++i) {
+    const Face& f = F[i];
+    if (f.vx < 0 || f.vy < 0 || f.vz < 0 || f.vx >= npoints || f.vy >= npoints || f.vz >= npoints)
+      return fail(MT_ERR_INVALID, "face %d: vertex index out of range", i);
+    if ((f.mat & 0xFFFF) >= nmaterials) return fail(MT_ERR_INVALID, "face %d: material %d of %d", i, f.mat & 0xFFFF, nmaterials);
+    if (f.uvx > -1 && (!uvs || f.uvx >= nuvs || f.uvy < 0 || f.uvy >= nuvs || f.uvz < 0 || f.uvz >= nuvs))
+      return fail(MT_ERR_INVALID, "face %d: uv index out of range", i);
+    if (f.nx > -1 && (!normals || f.nx >= nnormals || f.ny < 0 || f.ny >= nnormals || f.nz < 0 || f.nz >= nnormals))
+      return fail(MT_ERR_INVALID, "face %d: normal index out of range", i);
+  }
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  auto* s = new mt_scene();
+  s->ctx = ctx;
+  s->npoints = npoints;
+  s->nuvs = nuvs;
+  s->nnormals = nnormals;
+  s->ntri = nfaces;
+  s->nmat = nmaterials;
+  s->h_points.assign(points, points + 4 * (size_t)npoints);
+  s->h_faces.assign(faces, faces + 10 * (size_t)nfaces);
+  s->h_materials.assign((const uint8_t*)materials, (const uint8_t*)materials + 144 * (size_t)nmaterials);
+  int r = upload(&s->d_points, points, (size_t)npoints);
+  if (!r) r = upload(&s->d_uvs, uvs, uvs ? (size_t)nuvs : 1);
+  if (!r) r = upload(&s->d_normals, normals, normals ? (size_t)nnormals : 1);
+  if (!r) r = upload(&s->d_faces, faces, (size_t)nfaces);
+  if (!r) r = upload(&s->d_materials, materials, (size_t)nmaterials);
+  if (!r) r = upload_lights(s);
+  if (r) {
+    std::string keep = g_err;
+    free_scene(s);
+    delete s;
+    g_err = keep;
+    return r;
+  }
+  *out = s;
+  return MT_OK;
+}
+
+extern "C" int mt_scene_set_materials(mt_scene* s, const void* materials, int nmaterials) {
+  if (!s || !materials || nmaterials <= 0) return fail(MT_ERR_INVALID, "bad argument");
+  const Face* F = reinterpret_cast<const Face*>(s->h_faces.data());
+  for (int i = 0; i < s->ntri; ++i)
+    if ((F[i].mat & 0xFFFF) >= nmaterials) return fail(MT_ERR_INVALID, "face %d needs material %d", i, F[i].mat & 0xFFFF);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  CU(cudaStreamSynchronize(s->ctx->stream));
+  s->h_materials.assign((const uint8_t*)materials, (const uint8_t*)materials + 144 * (size_t)nmaterials);
+  s->nmat = nmaterials;
+  int r = upload(&s->d_materials, materials, (size_t)nmaterials);
+  if (!r) r = upload_lights(s);
+  return r;
+}
+
+extern "C" int mt_scene_light_count(const mt_scene* s) { return s ? s->nlights : -1; }
+
+extern "C" int mt_scene_destroy(mt_scene* s) {
+  if (!s) return fail(MT_ERR_INVALID, "NULL scene");
+  {
+    std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    free_scene(s);
+  }
+  delete s;
+  return MT_OK;
+}
+
+// ---------------------------------------------------------------- BVH build
+// CNormalBVH.build (src/cl/scene/CNormalBVH.java:45-148): recursive split at the
+// centre of the centroid bound's longest axis, one triangle per leaf, children
+// allocated as adjacent pairs in preorder, node.bound = node index. The
+// partition (CNormalBVH.java:132) is an un-vendored library routine; this build
+// uses a stable split "centroid[dim] < split", falling back to the middle index
+// when one side would be empty (CNormalBVH.java:135-136).
+namespace {
+struct Builder {
+  const float* pts;
+  const Face* faces;
+  int n;
+  std::vector<int> obj, tmp;
+  std::vector<float> tb, cen;
+  int32_t* nodes;   // 7 per node
+  float* bounds;    // 8 per node
+  int ptr = 1, max_depth = 0;
+
+  void init() {
+    obj.resize(n);
+    tb.resize(6 * (size_t)n);
+    cen.resize(3 * (size_t)n);
+    for (int t = 0; t < n; ++t) {
+      obj[t] = t;
+      const Face& f = faces[t];
+      const float* p[3] = {pts + 4 * (size_t)f.vx, pts + 4 * (size_t)f.vy, pts + 4 * (size_t)f.vz};
+      for (int a = 0; a < 3; ++a) {
+        float lo = INFINITY, hi = -INFINITY;
+        for (int k = 0; k < 3; ++k) {
+          if (p[k][a] < lo) lo = p[k][a];
+          if (p[k][a] > hi) hi = p[k][a];
+        }
+        tb[6 * (size_t)t + a] = lo;
+        tb[6 * (size_t)t + 3 + a] = hi;
+        cen[3 * (size_t)t + a] = 0.5f * (lo + hi);
+      }
+    }
+  }
+  void subdivide(int parent, int start, int end, int depth) {
+    // iterative on the right child to bound the C++ stack on deep trees
+    for (;;) {
+      max_depth = std::max(max_depth, depth);
+      float bmn[3] = {INFINITY, INFINITY, INFINITY}, bmx[3] = {-INFINITY, -INFINITY, -INFINITY};
+      float cmn[3] = {INFINITY, INFINITY, INFINITY}, cmx[3] = {-INFINITY, -INFINITY, -INFINITY};
+      for (int p = start; p < end; ++p) {
+        int t = obj[p];
+        for (int a = 0; a < 3; ++a) {
+          float lo = tb[6 * (size_t)t + a], hi = tb[6 * (size_t)t + 3 + a], c = cen[3 * (size_t)t + a];
+          bmn[a] = std::min(bmn[a], lo);
+          bmx[a] = std::max(bmx[a], hi);
+          cmn[a] = std::min(cmn[a], c);
+          cmx[a] = std::max(cmx[a], c);
+        }
+      }
+      int32_t* nd = nodes + 7 * (size_t)parent;
+      float* bd = bounds + 8 * (size_t)parent;
+      nd[0] = parent;  // bound
+      for (int a = 0; a < 3; ++a) {
+        bd[a] = bmn[a];
+        bd[4 + a] = bmx[a];
+      }
+      bd[3] = bd[7] = 0.f;
+      if (end - start < 2) {
+        nd[6] = obj[start];  // child
+        nd[5] = 1;           // isLeaf
+        return;
+      }
+      int li = ptr++, ri = ptr++;
+      int32_t* ln = nodes + 7 * (size_t)li;
+      int32_t* rn = nodes + 7 * (size_t)ri;
+      std::memset(ln, 0, 28);
+      std::memset(rn, 0, 28);
+      ln[4] = parent;  // parent
+      rn[4] = parent;
+      ln[1] = ri;      // sibling
+      rn[1] = li;
+      nd[2] = li;      // left
+      nd[3] = ri;      // right
+      float ex = cmx[0] - cmn[0], ey = cmx[1] - cmn[1], ez = cmx[2] - cmn[2];
+      int dim = (ex > ey && ex > ez) ? 0 : (ey > ez ? 1 : 2);
+      float split = 0.5f * (cmn[dim] + cmx[dim]);
+      int nl = 0;
+      for (int p = start; p < end; ++p) nl += cen[3 * (size_t)obj[p] + dim] < split;
+      int mid = start + nl;
+      if (mid != start && mid != end) {
+        tmp.resize(end - start);
+        int a = start, b = 0;
+        for (int p = start; p < end; ++p) {
+          int t = obj[p];
+          if (cen[3 * (size_t)t + dim] < split) obj[a++] = t;
+          else tmp[b++] = t;
+        }
+        std::memcpy(obj.data() + mid, tmp.data(), sizeof(int) * (size_t)b);
+      } else {
+        mid = start + (end - start) / 2;
+      }
+      subdivide(li, start, mid, depth + 1);
+      parent = ri;
+      start = mid;
+      depth = depth + 1;
+    }
+  }
+};
+
+// Convert the reference node layout into the traversal layout and upload it.
+int import_bvh(mt_scene* s, const int32_t* nodes, const float* bounds, int nnodes) {
+  const int n = s->ntri;
+  if (nnodes != 2 * n - 1) return fail(MT_ERR_INVALID, "%d nodes for %d triangles (want 2N-1)", nnodes, n);
+  auto node = [&](int i) { return nodes + 7 * (size_t)i; };
+  // BFS over interior nodes for record numbering; DFS leaf order for triangle slots.
+  std::vector<int> rec(nnodes, -1), slot(nnodes, -1), level(nnodes, 0);
+  std::vector<int> order;
+  order.reserve(n);
+  const int32_t* root = node(0);
+  int max_level = 0;
+  if (!root[5]) {
+    std::deque<int> q;
+    q.push_back(0);
+    int k = 0;
+    std::vector<char> seen(nnodes, 0);
+    seen[0] = 1;
+    while (!q.empty()) {
+      int i = q.front();
+      q.pop_front();
+      rec[i] = k++;
+      const int32_t* nd = node(i);
+      for (int c : {nd[2], nd[3]}) {
+        if (c <= 0 || c >= nnodes || seen[c]) return fail(MT_ERR_INVALID, "node %d: bad child %d", i, c);
+        seen[c] = 1;
+        const int32_t* cn = node(c);
+        if (cn[0] < 0 || cn[0] >= nnodes) return fail(MT_ERR_INVALID, "node %d: bad bound index %d", c, cn[0]);
+        level[c] = level[i] + 1;
+        max_level = std::max(max_level, level[c]);
+        if (!cn[5]) q.push_back(c);
+        else if (cn[6] < 0 || cn[6] >= n) return fail(MT_ERR_INVALID, "leaf %d: bad triangle %d", c, cn[6]);
+      }
+    }
+    // DFS (left before right) for leaf slots
+    std::vector<int> st{0};
+    while (!st.empty()) {
+      int i = st.back();
+      st.pop_back();
+      const int32_t* nd = node(i);
+      if (nd[5]) {
+        slot[i] = (int)order.size();
+        order.push_back(nd[6]);
+        continue;
+      }
+      st.push_back(nd[3]);
+      st.push_back(nd[2]);
+    }
+  } else {
+    if (root[6] < 0 || root[6] >= n) return fail(MT_ERR_INVALID, "root leaf: bad triangle");
+    slot[0] = 0;
+    order.push_back(root[6]);
+  }
+  // Deferred-node stack depth needed <= tree depth; the reference's bitstack holds 64 levels.
+  if (max_level > kStackDepth) return fail(MT_ERR_DEPTH, "BVH depth %d exceeds %d", max_level, kStackDepth);
+  const int nrec = root[5] ? 0 : n - 1;
+  std::vector<float4> hn(4 * (size_t)std::max(nrec, 1));
+  auto ref_of = [&](int c) { return node(c)[5] ? ~slot[c] : rec[c]; };
+  for (int i = 0; i < nnodes; ++i) {
+    if (rec[i] < 0) continue;
+    const int32_t* nd = node(i);
+    const float* bl = bounds + 8 * (size_t)node(nd[2])[0];
+    const float* br = bounds + 8 * (size_t)node(nd[3])[0];
+    float4* r = hn.data() + 4 * (size_t)rec[i];
+    r[0] = make_float4(bl[0], bl[4], bl[1], bl[5]);
+    r[1] = make_float4(br[0], br[4], br[1], br[5]);
+    r[2] = make_float4(bl[2], bl[6], br[2], br[6]);
+    int lr = ref_of(nd[2]), rr = ref_of(nd[3]);
+    float lf, rf;
+    std::memcpy(&lf, &lr, 4);
+    std::memcpy(&rf, &rr, 4);
+    r[3] = make_float4(lf, rf, 0.f, 0.f);
+  }
+  if ((int)order.size() != n) return fail(MT_ERR_INVALID, "BVH reaches %zu of %d triangles", order.size(), n);
+  std::vector<float4> ht(3 * (size_t)n);
+  const Face* F = reinterpret_cast<const Face*>(s->h_faces.data());
+  const float* P = s->h_points.data();
+  for (int k = 0; k < n; ++k) {
+    int f = order[k];
+    const float* p1 = P + 4 * (size_t)F[f].vx;
+    const float* p2 = P + 4 * (size_t)F[f].vy;
+    const float* p3 = P + 4 * (size_t)F[f].vz;
+    float fid;
+    std::memcpy(&fid, &f, 4);
+    ht[3 * (size_t)k + 0] = make_float4(p1[0], p1[1], p1[2], fid);
+    ht[3 * (size_t)k + 1] = make_float4(p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2], 0.f);
+    ht[3 * (size_t)k + 2] = make_float4(p3[0] - p1[0], p3[1] - p1[1], p3[2] - p1[2], 0.f);
+  }
+  int r = upload(&s->d_nodes, hn.data(), hn.size());
+  if (!r) r = upload(&s->d_tris, ht.data(), ht.size());
+  if (r) return r;
+  s->nrec = nrec;
+  s->root_ref = root[5] ? ~0 : 0;
+  s->depth = max_level;
+  s->has_bvh = 1;
+  return MT_OK;
+}
+}  // namespace
+
+extern "C" int mt_bvh_build(mt_scene* s, int32_t* nodes_out, float* bounds_out, int* depth_out) {
+  if (!s) return fail(MT_ERR_INVALID, "NULL scene");
+  const int n = s->ntri;
+  std::vector<int32_t> nodes(7 * (size_t)(2 * n - 1), 0);
+  std::vector<float> bounds(8 * (size_t)(2 * n - 1), 0.f);
+  Builder b;
+  b.pts = s->h_points.data();
+  b.faces = reinterpret_cast<const Face*>(s->h_faces.data());
+  b.n = n;
+  b.nodes = nodes.data();
+  b.bounds = bounds.data();
+  b.init();
+  b.subdivide(0, 0, n, 0);
+  if (nodes_out) std::memcpy(nodes_out, nodes.data(), nodes.size() * 4);
+  if (bounds_out) std::memcpy(bounds_out, bounds.data(), bounds.size() * 4);
+  if (depth_out) *depth_out = b.max_depth;
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  CU(cudaStreamSynchronize(s->ctx->stream));
+  return import_bvh(s, nodes.data(), bounds.data(), 2 * n - 1);
+}
+
+extern "C" int mt_bvh_build_host(const float* points, int npoints, const int32_t* faces, int nfaces,
+                                 int32_t* nodes_out, float* bounds_out, int* depth_out) {
+  if (!points || !faces || !nodes_out || !bounds_out || npoints <= 0 || nfaces <= 0)
+    return fail(MT_ERR_INVALID, "bad argument");
+  const Face* F = reinterpret_cast<const Face*>(faces);
+  for (int i = 0; i < nfaces; ++i)
+    if (F[i].vx < 0 || F[i].vy < 0 || F[i].vz < 0 || F[i].vx >= npoints || F[i].vy >= npoints || F[i].vz >= npoints)
+      return fail(MT_ERR_INVALID, "face %d: vertex index out of range", i);
+  std::memset(nodes_out, 0, 28 * (size_t)(2 * nfaces - 1));
+  std::memset(bounds_out, 0, 32 * (size_t)(2 * nfaces - 1));
+  Builder b;
+  b.pts = points;
+  b.faces = F;
+  b.n = nfaces;
+  b.nodes = nodes_out;
+  b.bounds = bounds_out;
+  b.init();
+  b.subdivide(0, 0, nfaces, 0);
+  if (depth_out) *depth_out = b.max_depth;
+  return MT_OK;
+}
+
+extern "C" int mt_bvh_import(mt_scene* s, const int32_t* nodes, const float* bounds, int nnodes) {
+  if (!s || !nodes || !bounds) return fail(MT_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  CU(cudaStreamSynchronize(s->ctx->stream));
+  return import_bvh(s, nodes, bounds, nnodes);
+}
+
+extern "C" int mt_scene_set_bvh_precision(mt_scene* s, int precision) {
+  if (!s) return fail(MT_ERR_INVALID, "NULL scene");
+  if (precision != 0) return fail(MT_ERR_INVALID, "BVH precision %d is not available in this build", precision);
+  s->precision = precision;
+  return MT_OK;
+}
+
+// -------------------------------------------------------------- environment
+extern "C" int mt_env_set(mt_scene* s, const float* rgb, int w, int h) {
+  if (!s || !rgb || w <= 0 || h <= 0) return fail(MT_ERR_INVALID, "bad environment map");
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  CU(cudaStreamSynchronize(s->ctx->stream));
+  size_t n = (size_t)w * h;
+  int r = upload(&s->d_env_rgb, rgb, n);
+  if (!r) { dfree(s->d_env_lum); r = dalloc(&s->d_env_lum, n); }
+  if (!r) { dfree(s->d_env_sat); r = dalloc(&s->d_env_sat, n); }
+  if (!r) { dfree(s->d_env_sat64); r = dalloc(&s->d_env_sat64, n); }
+  if (r) return r;
+  if (launch_env_build(s->ctx->stream, s->d_env_rgb, w, h, s->d_env_lum, s->d_env_sat64, s->d_env_sat))
+    return fail(MT_ERR_CUDA, "environment build launch: %s", cudaGetErrorString(cudaGetLastError()));
+  CU(cudaStreamSynchronize(s->ctx->stream));
+  s->env_w = w;
+  s->env_h = h;
+  s->env_present = 1;
+  return MT_OK;
+}
+
+extern "C" int mt_env_set_with_sat(mt_scene* s, const float* rgb, const float* lum, const float* sat, int w, int h) {
+  if (!s || !rgb || !lum || !sat || w <= 0 || h <= 0) return fail(MT_ERR_INVALID, "bad environment map");
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  CU(cudaStreamSynchronize(s->ctx->stream));
+  size_t n = (size_t)w * h;
+  int r = upload(&s->d_env_rgb, rgb, n);
+  if (!r) r = upload(&s->d_env_lum, lum, n);
+  if (!r) r = upload(&s->d_env_sat, sat, n);
+  if (r) return r;
+  dfree(s->d_env_sat64);
+  s->env_w = w;
+  s->env_h = h;
+  s->env_present = 1;
+  return MT_OK;
+}
+
+extern "C" int mt_env_clear(mt_scene* s) {
+  if (!s) return fail(MT_ERR_INVALID, "NULL scene");
+  s->env_present = 0;
+  return MT_OK;
+}
+
+extern "C" int mt_env_read(mt_scene* s, float* lum, double* sat64, float* sat32) {
+  if (!s || !s->env_present) return fail(MT_ERR_INVALID, "no environment map");
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  CU(cudaStreamSynchronize(s->ctx->stream));
+  size_t n = (size_t)s->env_w * s->env_h;
+  if (lum) CU(cudaMemcpy(lum, s->d_env_lum, n * 4, cudaMemcpyDeviceToHost));
+  if (sat32) CU(cudaMemcpy(sat32, s->d_env_sat, n * 4, cudaMemcpyDeviceToHost));
+  if (sat64) {
+    if (!s->d_env_sat64) return fail(MT_ERR_INVALID, "the SAT was given, not built in FP64");
+    CU(cudaMemcpy(sat64, s->d_env_sat64, n * 8, cudaMemcpyDeviceToHost));
+  }
+  return MT_OK;
+}
+
+extern "C" int mt_env_grid_config(mt_scene* s, int nu, int nv, int rx, int ry, int enable) {
+  if (!s || nu <= 0 || nv <= 0 || rx <= 0 || ry <= 0 || nu % rx || nv % ry) return fail(MT_ERR_INVALID, "bad grid");
+  s->grid_nu = nu;
+  s->grid_nv = nv;
+  s->grid_rx = rx;
+  s->grid_ry = ry;
+  s->grid_on = enable;
+  return MT_OK;
+}
+
+extern "C" int mt_env_grid_sat(mt_context* ctx, const float* func, float* sat_out, int nu, int nv, int rx, int ry,
+                               int fp64) {
+  if (!ctx || !func || !sat_out || nu <= 0 || nv <= 0) return fail(MT_ERR_INVALID, "bad argument");
+  if (!((rx == 8 || rx == 16 || rx == 32) && (ry == 8 || ry == 16 || ry == 32)) || nu % rx || nv % ry)
+    return fail(MT_ERR_INVALID, "tiles per cell must be 8, 16 or 32 and divide the grid");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  size_t n = (size_t)nu * nv;
+  float *d_func = nullptr, *d_sat = nullptr;
+  double* d_sat64 = nullptr;
+  int r = dalloc(&d_func, n);
+  if (!r) r = dalloc(&d_sat, n);
+  if (!r && fp64) r = dalloc(&d_sat64, n);
+  if (!r) {
+    cudaMemcpyAsync(d_func, func, n * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (launch_grid_sat(ctx->stream, d_func, d_sat, d_sat64, nu, nv, rx, ry, fp64))
+      r = fail(MT_ERR_CUDA, "grid SAT launch failed");
+    else if (cudaMemcpyAsync(sat_out, d_sat, n * 4, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+             cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      r = fail(MT_ERR_CUDA, "grid SAT copy: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  dfree(d_func);
+  dfree(d_sat);
+  dfree(d_sat64);
+  return r;
+}
+
+// -------------------------------------------------------------------- jobs
+namespace {
+
+struct CamF {
+  float position[4], lookat[4], up[4], dimension[2], fov, pad;
+};
+
+// Camera constants of InitCameraRayDataJitter (Initialize.cl:129-172) and
+// camera_transform (Matrix.cl:216-241), computed once per pass on the host in
+// FP32 with the reference's operation order.
+void camera_constants(const CamF& c, int W, int H, PassParams& pp) {
+  auto dot4 = [](const float* a, const float* b) { return ((a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]) + a[3] * b[3]; };
+  auto norm4 = [&](float* v) {
+    float l = std::sqrt(dot4(v, v));
+    for (int i = 0; i < 4; ++i) v[i] = v[i] / l;
+  };
+  auto cross4 = [](const float* a, const float* b, float* o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+    o[3] = 0.f;
+  };
+  float d[4], r[4], u[4];
+  for (int i = 0; i < 4; ++i) d[i] = c.lookat[i] - c.position[i];
+  norm4(d);
+  cross4(d, c.up, r);
+  norm4(r);
+  cross4(r, d, u);
+  float eInv[4][4] = {{1, 0, 0, c.position[0]}, {0, 1, 0, c.position[1]}, {0, 0, 1, c.position[2]}, {0, 0, 0, 1}};
+  float nd[4] = {d[0] * -1.f, d[1] * -1.f, d[2] * -1.f, d[3] * -1.f};
+  float v2w[4][4];
+  for (int row = 0; row < 4; ++row) {
+    v2w[row][0] = r[row];
+    v2w[row][1] = u[row];
+    v2w[row][2] = nd[row];
+    v2w[row][3] = row == 3 ? 1.f : 0.f;
+  }
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      float col[4] = {v2w[0][j], v2w[1][j], v2w[2][j], v2w[3][j]};
+      pp.cam_m[4 * i + j] = dot4(eInv[i], col);
+    }
+  float dimx = (float)W, dimy = (float)H;
+  float fov_rad = c.fov * 0.017453292519943295f;
+  pp.cam_d = 1.f / std::tan(fov_rad / 2.f);
+  pp.cam_a = dimx / dimy;
+  pp.inv_w = 1.f / dimx;
+  pp.inv_h = 1.f / dimy;
+  pp.dim_w = dimx;
+  pp.dim_h = dimy;
+}
+
+void free_job(mt_job* j) {
+  for (int k = 0; k < 2; ++k) {
+    dfree(j->fb.q_o[k]);
+    dfree(j->fb.q_d[k]);
+  }
+  dfree(j->fb.hit_t);
+  dfree(j->fb.hit_prim);
+  dfree(j->fb.thr);
+  dfree(j->fb.ps);
+  dfree(j->fb.flag);
+  dfree(j->fb.s_o);
+  dfree(j->fb.s_d);
+  dfree(j->fb.s_c);
+  dfree(j->fb.film);
+  dfree(j->fb.film_c);
+  dfree(j->d_ctrl);
+  dfree(j->d_totals);
+  dfree(j->d_status);
+  dfree(j->d_pp);
+  if (j->h_pp) cudaFreeHost(j->h_pp);
+  j->h_pp = nullptr;
+  for (auto& g : j->graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  for (cudaEvent_t* e : {&j->ev0, &j->ev1, &j->done[0], &j->done[1]}) {
+    if (*e) cudaEventDestroy(*e);
+    *e = nullptr;
+  }
+  for (auto& e : j->kev)
+    if (e) cudaEventDestroy(e);
+  j->kev.clear();
+}
+
+int check_cfg(const mt_render_config* c) {
+  if (!c) return fail(MT_ERR_INVALID, "NULL config");
+  if (c->width <= 0 || c->height <= 0 || (long long)c->width * c->height > (1ll << 30))
+    return fail(MT_ERR_INVALID, "resolution %dx%d", c->width, c->height);
+  if (c->max_depth < 1 || c->max_depth > kMaxDepth) return fail(MT_ERR_INVALID, "max_depth %d (1..%d)", c->max_depth, kMaxDepth);
+  if (c->mode != 0 && c->mode != 1) return fail(MT_ERR_INVALID, "mode %d", c->mode);
+  if (c->spp < 1 || c->spp > 4096) return fail(MT_ERR_INVALID, "spp %d", c->spp);
+  return MT_OK;
+}
+
+}  // namespace
+
+extern "C" int mt_job_create(mt_context* ctx, mt_scene* scene, const mt_render_config* cfg, mt_job** out) {
+  if (!ctx || !scene || !out) return fail(MT_ERR_INVALID, "NULL argument");
+  int r = check_cfg(cfg);
+  if (r) return r;
+  if (!scene->has_bvh) return fail(MT_ERR_INVALID, "scene has no BVH (mt_bvh_build / mt_bvh_import)");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  auto* j = new mt_job();
+  j->ctx = ctx;
+  j->scene = scene;
+  j->cfg = *cfg;
+  const size_t N = (size_t)cfg->width * cfg->height;
+  const int spp = cfg->spp;
+  for (int k = 0; k < 2 && !r; ++k) {
+    r = dalloc(&j->fb.q_o[k], N);
+    if (!r) r = dalloc(&j->fb.q_d[k], N);
+  }
+  if (!r) r = dalloc(&j->fb.hit_t, N);
+  if (!r) r = dalloc(&j->fb.hit_prim, N);
+  if (!r) r = dalloc(&j->fb.thr, N);
+  if (!r) r = dalloc(&j->fb.ps, N);
+  if (!r) r = dalloc(&j->fb.flag, N);
+  if (!r) r = dalloc(&j->fb.s_o, N);
+  if (!r) r = dalloc(&j->fb.s_d, N);
+  if (!r) r = dalloc(&j->fb.s_c, N);
+  if (!r) r = dalloc(&j->fb.film, N);
+  if (!r) r = dalloc(&j->fb.film_c, N);
+  if (!r) r = dalloc(&j->d_ctrl, (size_t)spp);
+  if (!r) r = dalloc(&j->d_totals, 4);
+  j->status_stride = (N + kShadeThreads - 1) / kShadeThreads;
+  if (!r) r = dalloc(&j->d_status, j->status_stride * (size_t)cfg->max_depth * spp);
+  if (!r) r = dalloc(&j->d_pp, 2 * (size_t)spp);
+  if (!r && cudaMallocHost((void**)&j->h_pp, sizeof(PassParams) * 2 * spp) != cudaSuccess)
+    r = fail(MT_ERR_NOMEM, "pinned pass parameters");
+  if (!r && (cudaEventCreate(&j->ev0) != cudaSuccess || cudaEventCreate(&j->ev1) != cudaSuccess ||
+             cudaEventCreate(&j->done[0]) != cudaSuccess || cudaEventCreate(&j->done[1]) != cudaSuccess))
+    r = fail(MT_ERR_CUDA, "event create");
+  if (!r && cfg->profile) {
+    j->kev.resize((size_t)spp * (2 + 3 * cfg->max_depth));
+    for (auto& e : j->kev)
+      if (cudaEventCreate(&e) != cudaSuccess) r = fail(MT_ERR_CUDA, "event create");
+  }
+  if (r) {
+    std::string keep = g_err;
+    free_job(j);
+    delete j;
+    g_err = keep;
+    return r;
+  }
+  std::memset(j->h_pp, 0, sizeof(PassParams) * 2 * spp);
+  j->h_ctrl.resize(spp);
+  cudaMemsetAsync(j->fb.film, 0, N * 16, ctx->stream);
+  cudaMemsetAsync(j->fb.film_c, 0, N * 16, ctx->stream);
+  cudaMemsetAsync(j->d_totals, 0, 32, ctx->stream);
+  CU(cudaStreamSynchronize(ctx->stream));
+  *out = j;
+  return MT_OK;
+}
+
+extern "C" int mt_job_destroy(mt_job* j) {
+  if (!j) return fail(MT_ERR_INVALID, "NULL job");
+  {
+    std::lock_guard<std::recursive_mutex> lk(j->ctx->mu);
+    cudaSetDevice(j->ctx->device);
+    cudaStreamSynchronize(j->ctx->stream);
+    free_job(j);
+  }
+  delete j;
+  return MT_OK;
+}
+
+extern "C" int mt_job_set_camera(mt_job* j, const void* camera) {
+  if (!j || !camera) return fail(MT_ERR_INVALID, "NULL argument");
+  std::memcpy(j->camera, camera, 64);
+  j->has_camera = 1;
+  return MT_OK;
+}
+
+namespace {
+// Enqueue one frame's passes reading parameter set `slot`.
+int enqueue_frame(mt_job* j, int slot) {
+  mt_context* ctx = j->ctx;
+  const mt_render_config& c = j->cfg;
+  DevScene S = j->scene->view();
+  DevEnv E = j->scene->env_view();
+  PassParams* hp = j->h_pp + (size_t)slot * c.spp;
+  PassParams* dp = j->d_pp + (size_t)slot * c.spp;
+  const size_t per_pass_events = 2 + 3 * (size_t)c.max_depth;
+  for (int p = 0; p < c.spp; ++p) {
+    CU(cudaMemcpyAsync(dp + p, hp + p, sizeof(PassParams), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemsetAsync(j->d_ctrl + p, 0, sizeof(Ctrl), ctx->stream));
+    CU(cudaMemsetAsync(j->d_status + j->status_stride * (size_t)c.max_depth * p, 0,
+                       j->status_stride * (size_t)c.max_depth * 8, ctx->stream));
+    cudaEvent_t* ev = j->kev.empty() ? nullptr : j->kev.data() + per_pass_events * p;
+    if (launch_pass(ctx->stream, S, E, dp + p, c.mode, c.max_depth, c.film_kahan, c.width, c.height, j->d_ctrl + p,
+                    j->fb, j->d_status + j->status_stride * (size_t)c.max_depth * p, j->status_stride, ctx->num_sms,
+                    ev, j->d_totals))
+      return fail(MT_ERR_CUDA, "pass launch: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  return MT_OK;
+}
+}  // namespace
+
+extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_count) {
+  if (!j) return fail(MT_ERR_INVALID, "NULL job");
+  if (!j->has_camera) return fail(MT_ERR_INVALID, "camera not set (mt_job_set_camera)");
+  const mt_render_config& c = j->cfg;
+  if (c.mode == 0 && !seeds) return fail(MT_ERR_INVALID, "mode 0 needs the allocateState seed pairs");
+  mt_context* ctx = j->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  // Parameter sets alternate between frames; wait only until the frame that
+  // last read this set has finished, so consecutive frames stay queued.
+  const int slot = j->slot;
+  j->slot ^= 1;
+  CU(cudaEventSynchronize(j->done[slot]));
+  CamF cam;
+  std::memcpy(&cam, j->camera, 64);
+  const int per_pass = 2 * (1 + 2 * c.max_depth);
+  for (int p = 0; p < c.spp; ++p) {
+    PassParams& pp = j->h_pp[(size_t)slot * c.spp + p];
+    camera_constants(cam, c.width, c.height, pp);
+    pp.frame_count = frame_count + (float)p;
+    pp.width = c.width;
+    pp.height = c.height;
+    pp.max_depth = c.max_depth;
+    pp.mode = c.mode;
+    pp.rr_depth = c.rr_depth;
+    pp.kahan = c.film_kahan;
+    if (c.mode == 0) std::memcpy(pp.seeds, seeds + (size_t)per_pass * p, sizeof(int32_t) * per_pass);
+  }
+  CU(cudaEventRecord(j->ev0, ctx->stream));
+  if (c.use_graph && !c.profile) {
+    if (!j->graph[slot]) {
+      cudaGraph_t g;
+      CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      int r = enqueue_frame(j, slot);
+      cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+      if (r) return r;
+      if (e != cudaSuccess) return fail(MT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&j->graph[slot], g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return fail(MT_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+    CU(cudaGraphLaunch(j->graph[slot], ctx->stream));
+  } else {
+    int r = enqueue_frame(j, slot);
+    if (r) return r;
+  }
+  CU(cudaEventRecord(j->ev1, ctx->stream));
+  CU(cudaEventRecord(j->done[slot], ctx->stream));
+  j->frames += c.spp;
+  return MT_OK;
+}
+
+extern "C" int mt_job_last_ms(mt_job* j, float* ms) {
+  if (!j || !ms) return fail(MT_ERR_INVALID, "NULL argument");
+  CU(cudaEventSynchronize(j->ev1));
+  CU(cudaEventElapsedTime(ms, j->ev0, j->ev1));
+  return MT_OK;
+}
+
+extern "C" int mt_job_total_rays(mt_job* j, int64_t* rays3) {
+  if (!j || !rays3) return fail(MT_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::recursive_mutex> lk(j->ctx->mu);
+  CU(cudaSetDevice(j->ctx->device));
+  unsigned long long t[4];
+  CU(cudaMemcpyAsync(t, j->d_totals, 32, cudaMemcpyDeviceToHost, j->ctx->stream));
+  CU(cudaStreamSynchronize(j->ctx->stream));
+  for (int k = 0; k < 3; ++k) rays3[k] = (int64_t)t[k];
+  if (t[3]) return fail(MT_ERR_DEVICE, "device error %llu latched", t[3]);
+  return MT_OK;
+}
+
+extern "C" int mt_job_kernel_ms(mt_job* j, float* ms) {
+  if (!j || !ms) return fail(MT_ERR_INVALID, "NULL argument");
+  if (j->kev.empty()) return fail(MT_ERR_INVALID, "job was not created with profile = 1");
+  CU(cudaEventSynchronize(j->ev1));
+  const mt_render_config& c = j->cfg;
+  const size_t per = 2 + 3 * (size_t)c.max_depth;
+  for (int p = 0; p < c.spp; ++p)
+    for (size_t k = 0; k + 1 < per; ++k)
+      CU(cudaEventElapsedTime(ms + (size_t)p * (per - 1) + k, j->kev[p * per + k], j->kev[p * per + k + 1]));
+  return MT_OK;
+}
+
+extern "C" int mt_job_stats(mt_job* j, int64_t* rays3, int32_t* counts) {
+  if (!j) return fail(MT_ERR_INVALID, "NULL job");
+  std::lock_guard<std::recursive_mutex> lk(j->ctx->mu);
+  CU(cudaSetDevice(j->ctx->device));
+  CU(cudaStreamSynchronize(j->ctx->stream));
+  const mt_render_config& c = j->cfg;
+  CU(cudaMemcpy(j->h_ctrl.data(), j->d_ctrl, sizeof(Ctrl) * c.spp, cudaMemcpyDeviceToHost));
+  int64_t prim = 0, ext = 0, sh = 0;
+  int err = 0;
+  for (int p = 0; p < c.spp; ++p) {
+    const Ctrl& k = j->h_ctrl[p];
+    prim += (int64_t)c.width * c.height;
+    for (int b = 2; b <= c.max_depth; ++b) ext += k.count[b];
+    sh += (int64_t)k.rays[2];
+    if (k.error) err = k.error;
+  }
+  if (rays3) {
+    rays3[0] = prim;
+    rays3[1] = ext;
+    rays3[2] = sh;
+  }
+  if (counts) {
+    const Ctrl& k = j->h_ctrl[c.spp - 1];
+    for (int b = 1; b <= c.max_depth; ++b) counts[b - 1] = k.count[b + 1];
+  }
+  if (err) return fail(MT_ERR_DEVICE, "device error %d latched during the frame", err);
+  return MT_OK;
+}
+
+extern "C" int mt_film_read(mt_job* j, float* rgba, int resolve) {
+  if (!j || !rgba) return fail(MT_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::recursive_mutex> lk(j->ctx->mu);
+  CU(cudaSetDevice(j->ctx->device));
+  const size_t N = (size_t)j->cfg.width * j->cfg.height;
+  CU(cudaMemcpyAsync(rgba, j->fb.film, N * 16, cudaMemcpyDeviceToHost, j->ctx->stream));
+  CU(cudaStreamSynchronize(j->ctx->stream));
+  if (resolve && j->frames > 0) {
+    // averageAccum (Image.cl:84-122): accum.xyz / frameCount, w = 1
+    float fc = (float)j->frames;
+    for (size_t i = 0; i < N; ++i) {
+      rgba[4 * i + 0] = rgba[4 * i + 0] / fc;
+      rgba[4 * i + 1] = rgba[4 * i + 1] / fc;
+      rgba[4 * i + 2] = rgba[4 * i + 2] / fc;
+      rgba[4 * i + 3] = 1.f;
+    }
+  }
+  return MT_OK;
+}
+
+extern "C" int mt_film_clear(mt_job* j) {
+  if (!j) return fail(MT_ERR_INVALID, "NULL job");
+  std::lock_guard<std::recursive_mutex> lk(j->ctx->mu);
+  CU(cudaSetDevice(j->ctx->device));
+  const size_t N = (size_t)j->cfg.width * j->cfg.height;
+  CU(cudaMemsetAsync(j->fb.film, 0, N * 16, j->ctx->stream));
+  CU(cudaMemsetAsync(j->fb.film_c, 0, N * 16, j->ctx->stream));
+  CU(cudaMemsetAsync(j->d_totals, 0, 32, j->ctx->stream));
+  j->frames = 0;
+  return MT_OK;
+}
+
+// ------------------------------------------------------------- ray queries
+namespace {
+int query(mt_scene* s, const void* rays, int n, int any, float* t_out, int32_t* prim_out) {
+  if (!s || (!rays && n) || !prim_out || (!any && !t_out) || n < 0) return fail(MT_ERR_INVALID, "bad argument");
+  if (!s->has_bvh) return fail(MT_ERR_INVALID, "scene has no BVH");
+  if (n == 0) return MT_OK;
+  mt_context* ctx = s->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  float4* d_rays = nullptr;
+  float* d_t = nullptr;
+  int* d_p = nullptr;
+  int r = dalloc(&d_rays, 5 * (size_t)n);
+  if (!r) r = dalloc(&d_t, (size_t)n);
+  if (!r) r = dalloc(&d_p, (size_t)n);
+  if (!r) {
+    cudaMemcpyAsync(d_rays, rays, 80 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemsetAsync(ctx->d_scratch, 0, 8, ctx->stream);
+    if (launch_query(ctx->stream, s->view(), d_rays, n, any, d_t, d_p, ctx->d_scratch, ctx->d_scratch + 1, ctx->num_sms))
+      r = fail(MT_ERR_CUDA, "query launch: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  int err = 0;
+  if (!r) {
+    if (!any) cudaMemcpyAsync(t_out, d_t, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaMemcpyAsync(prim_out, d_p, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaMemcpyAsync(&err, ctx->d_scratch + 1, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) r = fail(MT_ERR_CUDA, "query: %s", cudaGetErrorString(e));
+    else if (err) r = fail(MT_ERR_DEVICE, "device error %d", err);
+  }
+  dfree(d_rays);
+  dfree(d_t);
+  dfree(d_p);
+  return r;
+}
+}  // namespace
+
+extern "C" int mt_trace_closest(mt_scene* s, const void* rays, int n, float* t_out, int32_t* prim_out) {
+  return query(s, rays, n, 0, t_out, prim_out);
+}
+
+extern "C" int mt_trace_any(mt_scene* s, const void* rays, int n, int32_t* occluded_out) {
+  return query(s, rays, n, 1, nullptr, occluded_out);
+}
+
+extern "C" int mt_trace_closest_dev(mt_scene* s, mt_buffer* rays, int n, mt_buffer* t_out, mt_buffer* prim_out,
+                                    float* ms_out) {
+  if (!s || !rays || !t_out || !prim_out || n < 0) return fail(MT_ERR_INVALID, "bad argument");
+  if (rays->bytes < 80 * (size_t)n || t_out->bytes < 4 * (size_t)n || prim_out->bytes < 4 * (size_t)n)
+    return fail(MT_ERR_INVALID, "buffers too small for %d rays", n);
+  mt_context* ctx = s->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  cudaMemsetAsync(ctx->d_scratch, 0, 8, ctx->stream);
+  cudaEventRecord(a, ctx->stream);
+  int r = launch_query(ctx->stream, s->view(), (const float4*)rays->ptr, n, 0, (float*)t_out->ptr, (int*)prim_out->ptr,
+                       ctx->d_scratch, ctx->d_scratch + 1, ctx->num_sms);
+  cudaEventRecord(b, ctx->stream);
+  cudaError_t e = cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (r || e != cudaSuccess) return fail(MT_ERR_CUDA, "trace: %s", cudaGetErrorString(cudaGetLastError()));
+  if (ms_out) *ms_out = ms;
+  return MT_OK;
+}
+
+// ------------------------------------------------- kernels by name (stubs)
+struct mt_kernel {
+  mt_context* ctx;
+  std::string name;
+};
+extern "C" const char* mt_kernel_names(void) { return ""; }
+extern "C" int mt_kernel_create(mt_context* ctx, const char* name, mt_kernel** out) {
+  (void)ctx;
+  (void)out;
+  return fail(MT_ERR_INVALID, "unknown kernel '%s'", name ? name : "(null)");
+}
+extern "C" int mt_kernel_set_arg_buf(mt_kernel* k, int, mt_buffer*) { return k ? MT_OK : fail(MT_ERR_INVALID, "NULL"); }
+extern "C" int mt_kernel_set_arg_local(mt_kernel* k, int, size_t) { return k ? MT_OK : fail(MT_ERR_INVALID, "NULL"); }
+extern "C" int mt_launch_1d(mt_kernel* k, size_t, size_t) { return k ? MT_OK : fail(MT_ERR_INVALID, "NULL"); }
+extern "C" int mt_kernel_destroy(mt_kernel* k) {
+  delete k;
+  return MT_OK;
+}

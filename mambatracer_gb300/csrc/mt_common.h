@@ -1,0 +1,104 @@
+// Shared host/device definitions of the GB300 wavefront path tracer.
+#pragma once
+#include <cstdint>
+
+#ifndef __CUDACC__
+#include <vector_types.h>
+#endif
+
+namespace mt {
+
+constexpr int kMaxDepth = 32;        // bounces per pass (reference: 15)
+constexpr int kStackDepth = 64;      // traversal stack = the reference's 64-bit bitstack
+constexpr int kTraceThreads = 128;   // threads per traversal CTA
+constexpr int kShadeThreads = 256;   // threads per shade CTA (one compaction tile)
+
+// Device error codes latched in Ctrl::error.
+constexpr int kDevErrLookback = 1;   // decoupled look-back wait expired
+constexpr int kDevErrStack = 2;      // traversal stack overflow (BVH deeper than 64)
+
+// Reference Face (src/cl/kernel/Util.cl:95-102).
+struct Face {
+  int vx, vy, vz, uvx, uvy, uvz, nx, ny, nz, mat;
+};
+
+// Reference SurfaceParameter (src/cl/kernel/Bsdf.cl:24-42), 144 B.
+struct Material {
+  int isDiffuseTexture, isGlossyTexture, isRoughnessTexture, isMirrorTexture;
+  float4 diffuse_color, diffuse_param, glossy_color, glossy_param;
+  float4 mirror_color, mirror_param, emission_color, emission_param;
+};
+static_assert(sizeof(Material) == 144, "Material layout");
+
+// Scene as seen by kernels. Traversal data is the GPU layout:
+//   nodes: 4 float4 per interior record (BFS order):
+//     n0 = (L.min.x, L.max.x, L.min.y, L.max.y)
+//     n1 = (R.min.x, R.max.x, R.min.y, R.max.y)
+//     n2 = (L.min.z, L.max.z, R.min.z, R.max.z)
+//     n3 = (bits(left ref), bits(right ref), 0, 0)
+//   a child ref >= 0 is a record index, < 0 is ~(triangle slot).
+//   tris: 3 float4 per triangle slot (leaf order): (p1.xyz, bits(face id)),
+//     (p2 - p1, 0), (p3 - p1, 0), the edges of the reference's Moller-Trumbore.
+//   qnodes: 8-bit child boxes (precision 1): 2 float4 + 1 uint4 per record.
+struct DevScene {
+  const float4* nodes;
+  const float4* qnodes;
+  const float4* tris;
+  int root_ref;
+  int ntri;
+  int nrec;
+  int precision;
+  // shading data in the reference layout
+  const float4* points;
+  const float2* uvs;
+  const float4* normals;
+  const Face* faces;
+  const Material* materials;
+  const int* light_faces;
+  int nlights;
+};
+
+struct DevEnv {
+  const float4* rgb;
+  const float* lum;
+  const float* sat;   // FP32 copy of the inclusive SAT used for sampling
+  int w, h;
+  int present;
+  // adaptive light grid (mode 1): nu x nv, rx x ry tiles per cell
+  const float* grid_func;
+  const float* grid_sat;
+  float* grid_accum;
+  int grid_on;
+  int nu, nv, rx, ry;
+  float4 camera_pos;
+};
+
+// Per-pass control block in device memory (zeroed at the start of each pass).
+struct Ctrl {
+  int count[kMaxDepth + 2];     // queue length entering bounce b (count[1] = pixels)
+  int shadow[kMaxDepth + 2];    // shadow rays emitted at bounce b
+  int work[2 * (kMaxDepth + 2)];
+  int tiles[kMaxDepth + 2];
+  int error;
+  int pad;
+  unsigned long long rays[3];   // primary, extension, shadow traced
+};
+
+// Per-pass parameters (uploaded once per pass from pinned host memory).
+struct PassParams {
+  float cam_m[16];       // view->world matrix rows (Matrix.cl:216-241 mInv)
+  float cam_d;           // 1 / tan(radians(fov) / 2)
+  float cam_a;           // width / height
+  float inv_w, inv_h;    // 1 / width, 1 / height
+  float dim_w, dim_h;    // width, height as floats
+  float frame_count;     // State.frameCount
+  int width, height;
+  int max_depth;
+  int mode;
+  int rr_depth;
+  int kahan;
+  int pad;
+  int seeds[2 * (1 + 2 * kMaxDepth)];  // mode 0: allocateState() seed pairs
+};
+
+}  // namespace mt

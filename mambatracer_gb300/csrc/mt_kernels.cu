@@ -1,0 +1,538 @@
+// Wavefront frame kernels: raygen, closest-hit traversal, fused shading with
+// stable queue compaction, shadow traversal with film resolve.
+//
+// One pass of CDeviceGI.loop (src/cl/device/CDeviceGI.java:214-271) is
+//   k_raygen                       InitCameraRayDataJitter + InitPathData +
+//                                  InitIntersection + InitIntDataToIndex
+//   per bounce b:
+//     k_trace_closest              IntersectPrimitives (traversal part)
+//     k_shade                      IntersectPrimitives (hit record) + SetupBSDFPath +
+//                                  LightHitPass + CCompact.execute + DirectLight (light
+//                                  sample and BSDF evaluation) + SampleBSDFRayDirection
+//     k_trace_shadow               DirectLight's testOcclusion + addAccum
+// with every queue on the device, so a pass needs no host round trip.
+#include <cuda_runtime.h>
+
+#include "mt_device.cuh"
+#include "mt_kernels.h"
+#include "mt_traverse.cuh"
+
+namespace mt {
+
+using namespace dv;
+
+namespace {
+
+constexpr unsigned long long kFlagAgg = 1ull << 62;
+constexpr unsigned long long kFlagPfx = 2ull << 62;
+constexpr unsigned long long kValMask = (1ull << 62) - 1;
+constexpr unsigned long long kLowMask = (1ull << 31) - 1;
+constexpr int kSpinLimit = 1 << 22;
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Decoupled look-back over tile aggregates (single-pass stable compaction).
+// Returns the exclusive prefix of `tile`. Every wait is bounded: after
+// kSpinLimit polls the error is latched and the partial prefix is used.
+__device__ unsigned long long lookback(unsigned long long* status, int tile, unsigned long long agg, int* err) {
+  if (tile == 0) {
+    st_release(&status[0], kFlagPfx | agg);
+    return 0;
+  }
+  st_release(&status[tile], kFlagAgg | agg);
+  unsigned long long excl = 0;
+  int t = tile - 1;
+  while (t >= 0) {
+    unsigned long long s = 0;
+    int it = 0;
+    for (; it < kSpinLimit; ++it) {
+      s = ld_acquire(&status[t]);
+      if (s >> 62) break;
+      __nanosleep(32);
+    }
+    if (it == kSpinLimit) {
+      atomicExch(err, kDevErrLookback);
+      break;
+    }
+    excl += s & kValMask;
+    if ((s >> 62) == 2) break;
+    --t;
+  }
+  st_release(&status[tile], kFlagPfx | (excl + agg));
+  return excl;
+}
+
+// Block-wide exclusive scan of packed 64-bit counts (kShadeThreads threads).
+__device__ __forceinline__ unsigned long long block_scan(unsigned long long v, unsigned long long* total,
+                                                         unsigned long long* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long w = lane < kShadeThreads / 32 ? sh[lane] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kShadeThreads / 32) sh[lane] = w;
+  }
+  __syncthreads();
+  unsigned long long warp_excl = warp == 0 ? 0ull : sh[warp - 1];
+  *total = sh[kShadeThreads / 32 - 1];
+  __syncthreads();
+  return warp_excl + x - v;
+}
+
+__device__ __forceinline__ void film_add(float4* __restrict__ acc, float4* __restrict__ comp, int pixel, V v, int kahan) {
+  if (!abs_valid4(v)) return;  // addAccum, src/cl/kernel/Render.cl:1-7
+  V a = acc[pixel];
+  if (!kahan) {
+    acc[pixel] = add(a, v);
+    return;
+  }
+  V c = comp[pixel];
+  V y = sub(v, c);
+  V t = add(a, y);
+  comp[pixel] = sub(sub(t, a), y);
+  acc[pixel] = t;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- raygen
+// InitCameraRayDataJitter (src/cl/kernel/Initialize.cl:129-172) with the
+// per-frame camera constants precomputed on the host, plus the path and queue
+// resets of InitPathData / InitIntersection / InitIntDataToIndex.
+__global__ void k_raygen(const PassParams* __restrict__ pp, Ctrl* ctrl, FrameBufs fb) {
+  const int N = pp->width * pp->height;
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id == 0) ctrl->count[1] = N;
+  if (id >= N) return;
+  int32_t sx, sy;
+  if (pp->mode == 0) {
+    sx = pp->seeds[0];
+    sy = pp->seeds[1];
+  } else {
+    stage_seed(0, 0, &sx, &sy);
+  }
+  Seed s = gen_seed(sx, sy, pp->frame_count, pp->mode == 0 ? id : pixel_gid(id));
+  float r0 = rnd(s), r1 = rnd(s);
+  const int W = pp->width;
+  float px = (float)(id % W), py = (float)(id / W);
+  float j1 = pp->inv_w * (2.f * r0 - 1.f);
+  float j2 = pp->inv_h * (2.f * r1 - 1.f);
+  V d = normalize4(mk(pp->cam_a * (2.f * px / pp->dim_w - 1.f + j1), -2.f * py / pp->dim_h + 1.f + j2, -pp->cam_d, 0.f));
+  const float* m = pp->cam_m;
+  V z = zero4();
+  V m0 = mk(m[0], m[1], m[2], m[3]), m1 = mk(m[4], m[5], m[6], m[7]), m2 = mk(m[8], m[9], m[10], m[11]),
+    m3 = mk(m[12], m[13], m[14], m[15]);
+  V o = mk(dot3(m0, z) + m0.w, dot3(m1, z) + m1.w, dot3(m2, z) + m2.w, dot3(m3, z) + m3.w);
+  if (!(o.w == 1.f)) o = mk(o.x / o.w, o.y / o.w, o.z / o.w, 0.f);
+  V dw = mk(dot4(m0, d), dot4(m1, d), dot4(m2, d), 0.f);
+  fb.q_o[0][id] = mk(o.x, o.y, o.z, __int_as_float(id));
+  fb.q_d[0][id] = mk(dw.x, dw.y, dw.z, 0.f);
+  fb.thr[id] = mk(1.f, 1.f, 1.f, 1.f);
+  fb.ps[id] = mk(0.f, 0.f, 0.f, 1.f);  // hitpoint.xyz, lastPdfW
+  fb.flag[id] = 1;                     // lastSpecular
+}
+
+// ----------------------------------------------------------- traversal
+template <int TOP>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_closest(DevScene S, Ctrl* ctrl, int b, FrameBufs fb) {
+  __shared__ int stack[kStackDepth * kTraceThreads];
+  __shared__ float4 top[TOP > 0 ? 4 * TOP : 1];
+  if (TOP > 0) {
+    int n = 4 * min(TOP, S.nrec);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) top[i] = __ldg(S.nodes + i);
+    __syncthreads();
+  }
+  const int count = ctrl->count[b];
+  const int lane = threadIdx.x & 31;
+  const float4* __restrict__ qo = fb.q_o[(b + 1) & 1];
+  const float4* __restrict__ qd = fb.q_d[(b + 1) & 1];
+  int* st = stack + threadIdx.x;
+  bool overflow = false;
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&ctrl->work[2 * b], 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= count) break;
+    int i = base + lane;
+    if (i < count) {
+      tr::RayT r = tr::make_ray(__ldg(qo + i), __ldg(qd + i), 0.001f, CUDART_INF_F);
+      int prim = tr::traverse<false, TOP>(S, top, r, st, kTraceThreads, &overflow, nullptr);
+      fb.hit_t[i] = r.tmax;
+      fb.hit_prim[i] = prim;
+    }
+  }
+  if (overflow) atomicExch(&ctrl->error, kDevErrStack);
+}
+
+template <int TOP>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_shadow(DevScene S, Ctrl* ctrl, int b, int mode, FrameBufs fb,
+                                                                int kahan) {
+  __shared__ int stack[kStackDepth * kTraceThreads];
+  __shared__ float4 top[TOP > 0 ? 4 * TOP : 1];
+  if (TOP > 0) {
+    int n = 4 * min(TOP, S.nrec);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) top[i] = __ldg(S.nodes + i);
+    __syncthreads();
+  }
+  // mode 0: shadow slots are the compacted survivor slots (flagged by pixel >= 0)
+  const int count = mode == 0 ? ctrl->count[b + 1] : ctrl->shadow[b];
+  const int lane = threadIdx.x & 31;
+  int* st = stack + threadIdx.x;
+  bool overflow = false;
+  unsigned traced = 0;
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&ctrl->work[2 * b + 1], 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= count) break;
+    int i = base + lane;
+    if (i < count) {
+      float4 o = __ldg(fb.s_o + i);
+      int pixel = __float_as_int(o.w);
+      if (pixel >= 0) {
+        float4 d = __ldg(fb.s_d + i);
+        tr::RayT r = tr::make_ray(o, d, 0.0001f, d.w);
+        int h = tr::traverse<true, TOP>(S, top, r, st, kTraceThreads, &overflow, nullptr);
+        ++traced;
+        if (h < 0) {
+          float4 c = __ldg(fb.s_c + i);
+          film_add(fb.film, fb.film_c, pixel, mk(c.x, c.y, c.z, 1.f), kahan);
+        }
+      }
+    }
+  }
+  unsigned long long tot = traced;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
+  if (lane == 0 && tot) atomicAdd(&ctrl->rays[2], tot);
+  if (overflow) atomicExch(&ctrl->error, kDevErrStack);
+}
+
+// ----------------------------------------------------------------- shade
+// mode 0 (reference semantics): survivors are compacted first, the light and
+// BSDF samples of a survivor are keyed on its compacted slot as DirectLight and
+// SampleBSDFRayDirection key them on get_global_id; the shadow ray of survivor
+// j' sits at shadow slot j'.
+// mode 1 (benchmark semantics): samples are keyed on the pixel, Russian
+// roulette runs after the BSDF sample, and the survivors and shadow rays are
+// compacted together afterwards.
+template <int MODE>
+__global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene S, DevEnv E, const PassParams* __restrict__ pp,
+                                                         Ctrl* ctrl, int b, FrameBufs fb,
+                                                         unsigned long long* status) {
+  __shared__ unsigned long long sh[kShadeThreads / 32 + 1];
+  __shared__ int s_tile;
+  __shared__ unsigned long long s_base;
+  const int count = ctrl->count[b];
+  const int ntiles = (count + kShadeThreads - 1) / kShadeThreads;
+  if (threadIdx.x == 0) s_tile = atomicAdd(&ctrl->tiles[b], 1);
+  __syncthreads();
+  const int tile = s_tile;
+  if (tile >= ntiles) return;
+  const int j = tile * kShadeThreads + threadIdx.x;
+  const float fc = pp->frame_count;
+  const int kahan = pp->kahan;
+
+  bool alive = false;
+  int pixel = 0;
+  V thr = zero4(), ps = zero4();
+  int spec = 0;
+  Hit H;
+  Bsdf B;
+  B.mat = -1;
+  if (j < count) {
+    float4 qo = __ldg(fb.q_o[(b + 1) & 1] + j);
+    float4 qd = __ldg(fb.q_d[(b + 1) & 1] + j);
+    pixel = __float_as_int(qo.w);
+    V o = mk(qo.x, qo.y, qo.z, 0.f), d = mk(qd.x, qd.y, qd.z, 0.f);
+    const float t = fb.hit_t[j];
+    const int prim = fb.hit_prim[j];
+    thr = fb.thr[pixel];
+    ps = fb.ps[pixel];
+    spec = fb.flag[pixel];
+    if (prim >= 0) {
+      hit_record(S, o, d, t, prim, H);
+      B = setup_bsdf(S, d, H.n, H.mat);
+      if (B.mat >= 0) {
+        const Material& M = S.materials[B.mat];
+        if (is_emitter(M)) {  // LightHitPass emitter branch, Render.cl:76-104
+          float pick = 1.f / (float)S.nlights;
+          if (MODE == 1 && E.present && S.nlights > 0) pick = pick * 0.5f;
+          AreaLight L = get_area_light(S, M, prim);
+          float pdfA = 0.f;
+          V c = radiance_area(L, d, &pdfA);
+          if (zero3(c)) {
+            alive = true;  // Render.cl:88-89 returns with isect->hit still set
+          } else {
+            float w = 1.f;
+            if (!spec) {
+              float pdfW = pdf_a_to_w(pdfA, t, B.fix.z);
+              w = mis2(ps.w, pdfW * pick);
+            }
+            film_add(fb.film, fb.film_c, pixel, muls(mul(thr, c), w), kahan);
+          }
+        } else {
+          alive = true;
+        }
+      }
+    } else if (E.present) {  // LightHitPass environment branch, Render.cl:106-123
+      float pdfW = 0.f;
+      V c = radiance_env(E, d, &pdfW);
+      if (!zero3(c)) {
+        if (MODE == 1 && S.nlights > 0) pdfW = pdfW * 0.5f;
+        float w = 1.f;
+        if (!spec) w = mis2(ps.w, pdfW);
+        film_add(fb.film, fb.film_c, pixel, muls(mul(thr, c), w), kahan);
+      }
+    }
+  }
+
+  unsigned long long tot = 0;
+  int slot = -1, sslot = -1;
+  if (MODE == 0) {
+    unsigned long long excl = block_scan(alive ? 1ull : 0ull, &tot, sh);
+    if (threadIdx.x == 0) s_base = lookback(status, tile, tot, &ctrl->error);
+    __syncthreads();
+    slot = (int)(s_base + excl);
+    if (tile == ntiles - 1 && threadIdx.x == 0) {
+      ctrl->count[b + 1] = (int)(s_base + tot);
+      ctrl->shadow[b] = (int)(s_base + tot);
+    }
+  }
+
+  // DirectLight (Render.cl:377-466) and SampleBSDFRayDirection (Render.cl:233-285)
+  bool has_shadow = false;
+  V sho = zero4(), shd = zero4(), shc = zero4();
+  V ndir = zero4();
+  if (alive) {
+    int32_t lx, ly, bx, by;
+    int gid;
+    if (MODE == 0) {
+      lx = pp->seeds[2 * (2 * b)];
+      ly = pp->seeds[2 * (2 * b) + 1];
+      bx = lx;
+      by = ly;
+      gid = slot;
+    } else {
+      stage_seed(b, 1, &lx, &ly);
+      stage_seed(b, 2, &bx, &by);
+      gid = pixel_gid(pixel);
+    }
+    Seed s = gen_seed(lx, ly, fc, gid);
+    V dir = zero4();
+    float dist = 0.f, pdfW = 0.f, pick = 1.f;
+    V smp;
+    smp.x = rnd(s);
+    smp.y = rnd(s);
+    smp.z = rnd(s);
+    smp.w = rnd(s);
+    V rad = zero4();
+    bool smesh = false, senv = false;
+    if (E.present && S.nlights > 0) {
+      float r = rnd(s);
+      pick = pick * 0.5f;
+      if (r < 0.5f) smesh = true; else senv = true;
+    } else if (E.present) {
+      senv = true;
+    } else if (S.nlights > 0) {
+      smesh = true;
+    }
+    if (smesh) {
+      int li = (int)(rnd(s) * (float)S.nlights);
+      li = li < S.nlights ? li : S.nlights - 1;  // rounding of rnd * n for n > 2^22
+      int tri = S.light_faces[MODE == 0 ? 0 : li];  // Render.cl:305 reads light 0
+      pick = pick * (1.f / (float)S.nlights);
+      const Material& Ml = S.materials[__ldg(reinterpret_cast<const int*>(S.faces + tri) + 9) & 0xFFFF];
+      AreaLight L = get_area_light(S, Ml, tri);
+      rad = illuminate_area(L, H.p, smp.x, smp.y, &dir, &dist, &pdfW);
+    } else if (senv) {
+      rad = illuminate_env(E, smp, &dir, &dist, &pdfW);
+    }
+    if (!zero3(rad)) {
+      float bpdf = 0.f, cosO = 0.f;
+      V f = eval_bsdf(S, B, dir, &bpdf, &cosO);
+      if (!zero3(f)) {
+        float w = mis2(pdfW, bpdf);
+        float sc = (w * cosO / (pick * pdfW));
+        shc = mk(sc * (rad.x * f.x) * thr.x, sc * (rad.y * f.y) * thr.y, sc * (rad.z * f.z) * thr.z, 1.f);
+        sho = mk(H.p.x, H.p.y, H.p.z, __int_as_float(pixel));
+        shd = mk(dir.x, dir.y, dir.z, dist - 2.f * 1e-3f);
+        has_shadow = true;
+      }
+    }
+    // BSDF sample
+    Seed s2 = gen_seed(bx, by, fc, gid);
+    float s0 = rnd(s2), s1 = rnd(s2), sz = rnd(s2);
+    float pdf = 0.f, cosO = 0.f;
+    V f = sample_bsdf(S, B, s0, s1, sz, &ndir, &pdf, &cosO);
+    float q = cosO / pdf;
+    thr = mul(thr, muls(f, q));
+    spec = 0;
+    ps = mk(H.p.x, H.p.y, H.p.z, pdf);
+    if (MODE == 1 && pp->rr_depth > 0 && b >= pp->rr_depth) {
+      int32_t rx, ry;
+      stage_seed(b, 3, &rx, &ry);
+      Seed rs = gen_seed(rx, ry, fc, gid);
+      float u = rnd(rs);
+      float mx = maxf_(thr.x, maxf_(thr.y, thr.z));
+      float cont = minf_(0.95f, mx);
+      if (!(u < cont)) alive = false;
+      else thr = divs(thr, cont);
+    }
+    fb.thr[pixel] = thr;
+    fb.ps[pixel] = ps;
+    fb.flag[pixel] = 0;
+  }
+
+  if (MODE == 1) {
+    unsigned long long v = (alive ? 1ull : 0ull) | ((has_shadow ? 1ull : 0ull) << 31);
+    unsigned long long excl = block_scan(v, &tot, sh);
+    if (threadIdx.x == 0) s_base = lookback(status, tile, tot, &ctrl->error);
+    __syncthreads();
+    unsigned long long pos = s_base + excl;
+    slot = (int)(pos & kLowMask);
+    sslot = (int)(pos >> 31);
+    if (tile == ntiles - 1 && threadIdx.x == 0) {
+      unsigned long long all = s_base + tot;
+      ctrl->count[b + 1] = (int)(all & kLowMask);
+      ctrl->shadow[b] = (int)(all >> 31);
+    }
+  } else {
+    sslot = slot;
+  }
+  const int nq = b & 1;  // queue written for bounce b + 1
+  if (MODE == 0) {
+    if (alive) {
+      fb.q_o[nq][slot] = mk(H.p.x, H.p.y, H.p.z, __int_as_float(pixel));
+      fb.q_d[nq][slot] = mk(ndir.x, ndir.y, ndir.z, 0.f);
+      if (has_shadow) {
+        fb.s_o[sslot] = sho;
+        fb.s_d[sslot] = shd;
+        fb.s_c[sslot] = shc;
+      } else {
+        fb.s_o[sslot] = mk(0.f, 0.f, 0.f, __int_as_float(-1));
+      }
+    }
+  } else {
+    if (alive) {
+      fb.q_o[nq][slot] = mk(H.p.x, H.p.y, H.p.z, __int_as_float(pixel));
+      fb.q_d[nq][slot] = mk(ndir.x, ndir.y, ndir.z, 0.f);
+    }
+    if (has_shadow) {
+      fb.s_o[sslot] = sho;
+      fb.s_d[sslot] = shd;
+      fb.s_c[sslot] = shc;
+    }
+  }
+}
+
+// Adds a finished pass's ray counts into the job's running totals
+// [primary, extension, shadow].
+__global__ void k_accumulate(const Ctrl* ctrl, int max_depth, int n_pixels, unsigned long long* totals) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned long long ext = 0;
+  for (int b = 2; b <= max_depth; ++b) ext += (unsigned long long)ctrl->count[b];
+  totals[0] += (unsigned long long)n_pixels;
+  totals[1] += ext;
+  totals[2] += ctrl->rays[2];
+  if (ctrl->error) totals[3] = (unsigned long long)ctrl->error;
+}
+
+// ---------------------------------------------------------------- launchers
+namespace {
+template <int TOP>
+int trace_blocks_per_sm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest<TOP>, kTraceThreads, 0);
+  return n > 0 ? n : 1;
+}
+}  // namespace
+
+int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassParams* d_pp, int mode, int max_depth,
+                int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb, unsigned long long* status,
+                size_t status_stride, int num_sms, cudaEvent_t* ev, unsigned long long* totals) {
+  const int N = width * height;
+  constexpr int TOP = 256;
+  static int bps = 0;
+  if (bps == 0) bps = trace_blocks_per_sm<TOP>();
+  const int trace_grid = num_sms * bps;
+  const int tiles = (N + kShadeThreads - 1) / kShadeThreads;
+  int e = 0;
+  if (ev) cudaEventRecord(ev[e++], st);
+  k_raygen<<<(N + 255) / 256, 256, 0, st>>>(d_pp, ctrl, fb);
+  if (ev) cudaEventRecord(ev[e++], st);
+  for (int b = 1; b <= max_depth; ++b) {
+    k_trace_closest<TOP><<<trace_grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb);
+    if (ev) cudaEventRecord(ev[e++], st);
+    unsigned long long* stb = status + (size_t)(b - 1) * status_stride;
+    if (mode == 0)
+      k_shade<0><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+    else
+      k_shade<1><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+    if (ev) cudaEventRecord(ev[e++], st);
+    k_trace_shadow<TOP><<<trace_grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan);
+    if (ev) cudaEventRecord(ev[e++], st);
+  }
+  if (totals) k_accumulate<<<1, 32, 0, st>>>(ctrl, max_depth, N, totals);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// Ray queries on reference-layout rays (80 B): closest or any hit.
+__global__ void __launch_bounds__(kTraceThreads) k_query(DevScene S, const float4* __restrict__ rays, int n, int any,
+                                                         float* __restrict__ t_out, int* __restrict__ prim_out,
+                                                         int* work, int* err) {
+  __shared__ int stack[kStackDepth * kTraceThreads];
+  const int lane = threadIdx.x & 31;
+  int* st = stack + threadIdx.x;
+  bool overflow = false;
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(work, 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    int i = base + lane;
+    if (i < n) {
+      const float4* R = rays + 5 * (size_t)i;  // Ray: o, d, inv_d, sign, (extra, tMin, tMax)
+      float4 o = __ldg(R + 0), d = __ldg(R + 1), tail = __ldg(R + 4);
+      tr::RayT r = tr::make_ray(o, d, tail.z, tail.w);
+      if (any) {
+        int h = tr::traverse<true, 0>(S, nullptr, r, st, kTraceThreads, &overflow, nullptr);
+        prim_out[i] = h >= 0 ? 1 : 0;
+      } else {
+        int h = tr::traverse<false, 0>(S, nullptr, r, st, kTraceThreads, &overflow, nullptr);
+        t_out[i] = r.tmax;
+        prim_out[i] = h;
+      }
+    }
+  }
+  if (overflow) atomicExch(err, kDevErrStack);
+}
+
+int launch_query(cudaStream_t st, const DevScene& S, const float4* rays, int n, int any, float* t_out, int* prim_out,
+                 int* work, int* err, int num_sms) {
+  int bps = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_query, kTraceThreads, 0);
+  if (bps < 1) bps = 1;
+  k_query<<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace mt

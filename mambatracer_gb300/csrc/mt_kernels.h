@@ -1,0 +1,44 @@
+// Host-visible declarations of the device launchers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "mt_common.h"
+
+namespace mt {
+
+// Per-job frame buffers (structure of arrays).
+struct FrameBufs {
+  float4* q_o[2];   // ray queue: origin.xyz, bits(pixel)  (ping-pong by bounce parity)
+  float4* q_d[2];   // ray queue: direction.xyz, 0
+  float* hit_t;     // closest-hit distance per queue slot
+  int* hit_prim;    // closest-hit face id per queue slot (-1 = miss)
+  float4* thr;      // path throughput per pixel (4 lanes as the reference)
+  float4* ps;       // path: hitpoint.xyz, lastPdfW
+  int* flag;        // path: lastSpecular
+  float4* s_o;      // shadow queue: origin.xyz, bits(pixel or -1)
+  float4* s_d;      // shadow queue: direction.xyz, tMax
+  float4* s_c;      // shadow queue: contribution.xyz
+  float4* film;     // accumulated radiance per pixel
+  float4* film_c;   // Kahan compensation per pixel
+};
+
+// events: optional array of 2 + 3 * max_depth events recorded around each launch.
+// totals: optional running ray counts [primary, extension, shadow, error] of the job.
+int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassParams* d_pp, int mode,
+                int max_depth, int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb,
+                unsigned long long* status, size_t status_stride, int num_sms, cudaEvent_t* events,
+                unsigned long long* totals);
+
+int launch_query(cudaStream_t st, const DevScene& S, const float4* rays, int n, int any, float* t_out,
+                 int* prim_out, int* work, int* err, int num_sms);
+
+// Environment: luminance (FP32, RGBSpace.cl:28-32) and the inclusive SAT built
+// in FP64, with an FP32 copy for sampling.
+int launch_env_build(cudaStream_t st, const float4* rgb, int w, int h, float* lum, double* sat64, float* sat32);
+
+// Light-grid per-cell SAT (row passes of rx, column passes of ry), FP32 in the
+// reference's Kogge-Stone order or FP64.
+int launch_grid_sat(cudaStream_t st, const float* func, float* sat32, double* sat64, int nu, int nv, int rx, int ry,
+                    int fp64);
+
+}  // namespace mt

@@ -1,0 +1,165 @@
+// BVH traversal on the GPU layout (see DevScene in mt_common.h).
+//
+// Visit order is the reference's stackless traversal (src/cl/kernel/NormalBVH.cl:14-92):
+// at an interior node both child boxes are slab-tested (Util.cl:707-732); when
+// both are hit the nearer (right only if strictly nearer) is entered and the
+// other is deferred; leaves are single triangles tested with Moller-Trumbore
+// (Primitive.cl:3-29) and accepted when tMin < t < tMax (Util.cl:552-555).
+// The reference backtracks with a 64-bit bitstack and parent/sibling links; a
+// stack of deferred children in shared memory visits the same nodes in the same
+// order without re-reading parents. Identical order and identical arithmetic
+// give identical hit ids, including ties.
+#pragma once
+#include "mt_device.cuh"
+
+namespace mt {
+namespace tr {
+
+struct RayT {
+  float ox, oy, oz;
+  float ix, iy, iz;  // 1/d (IEEE division, as initGlobalRay stores inv_d)
+  float dx, dy, dz;
+  int sx, sy, sz;    // inv_d < 0
+  float tmin, tmax;
+};
+
+__device__ __forceinline__ RayT make_ray(float4 o, float4 d, float tmin, float tmax) {
+  RayT r;
+  r.ox = o.x; r.oy = o.y; r.oz = o.z;
+  r.dx = d.x; r.dy = d.y; r.dz = d.z;
+  r.ix = 1.f / d.x; r.iy = 1.f / d.y; r.iz = 1.f / d.z;
+  r.sx = r.ix < 0.f; r.sy = r.iy < 0.f; r.sz = r.iz < 0.f;
+  r.tmin = tmin;
+  r.tmax = tmax;
+  return r;
+}
+
+// Util.cl:707-732. lo/hi: the box along each axis; the near plane is picked by
+// the direction sign as getExtent(sign) does.
+__device__ __forceinline__ bool slab(const RayT& r, float lox, float hix, float loy, float hiy, float loz, float hiz,
+                                     float* tnear) {
+  float tmin = ((r.sx ? hix : lox) - r.ox) * r.ix;
+  float tmax = ((r.sx ? lox : hix) - r.ox) * r.ix;
+  float tymin = ((r.sy ? hiy : loy) - r.oy) * r.iy;
+  float tymax = ((r.sy ? loy : hiy) - r.oy) * r.iy;
+  bool ok = !((tmin > tymax) || (tymin > tmax));
+  tmin = (tymin > tmin) ? tymin : tmin;
+  tmax = (tymax < tmax) ? tymax : tmax;
+  float tzmin = ((r.sz ? hiz : loz) - r.oz) * r.iz;
+  float tzmax = ((r.sz ? loz : hiz) - r.oz) * r.iz;
+  ok = ok && !((tmin > tzmax) || (tzmin > tmax));
+  tmin = (tzmin > tmin) ? tzmin : tmin;
+  tmax = (tzmax < tmax) ? tzmax : tmax;
+  tmax *= 1.00000024f;
+  *tnear = tmin;
+  return ok && (tmin < r.tmax) && (tmax > r.tmin);
+}
+
+// Primitive.cl:3-29: returns t, or tmax when the triangle is missed. The
+// reference's float4 dot adds a w-lane product that is +0 for these operands,
+// which changes at most the sign of a zero result and never the outcome.
+__device__ __forceinline__ float tri_t(const RayT& r, float4 p1, float4 e1, float4 e2) {
+  float hx = r.dy * e2.z - r.dz * e2.y;
+  float hy = r.dz * e2.x - r.dx * e2.z;
+  float hz = r.dx * e2.y - r.dy * e2.x;
+  float a = (e1.x * hx + e1.y * hy) + e1.z * hz;
+  if (a > -0.0000001f && a < 0.0000001f) return r.tmax;
+  float f = 1.f / a;
+  float sx = r.ox - p1.x, sy = r.oy - p1.y, sz = r.oz - p1.z;
+  float b1 = f * ((sx * hx + sy * hy) + sz * hz);
+  float qx = sy * e1.z - sz * e1.y;
+  float qy = sz * e1.x - sx * e1.z;
+  float qz = sx * e1.y - sy * e1.x;
+  float b2 = f * ((r.dx * qx + r.dy * qy) + r.dz * qz);
+  float t = f * ((e2.x * qx + e2.y * qy) + e2.z * qz);
+  if (b1 < 0.f || b1 > 1.f || b2 < 0.f || b1 + b2 > 1.f || t < 0.f || t > r.tmax) return r.tmax;
+  return t;
+}
+
+struct NodeBoxes {
+  float lx0, lx1, ly0, ly1, lz0, lz1;
+  float rx0, rx1, ry0, ry1, rz0, rz1;
+  int left, right;
+};
+
+template <int TOP>
+__device__ __forceinline__ NodeBoxes load_node(const float4* __restrict__ nodes, const float4* smem_top, int rec) {
+  float4 n0, n1, n2, n3;
+  if (TOP > 0 && rec < TOP) {
+    n0 = smem_top[4 * rec + 0];
+    n1 = smem_top[4 * rec + 1];
+    n2 = smem_top[4 * rec + 2];
+    n3 = smem_top[4 * rec + 3];
+  } else {
+    const float4* p = nodes + 4 * (size_t)rec;
+    n0 = __ldg(p + 0);
+    n1 = __ldg(p + 1);
+    n2 = __ldg(p + 2);
+    n3 = __ldg(p + 3);
+  }
+  NodeBoxes b;
+  b.lx0 = n0.x; b.lx1 = n0.y; b.ly0 = n0.z; b.ly1 = n0.w;
+  b.rx0 = n1.x; b.rx1 = n1.y; b.ry0 = n1.z; b.ry1 = n1.w;
+  b.lz0 = n2.x; b.lz1 = n2.y; b.rz0 = n2.z; b.rz1 = n2.w;
+  b.left = __float_as_int(n3.x);
+  b.right = __float_as_int(n3.y);
+  return b;
+}
+
+struct TraceStats {
+  unsigned int interior, tris;
+};
+
+// Closest hit (ANY = false) or any hit (ANY = true). stack: this thread's
+// column of a [depth][threads] shared array. Returns the hit face id or -1; on
+// a closest hit r.tmax holds the hit distance. *overflow is set when the
+// deferred-node stack would exceed kStackDepth (the reference's bitstack limit).
+template <bool ANY, int TOP>
+__device__ __forceinline__ int traverse(const DevScene& S, const float4* smem_top, RayT& r, int* stack, int stride,
+                                        bool* overflow, TraceStats* st) {
+  int hit_face = -1;
+  int ref = S.root_ref;
+  int sp = 0;
+  const float4* __restrict__ nodes = S.nodes;
+  const float4* __restrict__ tris = S.tris;
+  for (;;) {
+    if (ref >= 0) {
+      NodeBoxes b = load_node<TOP>(nodes, smem_top, ref);
+      if (st) st->interior++;
+      float tl, trr;
+      bool hl = slab(r, b.lx0, b.lx1, b.ly0, b.ly1, b.lz0, b.lz1, &tl);
+      bool hr = slab(r, b.rx0, b.rx1, b.ry0, b.ry1, b.rz0, b.rz1, &trr);
+      if (hl && hr) {
+        int nearc = (trr < tl) ? b.right : b.left;
+        int farc = (trr < tl) ? b.left : b.right;
+        if (sp >= kStackDepth) {
+          *overflow = true;
+          return hit_face;
+        }
+        stack[sp * stride] = farc;
+        ++sp;
+        ref = nearc;
+        continue;
+      }
+      if (hl) { ref = b.left; continue; }
+      if (hr) { ref = b.right; continue; }
+    } else {
+      int slot = ~ref;
+      const float4* tp = tris + 3 * (size_t)slot;
+      float4 p1 = __ldg(tp + 0), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+      if (st) st->tris++;
+      float t = tri_t(r, p1, e1, e2);
+      if ((r.tmin < t) && (t < r.tmax)) {
+        hit_face = __float_as_int(p1.w);
+        if (ANY) return hit_face;
+        r.tmax = t;
+      }
+    }
+    if (sp == 0) return hit_face;
+    --sp;
+    ref = stack[sp * stride];
+  }
+}
+
+}  // namespace tr
+}  // namespace mt

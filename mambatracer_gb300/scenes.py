@@ -147,13 +147,13 @@ def _palette_materials(levels=64, glossy_fraction=1.0):
     return np.stack(mats)
 
 
-def soup(ntri=1_000_000, seed=1, width=1920, height=1080) -> Scene:
+def soup(ntri=1_000_000, seed=1, width=1920, height=1080, extent=1.0, edge_sigma=0.005) -> Scene:
     """Triangle soup: centroids U[-1,1]^3, edge vectors i.i.d. N(0, 0.005^2) per
     axis, per-triangle GGX roughness U[0.05, 0.8] and albedo U[0.2, 0.9]."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    c = rng.uniform(-1.0, 1.0, size=(ntri, 3))
-    e1 = rng.normal(0.0, 0.005, size=(ntri, 3))
-    e2 = rng.normal(0.0, 0.005, size=(ntri, 3))
+    c = rng.uniform(-extent, extent, size=(ntri, 3))
+    e1 = rng.normal(0.0, edge_sigma, size=(ntri, 3))
+    e2 = rng.normal(0.0, edge_sigma, size=(ntri, 3))
     p1 = c - (e1 + e2) / 3.0
     pts = np.empty((ntri * 3, 3), np.float64)
     pts[0::3] = p1

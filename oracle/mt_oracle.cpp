@@ -1028,7 +1028,10 @@ void render_frame(const Scene& S, const Env<R>& E, const CameraF& cam_in, const 
         if (alive) { rays[live] = rays[j]; pixels[live] = pixels[j]; ++live; }
       }
     }
-    if (P.mode == 1) count = live;
+    if (P.mode == 1) {
+      count = live;
+      if (counts_out) counts_out[b - 1] = count;  // queue entering the next bounce
+    }
   }
 }
 

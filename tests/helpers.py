@@ -1,0 +1,69 @@
+"""Shared helpers for the parity tests (oracle calls on the test side)."""
+import numpy as np
+
+from oracle.oracle import bvh_build, ptr
+
+
+def oracle_trace(orc, sc, nodes, bounds, rays, counts=False):
+    t = np.zeros(rays.shape[0], np.float32)
+    p = np.zeros(rays.shape[0], np.int32)
+    c = np.zeros((rays.shape[0], 2), np.int64) if counts else None
+    orc.lib.or_trace_closest(ptr(rays), rays.shape[0], ptr(sc.points), ptr(sc.faces), sc.ntri, ptr(nodes),
+                             ptr(bounds), ptr(t), ptr(p), ptr(c))
+    return (t, p, c) if counts else (t, p)
+
+
+def oracle_any(orc, sc, nodes, bounds, rays):
+    o = np.zeros(rays.shape[0], np.int32)
+    orc.lib.or_occlusion(ptr(rays), ptr(o), rays.shape[0], ptr(sc.points), ptr(sc.faces), sc.ntri, ptr(nodes),
+                         ptr(bounds), None)
+    return o
+
+
+def env_tables(orc, envmap, w, h):
+    lum = np.zeros(w * h, np.float32)
+    sat = np.zeros(w * h, np.float32)
+    orc.lib.or_env_lum_sat(ptr(envmap), w, h, ptr(lum), ptr(sat))
+    return lum, sat
+
+
+def oracle_frames(orc, sc, nodes, bounds, W, H, depth, mode, rr, seeds_list, env=None, fp64=False, acc=None,
+                  first_frame=1):
+    """Run len(seeds_list) frames of the oracle; returns (accum, counts per frame, ray counts)."""
+    if env is not None:
+        envmap, ew, eh = env
+        lum, sat = env_tables(orc, envmap, ew, eh)
+        if fp64:
+            lum64 = lum.astype(np.float64)
+            sat64 = np.zeros(ew * eh, np.float64)
+            orc.lib.or_env_sat_fp64(ptr(lum), ew, eh, ptr(sat64))
+            lum, sat = lum64, sat64
+    else:
+        ew = eh = 1
+        envmap = np.zeros((1, 4), np.float32)
+        lum = np.zeros(1, np.float64 if fp64 else np.float32)
+        sat = lum.copy()
+    if acc is None:
+        acc = np.zeros((W * H, 4), np.float64 if fp64 else np.float32)
+    cam = sc.camera.copy()
+    counts, rays = [], np.zeros(3, np.int64)
+    for f, seeds in enumerate(seeds_list):
+        c = np.zeros(depth, np.int32)
+        rc = np.zeros(3, np.int64)
+        s = None if seeds is None else np.ascontiguousarray(seeds, np.int32)
+        orc.lib.or_render_frame(ptr(cam), W, H, depth, mode, rr, ptr(s), float(first_frame + f), ptr(sc.points),
+                                ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces), sc.ntri, ptr(sc.materials), ptr(nodes),
+                                ptr(bounds), ptr(envmap), ptr(lum), ptr(sat), ew, eh, int(env is not None),
+                                int(fp64), ptr(acc), ptr(c), ptr(rc))
+        counts.append(c)
+        rays += rc
+    return acc, np.stack(counts), rays
+
+
+def rel_rmse(a, b):
+    a = np.asarray(a, np.float64)[:, :3]
+    b = np.asarray(b, np.float64)[:, :3]
+    return float(np.sqrt(np.mean((a - b) ** 2)) / max(np.sqrt(np.mean(b ** 2)), 1e-30))
+
+
+__all__ = ["oracle_trace", "oracle_any", "env_tables", "oracle_frames", "rel_rmse", "bvh_build", "ptr"]

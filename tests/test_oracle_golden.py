@@ -1,0 +1,166 @@
+"""The CPU oracle against golden outputs of MambaTracer's own kernels.
+
+tests/golden/ref_golden.npz holds outputs of the reference kernels (compiled as
+C++ from src/cl/kernel/*.cl, see tests/golden/make_golden.py) on seeded inputs;
+the restatement must reproduce them bit for bit.
+"""
+import numpy as np
+import pytest
+
+from mambatracer_gb300 import layout
+from tests.golden.make_golden import bsdf_material, unit
+from tests.helpers import bvh_build, ptr
+
+
+def beq(a, b):
+    return np.asarray(a).tobytes() == np.asarray(b).tobytes()
+
+
+@pytest.fixture(scope="module")
+def soup_bvh(orc, ginputs):
+    nodes, bounds, depth, _ = bvh_build(orc, ginputs["soup"])
+    return nodes, bounds
+
+
+def test_bvh_is_the_golden_one(soup_bvh, golden):
+    nodes, bounds = soup_bvh
+    sha = np.frombuffer(nodes.tobytes() + bounds.tobytes(), np.uint8).sum(dtype=np.uint64)
+    assert sha == golden["soup_nodes_sha"]
+
+
+@pytest.mark.parametrize("key", ["rays_in", "rays_out"])
+def test_intersect_primitives(orc, ginputs, golden, soup_bvh, key):
+    """IntersectPrimitives (NormalBVH.cl:94-233): hit ids, t, full hit records."""
+    sc = ginputs["soup"]
+    nodes, bounds = soup_bvh
+    rays = ginputs[key].copy()
+    isects = np.zeros(rays.shape[0], layout.INTERSECTION)
+    orc.lib.or_intersect(ptr(rays), ptr(isects), rays.shape[0], rays.shape[0], ptr(sc.points), ptr(sc.uvs),
+                         ptr(sc.normals), ptr(sc.faces), sc.ntri, ptr(nodes), ptr(bounds), None)
+    assert beq(rays["tMax"], golden[key + "_tmax"])
+    ids = np.where(isects["hit"] == 1, isects["id"], -1)
+    assert np.array_equal(ids, golden[key + "_id"])
+    hit = isects["hit"] == 1
+    g = golden[key + "_isect"]
+    assert hit.sum() > 10
+    for f in ("p", "n", "ng", "d", "uv", "mat"):
+        assert beq(isects[f][hit], g[f][hit]), f
+
+
+def test_occlusion(orc, ginputs, golden, soup_bvh):
+    sc = ginputs["soup"]
+    nodes, bounds = soup_bvh
+    rays = ginputs["rays_shadow"]
+    occ = np.zeros(rays.shape[0], np.int32)
+    orc.lib.or_occlusion(ptr(rays), ptr(occ), rays.shape[0], ptr(sc.points), ptr(sc.faces), sc.ntri, ptr(nodes),
+                         ptr(bounds), None)
+    assert occ.sum() > 100
+    assert np.array_equal(occ, golden["rays_shadow_occ"])
+
+
+def test_raygen(orc, ginputs, golden):
+    """InitCameraRayDataJitter (Initialize.cl:129-172)."""
+    cam = ginputs["room"].camera.copy()
+    rays = np.zeros(64 * 48, layout.RAY)
+    seed = np.array([536870923, 805306457], np.int32)
+    orc.lib.or_raygen(ptr(cam), ptr(rays), ptr(seed), 3.0, rays.shape[0], 0)
+    assert beq(rays, golden["raygen_rays"])
+
+
+def test_rng(orc, golden):
+    """WangHash / generate_seed / get_random (Sampling.cl:15-59)."""
+    assert [orc.lib.or_wanghash(i) for i in range(-50, 50)] == golden["wanghash"].tolist()
+    r = np.zeros(64, np.float32)
+    seed = np.array([536870923, 805306457], np.int32)
+    orc.lib.or_random(ptr(seed), 2.0, 12345, 64, ptr(r))
+    assert beq(r, golden["random_64"])
+
+
+def test_bsdf(orc, ginputs, golden):
+    """setupBsdf + SampleBsdf / EvaluateBsdf (Bsdf.cl:130-606), Lambert and GGX."""
+    room = ginputs["room"]
+    n4, d4, w4 = unit(ginputs["bsdf_n"]), unit(ginputs["bsdf_d"]), unit(ginputs["bsdf_w"])
+    res = np.zeros((2000, 12), np.float32)
+    ok = np.zeros((2000, 2), np.int32)
+    for k in range(2000):
+        m = bsdf_material(room, k, ginputs["bsdf_rough"][k])
+        dirv, pdf, c, f, pr = (np.zeros(4, np.float32), np.zeros(1, np.float32), np.zeros(1, np.float32),
+                               np.zeros(4, np.float32), np.zeros(2, np.float32))
+        ok[k, 0] = orc.lib.or_bsdf_sample(ptr(m), ptr(n4[k]), ptr(n4[k]), ptr(d4[k]), ptr(ginputs["bsdf_s"][k]),
+                                          ptr(dirv), ptr(pdf), ptr(c), ptr(f), ptr(pr))
+        res[k, 0:4], res[k, 4], res[k, 5] = dirv, pdf[0], c[0]
+        pdf2, c2, f2 = np.zeros(1, np.float32), np.zeros(1, np.float32), np.zeros(4, np.float32)
+        ok[k, 1] = orc.lib.or_bsdf_eval(ptr(m), ptr(n4[k]), ptr(n4[k]), ptr(d4[k]), ptr(w4[k]), ptr(pdf2), ptr(c2),
+                                        ptr(f2))
+        res[k, 6:10], res[k, 10], res[k, 11] = f2, pdf2[0], c2[0]
+    assert np.array_equal(ok, golden["bsdf_ok"])
+    assert beq(res, golden["bsdf_res"])
+
+
+def test_env_light(orc, ginputs, golden):
+    """Env luminance + SAT (SAT.cl:304-311), illuminateEnvironmentLight (Light.cl:195-227),
+    getRadianceEnvironmentLight (Light.cl:270-286)."""
+    env = ginputs["env"]
+    lum = np.zeros(128 * 64, np.float32)
+    sat = np.zeros(128 * 64, np.float32)
+    orc.lib.or_env_lum_sat(ptr(env), 128, 64, ptr(lum), ptr(sat))
+    assert beq(lum, golden["env_lum"]) and beq(sat, golden["env_sat"])
+    ill = np.zeros((2000, 9), np.float32)
+    rad = np.zeros((2000, 5), np.float32)
+    ed = unit(ginputs["env_d"])
+    for k in range(2000):
+        dirv, pdf, c = np.zeros(4, np.float32), np.zeros(1, np.float32), np.zeros(4, np.float32)
+        orc.lib.or_env_illuminate(ptr(env), ptr(lum), ptr(sat), 128, 64, ptr(ginputs["env_s"][k]), ptr(dirv),
+                                  ptr(pdf), ptr(c))
+        ill[k, 0:4], ill[k, 4], ill[k, 5:9] = dirv, pdf[0], c
+        pdf2, c2 = np.zeros(1, np.float32), np.zeros(4, np.float32)
+        orc.lib.or_env_radiance(ptr(env), ptr(lum), ptr(sat), 128, 64, ptr(ed[k]), ptr(pdf2), ptr(c2))
+        rad[k, 0], rad[k, 1:5] = pdf2[0], c2
+    assert beq(ill, golden["env_illuminate"])
+    assert beq(rad, golden["env_radiance"])
+
+
+def test_lightgrid_sat_spike(orc, golden):
+    """The one hand-checkable SAT in the reference's tests (test/lightgrid/TestSimpleGrid.java:39-67):
+    a single 0.01 at (x=10, y=11) of a 16 x 16 grid; the SAT is 0.01 on x >= 10, y >= 11, else 0."""
+    spike = np.zeros(256, np.float32)
+    spike[11 * 16 + 10] = 0.01
+    out = np.zeros(256, np.float32)
+    orc.lib.or_lightgrid_sat(ptr(spike), ptr(out), 16, 16, 16, 16)
+    expect = np.zeros((16, 16), np.float32)
+    expect[11:, 10:] = np.float32(0.01)
+    assert beq(out, expect.ravel())
+    assert beq(out, golden["spike_sat"])
+
+
+def test_lightgrid_sat_random(orc, ginputs, golden):
+    out = np.zeros(64 * 64, np.float32)
+    orc.lib.or_lightgrid_sat(ptr(ginputs["grid_func"]), ptr(out), 64, 64, 16, 32)
+    assert beq(out, golden["grid_sat"])
+
+
+def test_prefix_sum_fixture(golden):
+    """PrefixSumIntegerTest (test/algorithm/PrefixSumIntegerTest.java:22-38): 200 ones scan to
+    0..199 with total 200 (lane 0 of each group reads aux[-1], taken as 0)."""
+    assert golden["scan200_out"].tolist() == list(range(200))
+    assert int(golden["scan200_total"]) == 200
+
+
+def test_light_list(orc, ginputs, golden):
+    room = ginputs["room"]
+    lf = np.zeros(room.ntri, np.int32)
+    n = orc.lib.or_light_list(ptr(room.faces), room.ntri, ptr(room.materials), ptr(lf))
+    assert n == int(golden["room_lights"]) == 2
+    info = golden["room_light_info"].reshape(-1, 2)
+    assert lf[:n].tolist() == info[:, 0].tolist()
+    assert (info[:, 1] == 1).all()  # AREA_LIGHT
+
+
+def test_frames(orc, ginputs, golden):
+    """Two GI frames (CDeviceGI.loop restated) on the box room: film and queue lengths."""
+    from tests.helpers import oracle_frames
+    room = ginputs["room"]
+    nodes, bounds, _, _ = bvh_build(orc, room)
+    acc, counts, _ = oracle_frames(orc, room, nodes, bounds, 64, 48, 4, 0, 0, list(ginputs["frame_seeds"]))
+    assert np.array_equal(counts, golden["frame_counts"])
+    assert beq(acc, golden["frame_accum"])
