@@ -204,8 +204,10 @@ def run_gpu(args):
     cam = sc.camera.copy()
     job.set_camera(cam)
 
+    from mambatracer_gb300.dist import frame_number
+
     def frame_no(step):
-        return float(1 + step * world + rank)
+        return frame_number(step, rank, world)
 
     def barrier():
         if world > 1:
@@ -299,11 +301,17 @@ def run_gpu(args):
             pass
         peak = float(peaks.get("hbm_gbs", 6800.0))
         t_b1 = per_kernel["trace_closest_b1"]
+        traffic, traffic_src = None, None
+        tp = os.path.join(ROOT, "profiles", "trace_closest_soup1M_1080p.json")
+        if not args.small and os.path.exists(tp):
+            tj = json.load(open(tp))
+            traffic, traffic_src = tj["dram_bytes_per_launch"], tj["source"]
         achieved = alg_bytes / (t_b1 * 1e-3) / 1e9
         roofline = {"bound": "hbm", "kernel": "k_trace_closest (bounce 1, primary rays)",
                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-                    "traffic": None,
+                    "traffic": traffic,
+                    "traffic_source": traffic_src,
                     "alg_bytes_per_launch": alg_bytes, "rays_per_launch": width * height,
                     "interior_visits_per_ray": round(v_int, 2), "triangle_tests_per_ray": round(tri, 2),
                     "launch_ms": round(t_b1, 4),

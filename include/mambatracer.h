@@ -189,6 +189,20 @@ int mt_job_kernel_ms(mt_job* job, float* ms);
 int mt_ctx_event_record(mt_context* ctx, int slot);
 int mt_ctx_event_elapsed(mt_context* ctx, int from_slot, int to_slot, float* ms);
 
+/* --------------------------------------------------- queue compaction */
+
+/* CompactAtomic (src/cl/kernel/Compact.cl:21-40) as CCompact.execute uses it
+ * (src/cl/algorithms/CCompact.java:79-89): keeps the n Intersection records
+ * (96 B each) whose hit flag is set, with their pixel ids, writing them from
+ * slot *count_io onwards in input order, and adds the kept count to
+ * *count_io. All five pointers are device memory (see mt_buf_device_ptr).
+ * Input order is the order a serial run of CompactAtomic produces. The call
+ * returns when the compaction has finished. */
+int mt_compact_isects(mt_context* ctx, const void* isects_in, const int32_t* pixels_in, int n, void* isects_out,
+                      int32_t* pixels_out, int32_t* count_io);
+/* Device address of a buffer, for entry points that take device memory. */
+void* mt_buf_device_ptr(mt_buffer* buf);
+
 /* ------------------------------------------------------- ray queries */
 
 /* Closest hit over n rays in the reference Ray layout (80 B each, tMax is

@@ -13,6 +13,7 @@
 
 #include "../../include/mambatracer.h"
 #include "mt_common.h"
+#include "mt_compact.h"
 #include "mt_device.cuh"
 #include "mt_kernels.h"
 
@@ -63,6 +64,10 @@ struct mt_context {
   std::recursive_mutex mu;
   int* d_scratch = nullptr;  // [0] work counter, [1] error for ray queries
   cudaEvent_t ev[8] = {};
+  // compaction scratch, grown on demand
+  unsigned long long* cs_status = nullptr;
+  int* cs_words = nullptr;
+  size_t cs_tiles = 0;
 };
 
 struct mt_buffer {
@@ -192,6 +197,8 @@ extern "C" int mt_ctx_destroy(mt_context* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   dfree(ctx->d_scratch);
+  dfree(ctx->cs_status);
+  dfree(ctx->cs_words);
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   cudaStreamDestroy(ctx->stream);
@@ -1218,3 +1225,34 @@ extern "C" int mt_kernel_destroy(mt_kernel* k) {
   delete k;
   return MT_OK;
 }
+
+// ------------------------------------------------------------- compaction
+extern "C" int mt_compact_isects(mt_context* ctx, const void* isects_in, const int32_t* pixels_in, int n,
+                                 void* isects_out, int32_t* pixels_out, int32_t* count_io) {
+  if (!ctx || n < 0 || (n > 0 && (!isects_in || !pixels_in || !isects_out || !pixels_out)) || !count_io)
+    return fail(MT_ERR_INVALID, "bad argument");
+  if (n > (1 << 30)) return fail(MT_ERR_INVALID, "n = %d exceeds 2^30", n);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  const size_t tiles = (size_t)(n + kCompactThreads - 1) / kCompactThreads;
+  if (tiles > ctx->cs_tiles || !ctx->cs_words) {
+    CU(cudaStreamSynchronize(ctx->stream));
+    dfree(ctx->cs_status);
+    dfree(ctx->cs_words);
+    ctx->cs_tiles = 0;
+    int r = dalloc(&ctx->cs_status, tiles ? tiles : 1);
+    if (!r) r = dalloc(&ctx->cs_words, 4);
+    if (r) return r;
+    ctx->cs_tiles = tiles ? tiles : 1;
+  }
+  if (launch_compact_isects(ctx->stream, isects_in, pixels_in, n, isects_out, pixels_out, count_io,
+                            CompactScratch{ctx->cs_status, ctx->cs_words}))
+    return fail(MT_ERR_CUDA, "compaction launch: %s", cudaGetErrorString(cudaGetLastError()));
+  int err = 0;
+  CU(cudaMemcpyAsync(&err, ctx->cs_words + 2, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  if (err) return fail(MT_ERR_DEVICE, "compaction: device error %d", err);
+  return MT_OK;
+}
+
+extern "C" void* mt_buf_device_ptr(mt_buffer* b) { return b ? b->ptr : nullptr; }

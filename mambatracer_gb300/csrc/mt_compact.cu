@@ -1,0 +1,70 @@
+// Stable compaction of hit records: CompactAtomic (src/cl/kernel/Compact.cl:21-40)
+// as a single-pass prefix-sum compaction.
+//
+// The reference keeps every Intersection whose hit flag is set and its pixel
+// id, at slot atomic_inc(count): on a GPU the slot order is whatever order the
+// atomics land in; a serial run gives input order. This kernel gives input
+// order always (warp ballot/popc ranks, block scan, decoupled look-back), so
+// its output equals a serial CompactAtomic bit for bit. Slots start at the
+// value *count holds on entry, as atomic_inc's would, and *count ends at
+// entry value + kept.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/mambatracer.h"
+#include "mt_compact.h"
+#include "mt_scan.cuh"
+
+namespace mt {
+
+using namespace scan;
+
+// Intersection (src/cl/kernel/Util.cl:141-151): 96 B = 6 float4, hit at byte 80.
+__global__ void __launch_bounds__(kCompactThreads)
+    k_compact_isects(const float4* __restrict__ in, const int* __restrict__ pix_in, int n, float4* __restrict__ out,
+                     int* __restrict__ pix_out, int* __restrict__ count, unsigned long long* __restrict__ status,
+                     int* __restrict__ tile_counter, const int* __restrict__ base, int* __restrict__ err) {
+  __shared__ unsigned long long sh[kCompactThreads / 32 + 1];
+  __shared__ int s_tile;
+  __shared__ unsigned long long s_excl;
+  const int ntiles = (n + kCompactThreads - 1) / kCompactThreads;
+  if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);
+  __syncthreads();
+  const int tile = s_tile;
+  if (tile >= ntiles) return;
+  const int i = tile * kCompactThreads + threadIdx.x;
+  bool keep = false;
+  if (i < n) keep = __ldg(reinterpret_cast<const int*>(in + 6 * (size_t)i) + 20) != 0;
+  unsigned long long tot;
+  const unsigned long long excl = block_rank2<kCompactThreads>(keep, false, &tot, sh);
+  if (threadIdx.x == 0) s_excl = lookback(status, tile, tot, err);
+  __syncthreads();
+  const int b0 = *base;
+  if (keep) {
+    const size_t slot = (size_t)b0 + (size_t)(s_excl + excl);
+    const float4* src = in + 6 * (size_t)i;
+    float4* dst = out + 6 * slot;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) dst[k] = __ldg(src + k);
+    pix_out[slot] = __ldg(pix_in + i);
+  }
+  if (tile == ntiles - 1 && threadIdx.x == 0) *count = b0 + (int)(s_excl + tot);
+}
+
+int launch_compact_isects(cudaStream_t st, const void* isects_in, const int32_t* pixels_in, int n, void* isects_out,
+                          int32_t* pixels_out, int32_t* count_io, CompactScratch s) {
+  const int ntiles = (n + kCompactThreads - 1) / kCompactThreads;
+  if (cudaMemsetAsync(s.status, 0, sizeof(unsigned long long) * (size_t)(ntiles > 0 ? ntiles : 1), st) != cudaSuccess)
+    return -1;
+  if (cudaMemsetAsync(s.words, 0, 4 * sizeof(int), st) != cudaSuccess) return -1;
+  // words: [0] tile counter, [1] entry value of *count, [2] device error
+  if (cudaMemcpyAsync(s.words + 1, count_io, sizeof(int), cudaMemcpyDeviceToDevice, st) != cudaSuccess) return -1;
+  if (ntiles > 0)
+    k_compact_isects<<<ntiles, kCompactThreads, 0, st>>>(
+        static_cast<const float4*>(isects_in), pixels_in, n, static_cast<float4*>(isects_out), pixels_out, count_io,
+        s.status, s.words, s.words + 1, s.words + 2);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace mt

@@ -15,6 +15,7 @@
 
 #include "mt_device.cuh"
 #include "mt_kernels.h"
+#include "mt_scan.cuh"
 #include "mt_traverse.cuh"
 
 namespace mt {
@@ -23,79 +24,7 @@ using namespace dv;
 
 namespace {
 
-constexpr unsigned long long kFlagAgg = 1ull << 62;
-constexpr unsigned long long kFlagPfx = 2ull << 62;
-constexpr unsigned long long kValMask = (1ull << 62) - 1;
-constexpr unsigned long long kLowMask = (1ull << 31) - 1;
-constexpr int kSpinLimit = 1 << 22;
-
-__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-// Decoupled look-back over tile aggregates (single-pass stable compaction).
-// Returns the exclusive prefix of `tile`. Every wait is bounded: after
-// kSpinLimit polls the error is latched and the partial prefix is used.
-__device__ unsigned long long lookback(unsigned long long* status, int tile, unsigned long long agg, int* err) {
-  if (tile == 0) {
-    st_release(&status[0], kFlagPfx | agg);
-    return 0;
-  }
-  st_release(&status[tile], kFlagAgg | agg);
-  unsigned long long excl = 0;
-  int t = tile - 1;
-  while (t >= 0) {
-    unsigned long long s = 0;
-    int it = 0;
-    for (; it < kSpinLimit; ++it) {
-      s = ld_acquire(&status[t]);
-      if (s >> 62) break;
-      __nanosleep(32);
-    }
-    if (it == kSpinLimit) {
-      atomicExch(err, kDevErrLookback);
-      break;
-    }
-    excl += s & kValMask;
-    if ((s >> 62) == 2) break;
-    --t;
-  }
-  st_release(&status[tile], kFlagPfx | (excl + agg));
-  return excl;
-}
-
-// Block-wide exclusive scan of packed 64-bit counts (kShadeThreads threads).
-__device__ __forceinline__ unsigned long long block_scan(unsigned long long v, unsigned long long* total,
-                                                         unsigned long long* sh) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned long long x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) sh[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    unsigned long long w = lane < kShadeThreads / 32 ? sh[lane] : 0ull;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += y;
-    }
-    if (lane < kShadeThreads / 32) sh[lane] = w;
-  }
-  __syncthreads();
-  unsigned long long warp_excl = warp == 0 ? 0ull : sh[warp - 1];
-  *total = sh[kShadeThreads / 32 - 1];
-  __syncthreads();
-  return warp_excl + x - v;
-}
+using namespace scan;
 
 __device__ __forceinline__ void film_add(float4* __restrict__ acc, float4* __restrict__ comp, int pixel, V v, int kahan) {
   if (!abs_valid4(v)) return;  // addAccum, src/cl/kernel/Render.cl:1-7
@@ -308,7 +237,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene S, DevEnv E, c
   unsigned long long tot = 0;
   int slot = -1, sslot = -1;
   if (MODE == 0) {
-    unsigned long long excl = block_scan(alive ? 1ull : 0ull, &tot, sh);
+    unsigned long long excl = block_rank2<kShadeThreads>(alive, false, &tot, sh);
     if (threadIdx.x == 0) s_base = lookback(status, tile, tot, &ctrl->error);
     __syncthreads();
     slot = (int)(s_base + excl);
@@ -403,8 +332,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene S, DevEnv E, c
   }
 
   if (MODE == 1) {
-    unsigned long long v = (alive ? 1ull : 0ull) | ((has_shadow ? 1ull : 0ull) << 31);
-    unsigned long long excl = block_scan(v, &tot, sh);
+    unsigned long long excl = block_rank2<kShadeThreads>(alive, has_shadow, &tot, sh);
     if (threadIdx.x == 0) s_base = lookback(status, tile, tot, &ctrl->error);
     __syncthreads();
     unsigned long long pos = s_base + excl;
