@@ -80,78 +80,72 @@ __global__ void k_raygen(const PassParams* __restrict__ pp, Ctrl* ctrl, FrameBuf
 }
 
 // ----------------------------------------------------------- traversal
-template <int TOP>
-__global__ void __launch_bounds__(kTraceThreads) k_trace_closest(DevScene S, Ctrl* ctrl, int b, FrameBufs fb) {
-  __shared__ int stack[kStackDepth * kTraceThreads];
-  __shared__ float4 top[TOP > 0 ? 4 * TOP : 1];
-  if (TOP > 0) {
-    int n = 4 * min(TOP, S.nrec);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) top[i] = __ldg(S.nodes + i);
-    __syncthreads();
+namespace {
+struct QueueRays {
+  const float4* qo;
+  const float4* qd;
+  __device__ __forceinline__ tr::RayT operator()(int i) const {
+    return tr::make_ray(__ldg(qo + i), __ldg(qd + i), 0.001f, CUDART_INF_F);  // initGlobalRay, Util.cl:577-587
   }
-  const int count = ctrl->count[b];
-  const int lane = threadIdx.x & 31;
-  const float4* __restrict__ qo = fb.q_o[(b + 1) & 1];
-  const float4* __restrict__ qd = fb.q_d[(b + 1) & 1];
-  int* st = stack + threadIdx.x;
-  bool overflow = false;
-  for (;;) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(&ctrl->work[2 * b], 32);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= count) break;
-    int i = base + lane;
-    if (i < count) {
-      tr::RayT r = tr::make_ray(__ldg(qo + i), __ldg(qd + i), 0.001f, CUDART_INF_F);
-      int prim = tr::traverse<false, TOP>(S, top, r, st, kTraceThreads, &overflow, nullptr);
-      fb.hit_t[i] = r.tmax;
-      fb.hit_prim[i] = prim;
+};
+struct HitOut {
+  float* t;
+  int* prim;
+  __device__ __forceinline__ void operator()(int i, const tr::RayT& r, int hit) const {
+    t[i] = r.tmax;
+    prim[i] = hit;
+  }
+};
+struct ShadowRays {
+  const float4* so;
+  const float4* sd;
+  __device__ __forceinline__ tr::RayT operator()(int i) const {
+    float4 o = __ldg(so + i), d = __ldg(sd + i);
+    // initGlobalRayT (Util.cl:590-600); a slot without a shadow ray (pixel < 0)
+    // gets an empty interval and ends at the first node
+    return tr::make_ray(o, d, 0.0001f, __float_as_int(o.w) >= 0 ? d.w : -CUDART_INF_F);
+  }
+};
+struct ShadowResolve {
+  const float4* so;
+  const float4* sc;
+  float4* film;
+  float4* film_c;
+  int kahan;
+  unsigned* traced;
+  __device__ __forceinline__ void operator()(int i, const tr::RayT&, int hit) const {
+    int pixel = __float_as_int(__ldg(so + i).w);
+    if (pixel < 0) return;
+    ++*traced;
+    if (hit < 0) {  // unoccluded: addAccum(&accum[pixel], contrib), Render.cl:456-461
+      float4 c = __ldg(sc + i);
+      film_add(film, film_c, pixel, mk(c.x, c.y, c.z, 1.f), kahan);
     }
   }
+};
+constexpr int kSteps = 32;
+}  // namespace
+
+__global__ void __launch_bounds__(kTraceThreads, 8) k_trace_closest(DevScene S, Ctrl* ctrl, int b, FrameBufs fb) {
+  const int count = ctrl->count[b];
+  bool overflow = false;
+  tr::trace_persistent<false, kSteps>(S, count, &ctrl->work[2 * b], QueueRays{fb.q_o[(b + 1) & 1], fb.q_d[(b + 1) & 1]},
+                                     HitOut{fb.hit_t, fb.hit_prim}, &overflow);
   if (overflow) atomicExch(&ctrl->error, kDevErrStack);
 }
 
-template <int TOP>
-__global__ void __launch_bounds__(kTraceThreads) k_trace_shadow(DevScene S, Ctrl* ctrl, int b, int mode, FrameBufs fb,
-                                                                int kahan) {
-  __shared__ int stack[kStackDepth * kTraceThreads];
-  __shared__ float4 top[TOP > 0 ? 4 * TOP : 1];
-  if (TOP > 0) {
-    int n = 4 * min(TOP, S.nrec);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) top[i] = __ldg(S.nodes + i);
-    __syncthreads();
-  }
+__global__ void __launch_bounds__(kTraceThreads, 8) k_trace_shadow(DevScene S, Ctrl* ctrl, int b, int mode, FrameBufs fb,
+                                                                   int kahan) {
   // mode 0: shadow slots are the compacted survivor slots (flagged by pixel >= 0)
   const int count = mode == 0 ? ctrl->count[b + 1] : ctrl->shadow[b];
-  const int lane = threadIdx.x & 31;
-  int* st = stack + threadIdx.x;
   bool overflow = false;
   unsigned traced = 0;
-  for (;;) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(&ctrl->work[2 * b + 1], 32);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= count) break;
-    int i = base + lane;
-    if (i < count) {
-      float4 o = __ldg(fb.s_o + i);
-      int pixel = __float_as_int(o.w);
-      if (pixel >= 0) {
-        float4 d = __ldg(fb.s_d + i);
-        tr::RayT r = tr::make_ray(o, d, 0.0001f, d.w);
-        int h = tr::traverse<true, TOP>(S, top, r, st, kTraceThreads, &overflow, nullptr);
-        ++traced;
-        if (h < 0) {
-          float4 c = __ldg(fb.s_c + i);
-          film_add(fb.film, fb.film_c, pixel, mk(c.x, c.y, c.z, 1.f), kahan);
-        }
-      }
-    }
-  }
+  tr::trace_persistent<true, kSteps>(S, count, &ctrl->work[2 * b + 1], ShadowRays{fb.s_o, fb.s_d},
+                                    ShadowResolve{fb.s_o, fb.s_c, fb.film, fb.film_c, kahan, &traced}, &overflow);
   unsigned long long tot = traced;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
-  if (lane == 0 && tot) atomicAdd(&ctrl->rays[2], tot);
+  if ((threadIdx.x & 31) == 0 && tot) atomicAdd(&ctrl->rays[2], tot);
   if (overflow) atomicExch(&ctrl->error, kDevErrStack);
 }
 
@@ -386,10 +380,9 @@ __global__ void k_accumulate(const Ctrl* ctrl, int max_depth, int n_pixels, unsi
 
 // ---------------------------------------------------------------- launchers
 namespace {
-template <int TOP>
 int trace_blocks_per_sm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest<TOP>, kTraceThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest, kTraceThreads, 0);
   return n > 0 ? n : 1;
 }
 }  // namespace
@@ -398,9 +391,8 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
                 int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb, unsigned long long* status,
                 size_t status_stride, int num_sms, cudaEvent_t* ev, unsigned long long* totals) {
   const int N = width * height;
-  constexpr int TOP = 256;
   static int bps = 0;
-  if (bps == 0) bps = trace_blocks_per_sm<TOP>();
+  if (bps == 0) bps = trace_blocks_per_sm();
   const int trace_grid = num_sms * bps;
   const int tiles = (N + kShadeThreads - 1) / kShadeThreads;
   int e = 0;
@@ -408,7 +400,7 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
   k_raygen<<<(N + 255) / 256, 256, 0, st>>>(d_pp, ctrl, fb);
   if (ev) cudaEventRecord(ev[e++], st);
   for (int b = 1; b <= max_depth; ++b) {
-    k_trace_closest<TOP><<<trace_grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb);
+    k_trace_closest<<<trace_grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb);
     if (ev) cudaEventRecord(ev[e++], st);
     unsigned long long* stb = status + (size_t)(b - 1) * status_stride;
     if (mode == 0)
@@ -416,7 +408,7 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
     else
       k_shade<1><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
     if (ev) cudaEventRecord(ev[e++], st);
-    k_trace_shadow<TOP><<<trace_grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan);
+    k_trace_shadow<<<trace_grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan);
     if (ev) cudaEventRecord(ev[e++], st);
   }
   if (totals) k_accumulate<<<1, 32, 0, st>>>(ctrl, max_depth, N, totals);
@@ -424,33 +416,38 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
 }
 
 // Ray queries on reference-layout rays (80 B): closest or any hit.
-__global__ void __launch_bounds__(kTraceThreads) k_query(DevScene S, const float4* __restrict__ rays, int n, int any,
-                                                         float* __restrict__ t_out, int* __restrict__ prim_out,
-                                                         int* work, int* err) {
-  __shared__ int stack[kStackDepth * kTraceThreads];
-  const int lane = threadIdx.x & 31;
-  int* st = stack + threadIdx.x;
-  bool overflow = false;
-  for (;;) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(work, 32);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= n) break;
-    int i = base + lane;
-    if (i < n) {
-      const float4* R = rays + 5 * (size_t)i;  // Ray: o, d, inv_d, sign, (extra, tMin, tMax)
-      float4 o = __ldg(R + 0), d = __ldg(R + 1), tail = __ldg(R + 4);
-      tr::RayT r = tr::make_ray(o, d, tail.z, tail.w);
-      if (any) {
-        int h = tr::traverse<true, 0>(S, nullptr, r, st, kTraceThreads, &overflow, nullptr);
-        prim_out[i] = h >= 0 ? 1 : 0;
-      } else {
-        int h = tr::traverse<false, 0>(S, nullptr, r, st, kTraceThreads, &overflow, nullptr);
-        t_out[i] = r.tmax;
-        prim_out[i] = h;
-      }
+namespace {
+struct RefRays {
+  const float4* rays;
+  __device__ __forceinline__ tr::RayT operator()(int i) const {
+    const float4* R = rays + 5 * (size_t)i;  // Ray: o, d, inv_d, sign, (extra, tMin, tMax)
+    float4 o = __ldg(R + 0), d = __ldg(R + 1), tail = __ldg(R + 4);
+    return tr::make_ray(o, d, tail.z, tail.w);
+  }
+};
+struct QueryOut {
+  int any;
+  float* t;
+  int* prim;
+  __device__ __forceinline__ void operator()(int i, const tr::RayT& r, int hit) const {
+    if (any) {
+      prim[i] = hit >= 0 ? 1 : 0;
+    } else {
+      t[i] = r.tmax;
+      prim[i] = hit;
     }
   }
+};
+}  // namespace
+
+__global__ void __launch_bounds__(kTraceThreads, 8) k_query(DevScene S, const float4* __restrict__ rays, int n, int any,
+                                                            float* __restrict__ t_out, int* __restrict__ prim_out,
+                                                            int* work, int* err) {
+  bool overflow = false;
+  if (any)
+    tr::trace_persistent<true, kSteps>(S, n, work, RefRays{rays}, QueryOut{1, t_out, prim_out}, &overflow);
+  else
+    tr::trace_persistent<false, kSteps>(S, n, work, RefRays{rays}, QueryOut{0, t_out, prim_out}, &overflow);
   if (overflow) atomicExch(err, kDevErrStack);
 }
 

@@ -110,6 +110,132 @@ struct TraceStats {
   unsigned int interior, tris;
 };
 
+// Branch-free slab test for rays whose origin and 1/d are finite. With no
+// NaN possible, the reference's comparison chain (Util.cl:707-732) reduces to
+// max(near) <= min(far) on the three axes (near <= far holds per axis for a
+// valid box), and fmaxf/fminf give the same values; the sign of a zero
+// distance, which fmaxf may choose differently, never changes a comparison.
+// n*/f*: the near and far planes already picked by the direction sign.
+__device__ __forceinline__ bool slab_fast(const RayT& r, float nx, float fx, float ny, float fy, float nz, float fz,
+                                          float* tnear) {
+  float tmin = fmaxf(fmaxf((nx - r.ox) * r.ix, (ny - r.oy) * r.iy), (nz - r.oz) * r.iz);
+  float tmax = fminf(fminf((fx - r.ox) * r.ix, (fy - r.oy) * r.iy), (fz - r.oz) * r.iz);
+  *tnear = tmin;
+  return (tmin <= tmax) && (tmin < r.tmax) && (tmax * 1.00000024f > r.tmin);
+}
+
+__device__ __forceinline__ bool ray_is_finite(const RayT& r) {
+  return isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz) && isfinite(r.ox) && isfinite(r.oy) && isfinite(r.oz);
+}
+
+// Resumable traversal in the reference's visit order (see the file header).
+// Deferred children sit on a per-thread stack of (ref, entry distance). For
+// finite rays a deferred interior node whose entry distance is not below the
+// current closest hit is dropped when popped: its children's boxes nest in its
+// box and the slab arithmetic is monotonic, so both would miss and the
+// reference would test no triangle under it. Deferred leaves are always tested.
+// Runs at most `steps` node visits or triangle tests; returns true when the
+// ray is finished (hit_face / r.tmax hold the result).
+template <bool ANY>
+__device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref, int& sp, int& hit_face, bool finite,
+                                           int2* stack, int steps, bool* overflow) {
+  const float4* __restrict__ nodes = S.nodes;
+  const float4* __restrict__ tris = S.tris;
+  for (int it = 0; it < steps; ++it) {
+    if (ref >= 0) {
+      const float4* p = nodes + 4 * (size_t)ref;
+      float4 n0 = __ldg(p + 0), n1 = __ldg(p + 1), n2 = __ldg(p + 2), n3 = __ldg(p + 3);
+      float tl, trr;
+      bool hl, hr;
+      if (finite) {
+        hl = slab_fast(r, r.sx ? n0.y : n0.x, r.sx ? n0.x : n0.y, r.sy ? n0.w : n0.z, r.sy ? n0.z : n0.w,
+                       r.sz ? n2.y : n2.x, r.sz ? n2.x : n2.y, &tl);
+        hr = slab_fast(r, r.sx ? n1.y : n1.x, r.sx ? n1.x : n1.y, r.sy ? n1.w : n1.z, r.sy ? n1.z : n1.w,
+                       r.sz ? n2.w : n2.z, r.sz ? n2.z : n2.w, &trr);
+      } else {
+        hl = slab(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, &tl);
+        hr = slab(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, &trr);
+      }
+      const int left = __float_as_int(n3.x), right = __float_as_int(n3.y);
+      if (hl && hr) {
+        const bool rfirst = trr < tl;
+        if (sp >= kStackDepth) {
+          *overflow = true;
+          return true;
+        }
+        stack[sp++] = make_int2(rfirst ? left : right, __float_as_int(rfirst ? tl : trr));
+        ref = rfirst ? right : left;
+        continue;
+      }
+      if (hl) { ref = left; continue; }
+      if (hr) { ref = right; continue; }
+    } else {
+      const float4* tp = tris + 3 * (size_t)(~ref);
+      float4 p1 = __ldg(tp + 0), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+      float t = tri_t(r, p1, e1, e2);
+      if ((r.tmin < t) && (t < r.tmax)) {
+        hit_face = __float_as_int(p1.w);
+        if (ANY) return true;
+        r.tmax = t;
+      }
+    }
+    for (;;) {
+      if (sp == 0) return true;
+      int2 e = stack[--sp];
+      if (ANY || !finite || e.x < 0 || __int_as_float(e.y) < r.tmax) {
+        ref = e.x;
+        break;
+      }
+    }
+  }
+  return false;
+}
+
+// Persistent traversal over `count` rays with per-lane refill: every lane that
+// finished its ray takes the next one from the global counter, so warps stay
+// full while rays of very different lengths run side by side.
+// Src: RayT load(int i); Dst: void store(int i, const RayT&, int hit_face).
+template <bool ANY, int STEPS, class Src, class Dst>
+__device__ __forceinline__ void trace_persistent(const DevScene& S, int count, int* work, Src src, Dst dst,
+                                                 bool* overflow) {
+  const int lane = threadIdx.x & 31;
+  int2 stack[kStackDepth];
+  int i = -1;
+  bool exhausted = false;
+  RayT r;
+  int ref = 0, sp = 0, hit = -1;
+  bool finite = true;
+  for (;;) {
+    const bool need = (i < 0) && !exhausted;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(work, __popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const int k = base + __popc(m & ((1u << lane) - 1u));
+        if (k < count) {
+          i = k;
+          r = src(i);
+          finite = ray_is_finite(r);
+          ref = S.root_ref;
+          sp = 0;
+          hit = -1;
+        }
+      }
+      if (base + __popc(m) >= count) exhausted = true;
+    }
+    const bool active = i >= 0;
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active && trav_steps<ANY>(S, r, ref, sp, hit, finite, stack, STEPS, overflow)) {
+      dst(i, r, hit);
+      i = -1;
+    }
+  }
+}
+
+
 // Closest hit (ANY = false) or any hit (ANY = true). stack: this thread's
 // column of a [depth][threads] shared array. Returns the hit face id or -1; on
 // a closest hit r.tmax holds the hit distance. *overflow is set when the

@@ -37,7 +37,7 @@ def test_dense_soup(ctx, orc, inside):
     rays = layout.make_rays(o, d)
     t, p = S.trace_closest(rays)
     to, po = oracle_trace(orc, sc, nodes, bounds, rays)
-    assert (po >= 0).sum() > 20000
+    assert (po >= 0).sum() > (20000 if inside else 3000)
     assert np.array_equal(p, po)
     assert t.tobytes() == to.tobytes()
     rays2 = layout.make_rays(o, d, tmin=1e-4, tmax=0.2)
@@ -54,7 +54,7 @@ def test_primary_rays_box_room(ctx, orc):
     t, p = S.trace_closest(rays)
     to, po = oracle_trace(orc, sc, nodes, bounds, rays)
     assert np.array_equal(p, po) and t.tobytes() == to.tobytes()
-    assert (p >= 0).mean() > 0.9
+    assert (p >= 0).mean() > 0.7  # the open front of the room shows the background
     S.close()
 
 
@@ -88,7 +88,7 @@ def test_single_triangle(ctx, orc):
     room = scenes.box_room(8, 8)
     sc = scenes.Scene(points=room.points[:3].copy(), faces=room.faces[:1].copy(), materials=room.materials)
     S, nodes, bounds = gpu_scene(ctx, orc, sc)
-    o = np.tile(np.array([[0.3, 0.5, 0.2]], np.float32), (4, 1))
+    o = np.tile(np.array([[0.3, 0.5, 0.6]], np.float32), (4, 1))  # above (0.3, 0, 0.6), inside the triangle
     d = np.array([[0, -1, 0], [0, 1, 0], [1, 0, 0], [0, -1, 0.0001]], np.float32)
     rays = layout.make_rays(o, d)
     t, p = S.trace_closest(rays)
@@ -99,7 +99,7 @@ def test_single_triangle(ctx, orc):
 
 def test_too_deep_bvh_is_rejected(ctx):
     """The reference traversal keeps a 64-bit bitstack (NormalBVH.cl:20); deeper trees are refused."""
-    k = 80
+    k = 120  # depth 71 with this spacing
     pts = []
     for i in range(k):
         x = 2.0 ** (-i)
