@@ -202,6 +202,20 @@ int mt_compact_isects(mt_context* ctx, const void* isects_in, const int32_t* pix
                       int32_t* pixels_out, int32_t* count_io);
 /* Device address of a buffer, for entry points that take device memory. */
 void* mt_buf_device_ptr(mt_buffer* buf);
+/* The same compaction for callers that cannot allocate device memory (a host
+ * whose device memory all belongs to another allocator, or a plugin that may
+ * not allocate on its caller's behalf). No counterpart in the reference. It
+ * needs no context and allocates nothing: its scratch is a fixed array inside
+ * the library (128 KiB per GPU that loads it), so n may be at most 4194304
+ * records; larger n is refused with MT_ERR_INVALID. The caller passes inputs
+ * and outputs in device memory and a CUDA stream (NULL: the default stream);
+ * the call returns when the compaction on that stream has finished. The first
+ * call on a device looks up the scratch array's device address, so make it
+ * before any stream capture. Every call uses the same array: calls that overlap
+ * on the GPU (other streams, other host threads) race. Errors read through
+ * mt_last_error(). */
+int mt_compact_isects_noalloc(void* stream, const void* isects_in, const int32_t* pixels_in, int n,
+                              void* isects_out, int32_t* pixels_out, int32_t* count_io);
 
 /* ------------------------------------------------------- ray queries */
 

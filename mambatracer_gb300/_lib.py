@@ -81,6 +81,7 @@ SIGNATURES = {
     "mt_ctx_event_elapsed": (I, [P, I, I, C.POINTER(C.c_float)]),
     "mt_compact_isects": (I, [P, P, P, I, P, P, P]),
     "mt_buf_device_ptr": (P, [P]),
+    "mt_compact_isects_noalloc": (I, [P, P, P, I, P, P, P]),
     "mt_trace_closest": (I, [P, P, I, P, P]),
     "mt_trace_any": (I, [P, P, I, P]),
     "mt_trace_closest_dev": (I, [P, P, I, P, P, C.POINTER(C.c_float)]),

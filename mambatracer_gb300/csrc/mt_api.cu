@@ -157,6 +157,10 @@ struct mt_job {
 // ------------------------------------------------------------------ context
 extern "C" const char* mt_last_error(void) { return g_err.c_str(); }
 
+namespace mt {
+__attribute__((visibility("hidden"))) void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace mt
+
 extern "C" const char* mt_version(void) {
   return "mambatracer-gb300 sm_103a fmad=false prec-div prec-sqrt";
 }

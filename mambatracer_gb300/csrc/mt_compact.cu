@@ -67,4 +67,73 @@ int launch_compact_isects(cudaStream_t st, const void* isects_in, const int32_t*
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+// ------------------------------------------------------- no-allocation variant
+// For callers that cannot call cudaMalloc: a host whose device memory all
+// belongs to another allocator (a JVM-side pool, or a framework's caching
+// allocator that would first have to give memory back), or a plugin that may
+// not allocate on its caller's behalf. The compaction's scratch (one status
+// word per 256-record tile plus four counters) is this file-scope array, sized
+// for kNoAllocMaxRecords records; every GPU that loads the library holds it
+// (128 KiB) until the process exits.
+constexpr int kNoAllocMaxRecords = 1 << 22;
+constexpr int kNoAllocTiles = kNoAllocMaxRecords / kCompactThreads;
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocTiles + 2];
+
 }  // namespace mt
+
+#include <mutex>
+#include <string>
+
+namespace mt {
+__attribute__((visibility("hidden"))) void set_last_error(const char* msg);  // read by mt_last_error()
+}
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned long long* g_noalloc_addr[kMaxDevices] = {};
+
+int noalloc_fail(int code, const char* msg, cudaError_t e = cudaSuccess) {
+  std::string m = msg;
+  if (e != cudaSuccess) {
+    m += ": ";
+    m += cudaGetErrorString(e);
+  }
+  mt::set_last_error(m.c_str());
+  return code;
+}
+}  // namespace
+
+extern "C" int mt_compact_isects_noalloc(void* stream, const void* isects_in, const int32_t* pixels_in, int n,
+                                         void* isects_out, int32_t* pixels_out, int32_t* count_io) {
+  if (n < 0 || (n > 0 && (!isects_in || !pixels_in || !isects_out || !pixels_out)) || !count_io)
+    return noalloc_fail(MT_ERR_INVALID, "bad argument");
+  if (n > mt::kNoAllocMaxRecords)
+    return noalloc_fail(MT_ERR_INVALID, "n exceeds the 4194304 records the static scratch holds");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return noalloc_fail(MT_ERR_CUDA, "cudaGetDevice", e);
+  if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(MT_ERR_INVALID, "device index out of range");
+  unsigned long long* scratch;
+  {
+    // Set-up on the first call on each device, with that device current.
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, mt::g_noalloc_scratch);
+      if (e != cudaSuccess || !p) return noalloc_fail(MT_ERR_CUDA, "cudaGetSymbolAddress", e);
+      g_noalloc_addr[dev] = static_cast<unsigned long long*>(p);
+    }
+    scratch = g_noalloc_addr[dev];
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  mt::CompactScratch s{scratch, reinterpret_cast<int*>(scratch + mt::kNoAllocTiles)};
+  if (mt::launch_compact_isects(st, isects_in, pixels_in, n, isects_out, pixels_out, count_io, s))
+    return noalloc_fail(MT_ERR_CUDA, "compaction launch", cudaGetLastError());
+  int err = 0;
+  e = cudaMemcpyAsync(&err, s.words + 2, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return noalloc_fail(MT_ERR_CUDA, "compaction", e);
+  if (err) return noalloc_fail(MT_ERR_DEVICE, "compaction: a bounded wait ran out");
+  return MT_OK;
+}
