@@ -45,7 +45,7 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def config_dict(width, height, ntri, world):
+def config_dict(width, height, ntri, world, inflight=1):
     return {
         "workload": WORKLOAD if (width, height, ntri) == (W_DEFAULT, H_DEFAULT, NTRI) else
         f"soup{ntri}_{width}x{height}_depth{DEPTH}_rr{RR}_env{ENV_W}x{ENV_H}",
@@ -53,7 +53,7 @@ def config_dict(width, height, ntri, world):
         "environment": f"{ENV_W}x{ENV_H} FP32 lat-long sky gradient + 0.5 deg Gaussian sun (peak 5e4); SAT built in FP64",
         "resolution": f"{width}x{height}", "spp_per_step": 1, "max_depth": DEPTH, "rr_from_bounce": RR,
         "rng": "per-pixel seed pixel ^ 0x9E3779B9 into the reference WangHash chain",
-        "film": "FP32 Kahan-compensated", "launch": "CUDA graph per frame",
+        "film": "FP32 Kahan-compensated", "launch": "CUDA graph per frame" + (f", {inflight} frames in flight on separate streams" if inflight > 1 else ""),
         "l2": "no flush: per-step working set (path state + queues ~420 MB, BVH+triangles 112 MB) exceeds the 129 MB L2",
         "parallelism": f"replicas x{world} (pixels/frames independent, no collective)",
     }
@@ -200,7 +200,8 @@ def run_gpu(args):
     S = api.Scene(ctx, sc)
     nodes, bounds = S.build_bvh()
     S.set_env(env, ENV_W, ENV_H)
-    job = api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, use_graph=1)
+    job = api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, use_graph=1,
+                  inflight=args.inflight)
     cam = sc.camera.copy()
     job.set_camera(cam)
 
@@ -244,19 +245,23 @@ def run_gpu(args):
     import ctypes as C
 
     from mambatracer_gb300._lib import check, lib
-    film_host = torch.empty((width * height, 4), dtype=torch.float32, pin_memory=True)
+    nbuf = 5  # read i completes when read i + 4 is enqueued (four stay pending): its buffer is free for read i + 5
+    film_host = [torch.empty((width * height, 4), dtype=torch.float32, pin_memory=True) for _ in range(nbuf)]
     cam_host = torch.empty(64, dtype=torch.uint8, pin_memory=True)
     cam_host.numpy()[:] = np.frombuffer(cam.tobytes(), np.uint8)
     L = lib()
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = args.steps
     job.clear()
     barrier()
     ctx.finish()
     t0 = time.perf_counter()
     for i in range(e2e_steps):
+        # camera in, frame submitted, the film after this frame read back while
+        # the next frames render (a ring of pinned host films)
         check(L.mt_job_set_camera(job.h, C.c_void_p(cam_host.data_ptr())))
         check(L.mt_render_frame(job.h, None, frame_no(10000 + i)))
-        check(L.mt_film_read(job.h, C.c_void_p(film_host.data_ptr()), 0))
+        check(L.mt_film_read_async(job.h, C.c_void_p(film_host[i % nbuf].data_ptr()), 0))
+    check(L.mt_film_wait(job.h))
     e2e_s = time.perf_counter() - t0
     e2e_rays = int(job.total_rays().sum())
     if world > 1:
@@ -268,7 +273,8 @@ def run_gpu(args):
         e2e_rays = int(rr.item())
     e2e = {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s",
            "h2d_bytes_per_step": 64 + 416, "d2h_bytes_per_step": width * height * 16,
-           "note": "camera (64 B) and the pass parameters (416 B) in, the float4 film out, per frame"}
+           "note": ("camera (64 B) and the pass parameters (416 B) in, the float4 film after each frame out "
+                    "(mt_film_read_async into a ring of pinned buffers), per frame")}
 
     out = None
     if rank == 0:
@@ -332,10 +338,11 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (procedural soup and sky; no dataset)",
-            "config": config_dict(width, height, ntri, world),
+            "config": config_dict(width, height, ntri, world, args.inflight),
             "rays_per_step": round(total_rays / args.steps / world), "rays_split": rays.tolist(),
             "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e,
-            "gpu_launches": args.steps * (2 + 3 * DEPTH), "clocks": clk,
+            "gpu_launches": args.steps * (2 + 3 * DEPTH + (1 if args.inflight > 1 else 0)), "clocks": clk,
+            "inflight_frames": args.inflight,
             "msamples_per_s": round(width * height * args.steps * world / (ms * 1e-3) / 1e6, 2),
             "bvh_depth": S.depth, "alg_bytes_seconds": round(t_alg, 1),
         }
@@ -392,6 +399,7 @@ def main():
     ap.add_argument("--impl", default="mambatracer", choices=["mambatracer", "reference"])
     ap.add_argument("--small", action="store_true", help="small case for profiler captures")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--inflight", type=int, default=4, help="frames kept in flight on separate streams (1..4)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

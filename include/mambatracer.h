@@ -154,6 +154,9 @@ typedef struct mt_render_config {
   int spp;           /* passes per mt_render_frame call */
   int use_graph;     /* 1 = replay each frame's launches as a CUDA graph */
   int profile;       /* 1 = time every kernel launch with CUDA events (no graph) */
+  int inflight;      /* frames kept in flight on their own streams, 0 or 1 = one (1..4); each
+                        in-flight frame has its own path state and film, summed on read.
+                        profile = 1 forces one. */
 } mt_render_config;
 
 /* A render job: film + path state resident on the device (CDeviceGI.setup,
@@ -170,6 +173,15 @@ int mt_render_frame(mt_job* job, const int32_t* seeds, float frame_count);
 /* CImage film: accum (float4 per pixel). resolve != 0 divides by the frame
  * count as averageAccum does (src/cl/kernel/Image.cl:29-67). */
 int mt_film_read(mt_job* job, float* rgba, int resolve);
+/* The same read, enqueued: copies the film as of every frame submitted so far
+ * into rgba (pinned host memory for an asynchronous copy) and returns at once,
+ * so the next frames can be submitted while this one finishes. Up to four
+ * reads stay pending; a fifth first completes the oldest. rgba must stay valid
+ * until its read completes (mt_film_wait, mt_film_read, mt_film_clear, or the
+ * fifth read after it); resolve is applied then. No counterpart in the
+ * reference, whose image read (CImage.processImage/readImage) blocks. */
+int mt_film_read_async(mt_job* job, float* rgba, int resolve);
+int mt_film_wait(mt_job* job);
 int mt_film_clear(mt_job* job);
 /* Rays traced so far: [primary, extension, shadow], and the live queue length
  * after each bounce of the last pass (max_depth ints). */

@@ -127,8 +127,10 @@ class Job:
     """Film and path state of one render job resident on the device."""
 
     def __init__(self, ctx: Context, scene: Scene, width: int, height: int, max_depth: int = 15, mode: int = 0,
-                 rr_depth: int = 0, film_kahan: int = 1, spp: int = 1, use_graph: int = 0, profile: int = 0):
-        self.cfg = RenderConfig(width, height, max_depth, mode, rr_depth, film_kahan, spp, use_graph, profile)
+                 rr_depth: int = 0, film_kahan: int = 1, spp: int = 1, use_graph: int = 0, profile: int = 0,
+                 inflight: int = 1):
+        self.cfg = RenderConfig(width, height, max_depth, mode, rr_depth, film_kahan, spp, use_graph, profile,
+                                inflight)
         h = C.c_void_p()
         check(lib().mt_job_create(ctx.h, scene.h, C.byref(self.cfg), C.byref(h)))
         self.h = h
@@ -148,6 +150,17 @@ class Job:
         out = np.zeros((self.width * self.height, 4), np.float32)
         check(lib().mt_film_read(self.h, _p(out), int(resolve)))
         return out
+
+    def film_async(self, out: np.ndarray, resolve: bool = False):
+        """Enqueue a read of the film into `out` (float32, width*height x 4; pinned
+        memory for a copy that overlaps the next frame); complete it with wait()."""
+        assert out.dtype == np.float32 and out.size == self.width * self.height * 4 and out.flags.c_contiguous
+        self._pending = (getattr(self, "_pending", []) + [out])[-4:]
+        check(lib().mt_film_read_async(self.h, _p(out), int(resolve)))
+
+    def wait(self):
+        check(lib().mt_film_wait(self.h))
+        self._pending = []
 
     def clear(self):
         check(lib().mt_film_clear(self.h))

@@ -11,19 +11,20 @@
 #include <string>
 #include <vector>
 
-#include "../../include/mambatracer.h"
-#include "mt_common.h"
 #include "mt_compact.h"
 #include "mt_device.cuh"
-#include "mt_kernels.h"
+#include "mt_internal.h"
 
-using namespace mt;
-
-// ------------------------------------------------------------------ errors
+// ------------------------------------------------------------------ context
 namespace {
 thread_local std::string g_err;
+}
 
-int fail(int code, const char* fmt, ...) {
+extern "C" const char* mt_last_error(void) { return g_err.c_str(); }
+
+namespace mt {
+__attribute__((visibility("hidden"))) void set_last_error(const char* msg) { g_err = msg; }
+__attribute__((visibility("hidden"))) int fail(int code, const char* fmt, ...) {
   char buf[512];
   va_list ap;
   va_start(ap, fmt);
@@ -32,134 +33,15 @@ int fail(int code, const char* fmt, ...) {
   g_err = buf;
   return code;
 }
-#define CU(call)                                                                         \
-  do {                                                                                   \
-    cudaError_t e_ = (call);                                                             \
-    if (e_ != cudaSuccess) return fail(MT_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
-  } while (0)
-
-template <class T>
-int dalloc(T** p, size_t count) {
-  *p = nullptr;
-  if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return fail(MT_ERR_NOMEM, "cudaMalloc(%zu B): %s", count * sizeof(T), cudaGetErrorString(e));
-  }
-  return MT_OK;
-}
-template <class T>
-void dfree(T*& p) {
-  if (p) cudaFree((void*)p);
-  p = nullptr;
-}
-}  // namespace
-
-// ----------------------------------------------------------------- structs
-struct mt_context {
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t stream = nullptr;
-  std::recursive_mutex mu;
-  int* d_scratch = nullptr;  // [0] work counter, [1] error for ray queries
-  cudaEvent_t ev[8] = {};
-  // compaction scratch, grown on demand
-  unsigned long long* cs_status = nullptr;
-  int* cs_words = nullptr;
-  size_t cs_tiles = 0;
-};
-
-struct mt_buffer {
-  mt_context* ctx;
-  void* ptr;
-  size_t bytes;
-};
-
-struct mt_scene {
-  mt_context* ctx;
-  int npoints = 0, nuvs = 0, nnormals = 0, ntri = 0, nmat = 0;
-  std::vector<float> h_points;
-  std::vector<int32_t> h_faces;
-  std::vector<uint8_t> h_materials;
-  float4* d_points = nullptr;
-  float2* d_uvs = nullptr;
-  float4* d_normals = nullptr;
-  Face* d_faces = nullptr;
-  Material* d_materials = nullptr;
-  int* d_light_faces = nullptr;
-  int nlights = 0;
-  // traversal layout
-  float4* d_nodes = nullptr;
-  float4* d_tris = nullptr;
-  int nrec = 0, root_ref = 0, depth = 0, has_bvh = 0, precision = 0;
-  // environment
-  float4* d_env_rgb = nullptr;
-  float* d_env_lum = nullptr;
-  float* d_env_sat = nullptr;
-  double* d_env_sat64 = nullptr;
-  int env_w = 0, env_h = 0, env_present = 0;
-  int grid_nu = 1600, grid_nv = 1600, grid_rx = 16, grid_ry = 32, grid_on = 0;
-
-  DevScene view() const {
-    DevScene s{};
-    s.nodes = d_nodes;
-    s.qnodes = nullptr;
-    s.tris = d_tris;
-    s.root_ref = root_ref;
-    s.ntri = ntri;
-    s.nrec = nrec;
-    s.precision = precision;
-    s.points = d_points;
-    s.uvs = d_uvs;
-    s.normals = d_normals;
-    s.faces = d_faces;
-    s.materials = d_materials;
-    s.light_faces = d_light_faces;
-    s.nlights = nlights;
-    return s;
-  }
-  DevEnv env_view() const {
-    DevEnv e{};
-    e.rgb = d_env_rgb;
-    e.lum = d_env_lum;
-    e.sat = d_env_sat;
-    e.w = env_w;
-    e.h = env_h;
-    e.present = env_present;
-    e.grid_on = 0;
-    return e;
-  }
-};
-
-struct mt_job {
-  mt_context* ctx;
-  mt_scene* scene;
-  mt_render_config cfg;
-  FrameBufs fb{};
-  Ctrl* d_ctrl = nullptr;  // one per pass
-  unsigned long long* d_status = nullptr;
-  size_t status_stride = 0;
-  PassParams* h_pp = nullptr;  // pinned, 2 sets of one per pass (alternating frames)
-  PassParams* d_pp = nullptr;  // 2 sets of one per pass
-  unsigned char camera[64];
-  int has_camera = 0;
-  double frames = 0;  // passes accumulated in the film
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t done[2] = {nullptr, nullptr};  // frame completion per parameter set
-  int slot = 0;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  std::vector<cudaEvent_t> kev;  // profile: 2 + 3 * max_depth per pass
-  unsigned long long* d_totals = nullptr;  // running [primary, extension, shadow, error]
-  std::vector<Ctrl> h_ctrl;
-};
-
-// ------------------------------------------------------------------ context
-extern "C" const char* mt_last_error(void) { return g_err.c_str(); }
-
-namespace mt {
-__attribute__((visibility("hidden"))) void set_last_error(const char* msg) { g_err = msg; }
 }  // namespace mt
+
+void join_jobs(mt_context* ctx) {
+  for (mt_job* j : ctx->jobs) {
+    for (JobSlot& s : j->slots)
+      if (s.done) cudaStreamWaitEvent(ctx->stream, s.done, 0);
+    if (j->rdone) cudaStreamWaitEvent(ctx->stream, j->rdone, 0);
+  }
+}
 
 extern "C" const char* mt_version(void) {
   return "mambatracer-gb300 sm_103a fmad=false prec-div prec-sqrt";
@@ -214,6 +96,7 @@ extern "C" int mt_ctx_event_record(mt_context* ctx, int slot) {
   if (!ctx || slot < 0 || slot >= 8) return fail(MT_ERR_INVALID, "bad event slot");
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   CU(cudaSetDevice(ctx->device));
+  join_jobs(ctx);
   CU(cudaEventRecord(ctx->ev[slot], ctx->stream));
   return MT_OK;
 }
@@ -230,6 +113,7 @@ extern "C" int mt_finish(mt_context* ctx) {
   if (!ctx) return fail(MT_ERR_INVALID, "ctx is NULL");
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   CU(cudaSetDevice(ctx->device));
+  join_jobs(ctx);
   CU(cudaStreamSynchronize(ctx->stream));
   return MT_OK;
 }
@@ -793,351 +677,6 @@ extern "C" int mt_env_grid_sat(mt_context* ctx, const float* func, float* sat_ou
   dfree(d_sat);
   dfree(d_sat64);
   return r;
-}
-
-// -------------------------------------------------------------------- jobs
-namespace {
-
-struct CamF {
-  float position[4], lookat[4], up[4], dimension[2], fov, pad;
-};
-
-// Camera constants of InitCameraRayDataJitter (Initialize.cl:129-172) and
-// camera_transform (Matrix.cl:216-241), computed once per pass on the host in
-// FP32 with the reference's operation order.
-void camera_constants(const CamF& c, int W, int H, PassParams& pp) {
-  auto dot4 = [](const float* a, const float* b) { return ((a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]) + a[3] * b[3]; };
-  auto norm4 = [&](float* v) {
-    float l = std::sqrt(dot4(v, v));
-    for (int i = 0; i < 4; ++i) v[i] = v[i] / l;
-  };
-  auto cross4 = [](const float* a, const float* b, float* o) {
-    o[0] = a[1] * b[2] - a[2] * b[1];
-    o[1] = a[2] * b[0] - a[0] * b[2];
-    o[2] = a[0] * b[1] - a[1] * b[0];
-    o[3] = 0.f;
-  };
-  float d[4], r[4], u[4];
-  for (int i = 0; i < 4; ++i) d[i] = c.lookat[i] - c.position[i];
-  norm4(d);
-  cross4(d, c.up, r);
-  norm4(r);
-  cross4(r, d, u);
-  float eInv[4][4] = {{1, 0, 0, c.position[0]}, {0, 1, 0, c.position[1]}, {0, 0, 1, c.position[2]}, {0, 0, 0, 1}};
-  float nd[4] = {d[0] * -1.f, d[1] * -1.f, d[2] * -1.f, d[3] * -1.f};
-  float v2w[4][4];
-  for (int row = 0; row < 4; ++row) {
-    v2w[row][0] = r[row];
-    v2w[row][1] = u[row];
-    v2w[row][2] = nd[row];
-    v2w[row][3] = row == 3 ? 1.f : 0.f;
-  }
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) {
-      float col[4] = {v2w[0][j], v2w[1][j], v2w[2][j], v2w[3][j]};
-      pp.cam_m[4 * i + j] = dot4(eInv[i], col);
-    }
-  float dimx = (float)W, dimy = (float)H;
-  float fov_rad = c.fov * 0.017453292519943295f;
-  pp.cam_d = 1.f / std::tan(fov_rad / 2.f);
-  pp.cam_a = dimx / dimy;
-  pp.inv_w = 1.f / dimx;
-  pp.inv_h = 1.f / dimy;
-  pp.dim_w = dimx;
-  pp.dim_h = dimy;
-}
-
-void free_job(mt_job* j) {
-  for (int k = 0; k < 2; ++k) {
-    dfree(j->fb.q_o[k]);
-    dfree(j->fb.q_d[k]);
-  }
-  dfree(j->fb.hit_t);
-  dfree(j->fb.hit_prim);
-  dfree(j->fb.thr);
-  dfree(j->fb.ps);
-  dfree(j->fb.flag);
-  dfree(j->fb.s_o);
-  dfree(j->fb.s_d);
-  dfree(j->fb.s_c);
-  dfree(j->fb.film);
-  dfree(j->fb.film_c);
-  dfree(j->d_ctrl);
-  dfree(j->d_totals);
-  dfree(j->d_status);
-  dfree(j->d_pp);
-  if (j->h_pp) cudaFreeHost(j->h_pp);
-  j->h_pp = nullptr;
-  for (auto& g : j->graph) {
-    if (g) cudaGraphExecDestroy(g);
-    g = nullptr;
-  }
-  for (cudaEvent_t* e : {&j->ev0, &j->ev1, &j->done[0], &j->done[1]}) {
-    if (*e) cudaEventDestroy(*e);
-    *e = nullptr;
-  }
-  for (auto& e : j->kev)
-    if (e) cudaEventDestroy(e);
-  j->kev.clear();
-}
-
-int check_cfg(const mt_render_config* c) {
-  if (!c) return fail(MT_ERR_INVALID, "NULL config");
-  if (c->width <= 0 || c->height <= 0 || (long long)c->width * c->height > (1ll << 30))
-    return fail(MT_ERR_INVALID, "resolution %dx%d", c->width, c->height);
-  if (c->max_depth < 1 || c->max_depth > kMaxDepth) return fail(MT_ERR_INVALID, "max_depth %d (1..%d)", c->max_depth, kMaxDepth);
-  if (c->mode != 0 && c->mode != 1) return fail(MT_ERR_INVALID, "mode %d", c->mode);
-  if (c->spp < 1 || c->spp > 4096) return fail(MT_ERR_INVALID, "spp %d", c->spp);
-  return MT_OK;
-}
-
-}  // namespace
-
-extern "C" int mt_job_create(mt_context* ctx, mt_scene* scene, const mt_render_config* cfg, mt_job** out) {
-  if (!ctx || !scene || !out) return fail(MT_ERR_INVALID, "NULL argument");
-  int r = check_cfg(cfg);
-  if (r) return r;
-  if (!scene->has_bvh) return fail(MT_ERR_INVALID, "scene has no BVH (mt_bvh_build / mt_bvh_import)");
-  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-  CU(cudaSetDevice(ctx->device));
-  auto* j = new mt_job();
-  j->ctx = ctx;
-  j->scene = scene;
-  j->cfg = *cfg;
-  const size_t N = (size_t)cfg->width * cfg->height;
-  const int spp = cfg->spp;
-  for (int k = 0; k < 2 && !r; ++k) {
-    r = dalloc(&j->fb.q_o[k], N);
-    if (!r) r = dalloc(&j->fb.q_d[k], N);
-  }
-  if (!r) r = dalloc(&j->fb.hit_t, N);
-  if (!r) r = dalloc(&j->fb.hit_prim, N);
-  if (!r) r = dalloc(&j->fb.thr, N);
-  if (!r) r = dalloc(&j->fb.ps, N);
-  if (!r) r = dalloc(&j->fb.flag, N);
-  if (!r) r = dalloc(&j->fb.s_o, N);
-  if (!r) r = dalloc(&j->fb.s_d, N);
-  if (!r) r = dalloc(&j->fb.s_c, N);
-  if (!r) r = dalloc(&j->fb.film, N);
-  if (!r) r = dalloc(&j->fb.film_c, N);
-  if (!r) r = dalloc(&j->d_ctrl, (size_t)spp);
-  if (!r) r = dalloc(&j->d_totals, 4);
-  j->status_stride = (N + kShadeThreads - 1) / kShadeThreads;
-  if (!r) r = dalloc(&j->d_status, j->status_stride * (size_t)cfg->max_depth * spp);
-  if (!r) r = dalloc(&j->d_pp, 2 * (size_t)spp);
-  if (!r && cudaMallocHost((void**)&j->h_pp, sizeof(PassParams) * 2 * spp) != cudaSuccess)
-    r = fail(MT_ERR_NOMEM, "pinned pass parameters");
-  if (!r && (cudaEventCreate(&j->ev0) != cudaSuccess || cudaEventCreate(&j->ev1) != cudaSuccess ||
-             cudaEventCreate(&j->done[0]) != cudaSuccess || cudaEventCreate(&j->done[1]) != cudaSuccess))
-    r = fail(MT_ERR_CUDA, "event create");
-  if (!r && cfg->profile) {
-    j->kev.resize((size_t)spp * (2 + 3 * cfg->max_depth));
-    for (auto& e : j->kev)
-      if (cudaEventCreate(&e) != cudaSuccess) r = fail(MT_ERR_CUDA, "event create");
-  }
-  if (r) {
-    std::string keep = g_err;
-    free_job(j);
-    delete j;
-    g_err = keep;
-    return r;
-  }
-  std::memset(j->h_pp, 0, sizeof(PassParams) * 2 * spp);
-  j->h_ctrl.resize(spp);
-  cudaMemsetAsync(j->fb.film, 0, N * 16, ctx->stream);
-  cudaMemsetAsync(j->fb.film_c, 0, N * 16, ctx->stream);
-  cudaMemsetAsync(j->d_totals, 0, 32, ctx->stream);
-  CU(cudaStreamSynchronize(ctx->stream));
-  *out = j;
-  return MT_OK;
-}
-
-extern "C" int mt_job_destroy(mt_job* j) {
-  if (!j) return fail(MT_ERR_INVALID, "NULL job");
-  {
-    std::lock_guard<std::recursive_mutex> lk(j->ctx->mu);
-    cudaSetDevice(j->ctx->device);
-    cudaStreamSynchronize(j->ctx->stream);
-    free_job(j);
-  }
-  delete j;
-  return MT_OK;
-}
-
-extern "C" int mt_job_set_camera(mt_job* j, const void* camera) {
-  if (!j || !camera) return fail(MT_ERR_INVALID, "NULL argument");
-  std::memcpy(j->camera, camera, 64);
-  j->has_camera = 1;
-  return MT_OK;
-}
-
-namespace {
-// Enqueue one frame's passes reading parameter set `slot`.
-int enqueue_frame(mt_job* j, int slot) {
-  mt_context* ctx = j->ctx;
-  const mt_render_config& c = j->cfg;
-  DevScene S = j->scene->view();
-  DevEnv E = j->scene->env_view();
-  PassParams* hp = j->h_pp + (size_t)slot * c.spp;
-  PassParams* dp = j->d_pp + (size_t)slot * c.spp;
-  const size_t per_pass_events = 2 + 3 * (size_t)c.max_depth;
-  for (int p = 0; p < c.spp; ++p) {
-    CU(cudaMemcpyAsync(dp + p, hp + p, sizeof(PassParams), cudaMemcpyHostToDevice, ctx->stream));
-    CU(cudaMemsetAsync(j->d_ctrl + p, 0, sizeof(Ctrl), ctx->stream));
-    CU(cudaMemsetAsync(j->d_status + j->status_stride * (size_t)c.max_depth * p, 0,
-                       j->status_stride * (size_t)c.max_depth * 8, ctx->stream));
-    cudaEvent_t* ev = j->kev.empty() ? nullptr : j->kev.data() + per_pass_events * p;
-    if (launch_pass(ctx->stream, S, E, dp + p, c.mode, c.max_depth, c.film_kahan, c.width, c.height, j->d_ctrl + p,
-                    j->fb, j->d_status + j->status_stride * (size_t)c.max_depth * p, j->status_stride, ctx->num_sms,
-                    ev, j->d_totals))
-      return fail(MT_ERR_CUDA, "pass launch: %s", cudaGetErrorString(cudaGetLastError()));
-  }
-  return MT_OK;
-}
-}  // namespace
-
-extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_count) {
-  if (!j) return fail(MT_ERR_INVALID, "NULL job");
-  if (!j->has_camera) return fail(MT_ERR_INVALID, "camera not set (mt_job_set_camera)");
-  const mt_render_config& c = j->cfg;
-  if (c.mode == 0 && !seeds) return fail(MT_ERR_INVALID, "mode 0 needs the allocateState seed pairs");
-  mt_context* ctx = j->ctx;
-  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-  CU(cudaSetDevice(ctx->device));
-  // Parameter sets alternate between frames; wait only until the frame that
-  // last read this set has finished, so consecutive frames stay queued.
-  const int slot = j->slot;
-  j->slot ^= 1;
-  CU(cudaEventSynchronize(j->done[slot]));
-  CamF cam;
-  std::memcpy(&cam, j->camera, 64);
-  const int per_pass = 2 * (1 + 2 * c.max_depth);
-  for (int p = 0; p < c.spp; ++p) {
-    PassParams& pp = j->h_pp[(size_t)slot * c.spp + p];
-    camera_constants(cam, c.width, c.height, pp);
-    pp.frame_count = frame_count + (float)p;
-    pp.width = c.width;
-    pp.height = c.height;
-    pp.max_depth = c.max_depth;
-    pp.mode = c.mode;
-    pp.rr_depth = c.rr_depth;
-    pp.kahan = c.film_kahan;
-    if (c.mode == 0) std::memcpy(pp.seeds, seeds + (size_t)per_pass * p, sizeof(int32_t) * per_pass);
-  }
-  CU(cudaEventRecord(j->ev0, ctx->stream));
-  if (c.use_graph && !c.profile) {
-    if (!j->graph[slot]) {
-      cudaGraph_t g;
-      CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      int r = enqueue_frame(j, slot);
-      cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-      if (r) return r;
-      if (e != cudaSuccess) return fail(MT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-      e = cudaGraphInstantiate(&j->graph[slot], g, 0);
-      cudaGraphDestroy(g);
-      if (e != cudaSuccess) return fail(MT_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-    }
-    CU(cudaGraphLaunch(j->graph[slot], ctx->stream));
-  } else {
-    int r = enqueue_frame(j, slot);
-    if (r) return r;
-  }
-  CU(cudaEventRecord(j->ev1, ctx->stream));
-  CU(cudaEventRecord(j->done[slot], ctx->stream));
-  j->frames += c.spp;
-  return MT_OK;
-}
-
-extern "C" int mt_job_last_ms(mt_job* j, float* ms) {
-  if (!j || !ms) return fail(MT_ERR_INVALID, "NULL argument");
-  CU(cudaEventSynchronize(j->ev1));
-  CU(cudaEventElapsedTime(ms, j->ev0, j->ev1));
-  return MT_OK;
-}
-
-extern "C" int mt_job_total_rays(mt_job* j, int64_t* rays3) {
-  if (!j || !rays3) return fail(MT_ERR_INVALID, "NULL argument");
-  std::lock_guard<std::recursive_mutex> lk(j->ctx->mu);
-  CU(cudaSetDevice(j->ctx->device));
-  unsigned long long t[4];
-  CU(cudaMemcpyAsync(t, j->d_totals, 32, cudaMemcpyDeviceToHost, j->ctx->stream));
-  CU(cudaStreamSynchronize(j->ctx->stream));
-  for (int k = 0; k < 3; ++k) rays3[k] = (int64_t)t[k];
-  if (t[3]) return fail(MT_ERR_DEVICE, "device error %llu latched", t[3]);
-  return MT_OK;
-}
-
-extern "C" int mt_job_kernel_ms(mt_job* j, float* ms) {
-  if (!j || !ms) return fail(MT_ERR_INVALID, "NULL argument");
-  if (j->kev.empty()) return fail(MT_ERR_INVALID, "job was not created with profile = 1");
-  CU(cudaEventSynchronize(j->ev1));
-  const mt_render_config& c = j->cfg;
-  const size_t per = 2 + 3 * (size_t)c.max_depth;
-  for (int p = 0; p < c.spp; ++p)
-    for (size_t k = 0; k + 1 < per; ++k)
-      CU(cudaEventElapsedTime(ms + (size_t)p * (per - 1) + k, j->kev[p * per + k], j->kev[p * per + k + 1]));
-  return MT_OK;
-}
-
-extern "C" int mt_job_stats(mt_job* j, int64_t* rays3, int32_t* counts) {
-  if (!j) return fail(MT_ERR_INVALID, "NULL job");
-  std::lock_guard<std::recursive_mutex> lk(j->ctx->mu);
-  CU(cudaSetDevice(j->ctx->device));
-  CU(cudaStreamSynchronize(j->ctx->stream));
-  const mt_render_config& c = j->cfg;
-  CU(cudaMemcpy(j->h_ctrl.data(), j->d_ctrl, sizeof(Ctrl) * c.spp, cudaMemcpyDeviceToHost));
-  int64_t prim = 0, ext = 0, sh = 0;
-  int err = 0;
-  for (int p = 0; p < c.spp; ++p) {
-    const Ctrl& k = j->h_ctrl[p];
-    prim += (int64_t)c.width * c.height;
-    for (int b = 2; b <= c.max_depth; ++b) ext += k.count[b];
-    sh += (int64_t)k.rays[2];
-    if (k.error) err = k.error;
-  }
-  if (rays3) {
-    rays3[0] = prim;
-    rays3[1] = ext;
-    rays3[2] = sh;
-  }
-  if (counts) {
-    const Ctrl& k = j->h_ctrl[c.spp - 1];
-    for (int b = 1; b <= c.max_depth; ++b) counts[b - 1] = k.count[b + 1];
-  }
-  if (err) return fail(MT_ERR_DEVICE, "device error %d latched during the frame", err);
-  return MT_OK;
-}
-
-extern "C" int mt_film_read(mt_job* j, float* rgba, int resolve) {
-  if (!j || !rgba) return fail(MT_ERR_INVALID, "NULL argument");
-  std::lock_guard<std::recursive_mutex> lk(j->ctx->mu);
-  CU(cudaSetDevice(j->ctx->device));
-  const size_t N = (size_t)j->cfg.width * j->cfg.height;
-  CU(cudaMemcpyAsync(rgba, j->fb.film, N * 16, cudaMemcpyDeviceToHost, j->ctx->stream));
-  CU(cudaStreamSynchronize(j->ctx->stream));
-  if (resolve && j->frames > 0) {
-    // averageAccum (Image.cl:84-122): accum.xyz / frameCount, w = 1
-    float fc = (float)j->frames;
-    for (size_t i = 0; i < N; ++i) {
-      rgba[4 * i + 0] = rgba[4 * i + 0] / fc;
-      rgba[4 * i + 1] = rgba[4 * i + 1] / fc;
-      rgba[4 * i + 2] = rgba[4 * i + 2] / fc;
-      rgba[4 * i + 3] = 1.f;
-    }
-  }
-  return MT_OK;
-}
-
-extern "C" int mt_film_clear(mt_job* j) {
-  if (!j) return fail(MT_ERR_INVALID, "NULL job");
-  std::lock_guard<std::recursive_mutex> lk(j->ctx->mu);
-  CU(cudaSetDevice(j->ctx->device));
-  const size_t N = (size_t)j->cfg.width * j->cfg.height;
-  CU(cudaMemsetAsync(j->fb.film, 0, N * 16, j->ctx->stream));
-  CU(cudaMemsetAsync(j->fb.film_c, 0, N * 16, j->ctx->stream));
-  CU(cudaMemsetAsync(j->d_totals, 0, 32, j->ctx->stream));
-  j->frames = 0;
-  return MT_OK;
 }
 
 // ------------------------------------------------------------- ray queries

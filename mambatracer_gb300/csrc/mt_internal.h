@@ -1,0 +1,178 @@
+// Internal definitions shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mambatracer.h"
+#include "mt_common.h"
+#include "mt_kernels.h"
+
+using namespace mt;
+
+struct mt_job;
+
+// ------------------------------------------------------------------ errors
+namespace mt {
+// Records the message mt_last_error() returns on this thread; returns code.
+__attribute__((visibility("hidden"))) int fail(int code, const char* fmt, ...);
+}  // namespace mt
+using mt::fail;
+
+namespace {
+#define CU(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) return fail(MT_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(MT_ERR_NOMEM, "cudaMalloc(%zu B): %s", count * sizeof(T), cudaGetErrorString(e));
+  }
+  return MT_OK;
+}
+template <class T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+}  // namespace
+
+// ----------------------------------------------------------------- structs
+struct mt_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::recursive_mutex mu;
+  int* d_scratch = nullptr;  // [0] work counter, [1] error for ray queries
+  cudaEvent_t ev[8] = {};
+  // compaction scratch, grown on demand
+  unsigned long long* cs_status = nullptr;
+  int* cs_words = nullptr;
+  size_t cs_tiles = 0;
+  std::vector<mt_job*> jobs;  // jobs whose streams join into `stream`
+};
+
+struct mt_buffer {
+  mt_context* ctx;
+  void* ptr;
+  size_t bytes;
+};
+
+struct mt_scene {
+  mt_context* ctx;
+  int npoints = 0, nuvs = 0, nnormals = 0, ntri = 0, nmat = 0;
+  std::vector<float> h_points;
+  std::vector<int32_t> h_faces;
+  std::vector<uint8_t> h_materials;
+  float4* d_points = nullptr;
+  float2* d_uvs = nullptr;
+  float4* d_normals = nullptr;
+  Face* d_faces = nullptr;
+  Material* d_materials = nullptr;
+  int* d_light_faces = nullptr;
+  int nlights = 0;
+  // traversal layout
+  float4* d_nodes = nullptr;
+  float4* d_tris = nullptr;
+  int nrec = 0, root_ref = 0, depth = 0, has_bvh = 0, precision = 0;
+  // environment
+  float4* d_env_rgb = nullptr;
+  float* d_env_lum = nullptr;
+  float* d_env_sat = nullptr;
+  double* d_env_sat64 = nullptr;
+  int env_w = 0, env_h = 0, env_present = 0;
+  int grid_nu = 1600, grid_nv = 1600, grid_rx = 16, grid_ry = 32, grid_on = 0;
+
+  DevScene view() const {
+    DevScene s{};
+    s.nodes = d_nodes;
+    s.qnodes = nullptr;
+    s.tris = d_tris;
+    s.root_ref = root_ref;
+    s.ntri = ntri;
+    s.nrec = nrec;
+    s.precision = precision;
+    s.points = d_points;
+    s.uvs = d_uvs;
+    s.normals = d_normals;
+    s.faces = d_faces;
+    s.materials = d_materials;
+    s.light_faces = d_light_faces;
+    s.nlights = nlights;
+    return s;
+  }
+  DevEnv env_view() const {
+    DevEnv e{};
+    e.rgb = d_env_rgb;
+    e.lum = d_env_lum;
+    e.sat = d_env_sat;
+    e.w = env_w;
+    e.h = env_h;
+    e.present = env_present;
+    e.grid_on = 0;
+    return e;
+  }
+};
+
+// One in-flight frame's resources: path state, queues, film, parameters,
+// control blocks, and the stream its frames run on.
+struct JobSlot {
+  FrameBufs fb{};
+  Ctrl* d_ctrl = nullptr;                  // one per pass
+  unsigned long long* d_status = nullptr;  // compaction tile status, per pass and bounce
+  PassParams* h_pp = nullptr;              // pinned, one per pass
+  PassParams* d_pp = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr, done = nullptr;
+  cudaGraphExec_t graph = nullptr;
+};
+
+struct mt_job {
+  mt_context* ctx;
+  mt_scene* scene;
+  mt_render_config cfg;
+  int nslots = 1;
+  std::vector<JobSlot> slots;
+  int next = 0;   // slot of the next frame
+  int last = -1;  // slot of the last frame
+  size_t status_stride = 0;
+  unsigned char camera[64];
+  int has_camera = 0;
+  double frames = 0;                       // passes accumulated in the film
+  // nslots > 1: each frame renders into its slot's film from zero, and a merge
+  // on the slot's stream adds it into this film in frame order
+  float4* d_film = nullptr;
+  float4* d_film_c = nullptr;
+  std::vector<cudaEvent_t> kev;            // profile: 2 + 3 * max_depth per pass
+  unsigned long long* d_totals = nullptr;  // running [primary, extension, shadow, error]
+  std::vector<Ctrl> h_ctrl;
+  // asynchronous film reads
+  static constexpr int kMaxReads = 4;
+  struct Read {
+    float* host = nullptr;
+    int resolve = 0;
+    double frames = 0;
+    cudaEvent_t ev = nullptr;
+  };
+  cudaStream_t rstream = nullptr;
+  cudaEvent_t rfork = nullptr;
+  cudaEvent_t rdone = nullptr;  // the latest read's event: one of reads[].ev
+  Read reads[kMaxReads];        // pending reads, oldest at r_head
+  int r_head = 0, r_count = 0;
+  const float4* film() const { return nslots > 1 ? d_film : slots[0].fb.film; }
+};
+
+// Makes the context stream wait for every job stream's submitted work.
+void join_jobs(mt_context* ctx);

@@ -372,10 +372,11 @@ __global__ void k_accumulate(const Ctrl* ctrl, int max_depth, int n_pixels, unsi
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   unsigned long long ext = 0;
   for (int b = 2; b <= max_depth; ++b) ext += (unsigned long long)ctrl->count[b];
-  totals[0] += (unsigned long long)n_pixels;
-  totals[1] += ext;
-  totals[2] += ctrl->rays[2];
-  if (ctrl->error) totals[3] = (unsigned long long)ctrl->error;
+  // frames of in-flight slots finish concurrently: the totals are shared
+  atomicAdd(totals + 0, (unsigned long long)n_pixels);
+  atomicAdd(totals + 1, ext);
+  atomicAdd(totals + 2, (unsigned long long)ctrl->rays[2]);
+  if (ctrl->error) atomicExch(totals + 3, (unsigned long long)ctrl->error);
 }
 
 // ---------------------------------------------------------------- launchers

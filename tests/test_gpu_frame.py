@@ -112,6 +112,44 @@ def test_graph_spp_and_kahan_are_consistent(ctx, orc):
     S.close()
 
 
+@pytest.mark.parametrize("inflight", [2, 4])
+def test_inflight_frames_match_one_stream(ctx, orc, inflight):
+    """Frames kept in flight on separate streams trace the same rays as one stream
+    (exact totals), and their summed films equal its film up to FP32 summation order."""
+    sc = scenes.soup(20000, seed=4, extent=0.8, edge_sigma=0.02)
+    S, _, _ = setup(ctx, orc, sc, (scenes.sky_env(256, 128), 256, 128))
+    out = {}
+    for n in (1, inflight):
+        J = api.Job(ctx, S, 96, 64, max_depth=6, mode=1, rr_depth=3, film_kahan=1, use_graph=1, inflight=n)
+        J.set_camera(sc.camera)
+        per_frame = []
+        bufs = [np.zeros((96 * 64, 4), np.float32) for _ in range(7)]
+        for f in range(7):
+            J.render(None, float(f + 1))
+            if n == 1:
+                per_frame.append(J.film(resolve=True))
+            else:
+                # pipelined reads: the film after frame f is read while later frames
+                # render; the fifth pending read completes the oldest
+                J.film_async(bufs[f], resolve=True)
+        if n > 1:
+            J.wait()
+            per_frame = bufs
+        out[n] = (J.film(), J.total_rays(), per_frame)
+        J.clear()
+        J.render(None, 1.0)
+        out[n, "after_clear"] = J.film()
+        J.close()
+    assert np.array_equal(out[1][1], out[inflight][1])
+    assert out[1][1][2] > 0
+    assert rel_rmse(out[inflight][0], out[1][0]) < 1e-6
+    assert np.abs(out[1][0]).sum() > 0
+    for a, b in zip(out[inflight][2], out[1][2]):
+        assert rel_rmse(a, b) < 1e-6
+    assert rel_rmse(out[inflight, "after_clear"], out[1, "after_clear"]) < 1e-6
+    S.close()
+
+
 def test_fp64_oracle_image_error(ctx, orc):
     """Spec bound: FP32 GPU film (Kahan) within 1e-3 relative RMSE of the FP64
     oracle at matched spp (same pixel-keyed random numbers)."""
