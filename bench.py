@@ -37,6 +37,8 @@ sys.path.insert(0, ROOT)
 W_DEFAULT, H_DEFAULT, DEPTH, RR = 1920, 1080, 8, 3
 NTRI = 1_000_000
 ENV_W, ENV_H = 2048, 1024
+GRID = (1600, 1600, 16, 32)  # light grid: nu, nv, tiles per cell (reference defaults, CLightGrid.java)
+GRID_UPDATES = 5             # CDeviceGI.loop updates the grid after its first 5 frames
 METRIC = "Mrays/s (primary + extension + shadow rays traced, device-counted)"
 WORKLOAD = "soup1M_1920x1080_depth8_rr3_env2048x1024"
 
@@ -51,6 +53,8 @@ def config_dict(width, height, ntri, world, inflight=1):
         f"soup{ntri}_{width}x{height}_depth{DEPTH}_rr{RR}_env{ENV_W}x{ENV_H}",
         "scene": f"{ntri}-triangle soup, centroids U[-1,1]^3, edges N(0,0.005^2), GGX r U[0.05,0.8], albedo U[0.2,0.9]",
         "environment": f"{ENV_W}x{ENV_H} FP32 lat-long sky gradient + 0.5 deg Gaussian sun (peak 5e4); SAT built in FP64",
+        "light_grid": (f"{GRID[0]}x{GRID[1]} grid of {GRID[2]}x{GRID[3]}-tile cells, FP64 per-cell SATs, updated from "
+                       f"environment hits after each of the first {GRID_UPDATES} warm-up frames, then fixed"),
         "resolution": f"{width}x{height}", "spp_per_step": 1, "max_depth": DEPTH, "rr_from_bounce": RR,
         "rng": "per-pixel seed pixel ^ 0x9E3779B9 into the reference WangHash chain",
         "film": "FP32 Kahan-compensated", "launch": "CUDA graph per frame" + (f", {inflight} frames in flight on separate streams" if inflight > 1 else ""),
@@ -111,11 +115,25 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- CPU side
-def cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, seconds, threads):
-    """Oracle frames (benchmark semantics) rendered in parallel threads for about
-    `seconds`; returns (rays, wall seconds, frames)."""
+def cpu_grid(orc, sat):
+    """The light grid's initial function and per-cell SATs for the environment."""
+    from oracle.oracle import ptr
+    nu, nv, rx, ry = GRID
+    func = np.zeros(nu * nv, np.float32)
+    orc.lib.or_grid_init_func(None, ptr(sat), ENV_W, ENV_H, nu, nv, rx, ry, ptr(func))
+    gsat = np.zeros(nu * nv, np.float32)
+    orc.lib.or_lightgrid_sat(ptr(func), ptr(gsat), nu, nv, rx, ry)
+    return func, gsat
+
+
+def cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, seconds, threads, grid):
+    """Oracle frames (benchmark semantics, grid-guided environment sampling on the
+    given grid) rendered in parallel threads for about `seconds`; returns (rays,
+    wall seconds, frames)."""
     from oracle.oracle import ptr
     cam = sc.camera.copy()
+    pos = np.ascontiguousarray(cam["position"].reshape(-1)[:4], np.float32)
+    gfunc, gsat = grid
     stop = time.perf_counter() + seconds
     lock = threading.Lock()
     total = {"rays": 0, "frames": 0}
@@ -126,10 +144,11 @@ def cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, second
             acc = np.zeros((width * height, 4), np.float32)
             c = np.zeros(DEPTH, np.int32)
             rc = np.zeros(3, np.int64)
-            orc.lib.or_render_frame(ptr(cam), width, height, DEPTH, 1, RR, None, float(1 + tid + 1000 * f),
-                                    ptr(sc.points), ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces), sc.ntri,
-                                    ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(env), ptr(lum), ptr(sat), ENV_W,
-                                    ENV_H, 1, 0, ptr(acc), ptr(c), ptr(rc))
+            orc.lib.or_render_frame_grid(ptr(cam), width, height, DEPTH, 1, RR, None, float(1 + tid + 1000 * f),
+                                         ptr(sc.points), ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces), sc.ntri,
+                                         ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(env), ptr(lum), ptr(sat),
+                                         ENV_W, ENV_H, 1, 0, ptr(acc), ptr(c), ptr(rc), ptr(gfunc), ptr(gsat), None,
+                                         *GRID, ptr(pos), 1, 0)
             with lock:
                 total["rays"] += int(rc.sum())
                 total["frames"] += 1
@@ -200,8 +219,9 @@ def run_gpu(args):
     S = api.Scene(ctx, sc)
     nodes, bounds = S.build_bvh()
     S.set_env(env, ENV_W, ENV_H)
+    S.grid_config(*GRID, enable=2)  # grid-guided environment sampling, FP64 per-cell SATs
     job = api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, use_graph=1,
-                  inflight=args.inflight)
+                  inflight=args.inflight, grid_updates=min(GRID_UPDATES, args.warmup))
     cam = sc.camera.copy()
     job.set_camera(cam)
 
@@ -279,7 +299,8 @@ def run_gpu(args):
     out = None
     if rank == 0:
         # per-launch device times (profiled frames, no graph) for the roofline
-        pj = api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, profile=1)
+        pj = api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, profile=1,
+                     grid_updates=0)
         pj.set_camera(cam)
         prof_frames = 5
         kms = []
@@ -329,7 +350,8 @@ def run_gpu(args):
         clum = np.zeros(ENV_W * ENV_H, np.float32)
         csat = np.zeros(ENV_W * ENV_H, np.float32)
         orc.lib.or_env_lum_sat(ptr(cenv), ENV_W, ENV_H, ptr(clum), ptr(csat))
-        crays, csec, cframes = cpu_render_rate(orc, csc, cn, cb, cenv, clum, csat, cw, ch, args.cpu_seconds, threads)
+        crays, csec, cframes = cpu_render_rate(orc, csc, cn, cb, cenv, clum, csat, cw, ch, args.cpu_seconds, threads,
+                                               cpu_grid(orc, csat))
         cpu_baseline = {"value": round(crays / csec / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                         "sample": f"{cframes} frames of {cw}x{ch} (1/16 of the pixels, same scene, camera, depth, RR) "
                                   f"in {threads} threads for {csec:.1f} s; oracle/mt_oracle.cpp (FP32)"}
@@ -366,12 +388,13 @@ def run_reference(args):
     orc = Oracle()
     threads = os.cpu_count() or 1
     sc, nodes, bounds, env, lum, sat = cpu_scene(orc, NTRI)
+    grid = cpu_grid(orc, sat)
     width, height = W_DEFAULT // 4, H_DEFAULT // 4
     for _ in range(args.warmup):
-        cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, 0.0, threads)
+        cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, 0.0, threads, grid)
     rays = secs = frames = 0
     for _ in range(args.steps):
-        r, s, f = cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, 0.0, threads)
+        r, s, f = cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, 0.0, threads, grid)
         rays, secs, frames = rays + r, secs + s, frames + f
     value = rays / secs / 1e6
     sample = (f"each step: {threads} frames of {width}x{height} (1/16 of the 1080p pixels) rendered in parallel, "

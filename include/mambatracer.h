@@ -135,8 +135,11 @@ int mt_env_clear(mt_scene* scene);
 int mt_env_read(mt_scene* scene, float* lum, double* sat64, float* sat32);
 
 /* Adaptive light grid (CAdaptiveEnvironment, src/cl/algorithms/CAdaptiveEnvironment.java:69-145):
- * nu x nv grid of cells of rx x ry tiles (reference: 1600 x 1600, 16 x 32).
- * enable = 0 turns grid-guided sampling off (full-map SAT as the reference). */
+ * nu x nv values, (nu/rx) x (nv/ry) cells of rx x ry tiles (reference: 1600 x 1600, 16 x 32;
+ * rx, ry in {8, 16, 32}). enable: 0 = off (environment sampled off the full-map SAT, as the
+ * reference renders), 1 = grid-guided environment sampling in mode-1 jobs with per-cell SATs in
+ * the reference's FP32 order, 2 = the same with FP64 per-cell SATs. Each mode-1 job keeps its own
+ * grid (it depends on the job's camera); rx and ry must divide the environment map's size. */
 int mt_env_grid_config(mt_scene* scene, int nu, int nv, int rx, int ry, int enable);
 /* Per-cell SAT of a given func (prefixSumRowSubgrid + prefixSumColSubgrid,
  * src/cl/kernel/LightGrid.cl:347-400); fp64 != 0 builds it in FP64. */
@@ -157,12 +160,18 @@ typedef struct mt_render_config {
   int inflight;      /* frames kept in flight on their own streams, 0 or 1 = one (1..4); each
                         in-flight frame has its own path state and film, summed on read.
                         profile = 1 forces one. */
+  int grid_updates;  /* mode 1 with the scene's light grid on: the first grid_updates frames add
+                        the luminance of environment hits into the grid, which is updated after
+                        each of them (CDeviceGI.java:263-264 updates after the first 5) */
 } mt_render_config;
 
 /* A render job: film + path state resident on the device (CDeviceGI.setup,
  * src/cl/device/CDeviceGI.java:116-164). */
 int mt_job_create(mt_context* ctx, mt_scene* scene, const mt_render_config* cfg, mt_job** out);
 int mt_job_destroy(mt_job* job);
+/* The job's light grid (nu * nv floats each, NULL to skip): func (the sampled
+ * function), its per-cell SAT, and the accumulated environment luminance. */
+int mt_job_grid_read(mt_job* job, float* func, float* sat, float* accum);
 /* CDeviceGI.updateCamera (src/cl/device/CDeviceGI.java:308-313). */
 int mt_job_set_camera(mt_job* job, const void* camera);
 /* One GI frame: CDeviceGI.loop (src/cl/device/CDeviceGI.java:214-271) without

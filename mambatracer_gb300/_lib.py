@@ -25,7 +25,8 @@ class MTError(RuntimeError):
 class RenderConfig(C.Structure):
     _fields_ = [("width", C.c_int), ("height", C.c_int), ("max_depth", C.c_int), ("mode", C.c_int),
                 ("rr_depth", C.c_int), ("film_kahan", C.c_int), ("spp", C.c_int), ("use_graph", C.c_int),
-                ("profile", C.c_int), ("inflight", C.c_int)]
+                ("profile", C.c_int), ("inflight", C.c_int),
+                ("grid_updates", C.c_int)]
 
 
 P = C.c_void_p
@@ -73,6 +74,7 @@ SIGNATURES = {
     "mt_render_frame": (I, [P, P, F]),
     "mt_film_read": (I, [P, P, I]),
     "mt_film_read_async": (I, [P, P, I]),
+    "mt_job_grid_read": (I, [P, P, P, P]),
     "mt_film_wait": (I, [P]),
     "mt_film_clear": (I, [P]),
     "mt_job_stats": (I, [P, P, P]),

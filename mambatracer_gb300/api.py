@@ -65,6 +65,7 @@ class Scene:
                                     _p(faces), faces.shape[0], _p(mats), mats.shape[0], C.byref(h)))
         self.h = h
         self.depth = None
+        self.grid = (1600, 1600, 16, 32, 0)
 
     def build_bvh(self):
         """CNormalBVH.build on the host (returns nodes, bounds in the reference layout)."""
@@ -98,6 +99,11 @@ class Scene:
         check(lib().mt_env_read(self.h, _p(lum), _p(sat64), _p(sat32)))
         return lum, sat64, sat32
 
+    def grid_config(self, nu: int = 1600, nv: int = 1600, rx: int = 16, ry: int = 32, enable: int = 1):
+        """Adaptive light grid for mode-1 jobs (0 off, 1 FP32 per-cell SATs, 2 FP64)."""
+        check(lib().mt_env_grid_config(self.h, nu, nv, rx, ry, enable))
+        self.grid = (nu, nv, rx, ry, enable)
+
     @property
     def light_count(self) -> int:
         return lib().mt_scene_light_count(self.h)
@@ -128,9 +134,10 @@ class Job:
 
     def __init__(self, ctx: Context, scene: Scene, width: int, height: int, max_depth: int = 15, mode: int = 0,
                  rr_depth: int = 0, film_kahan: int = 1, spp: int = 1, use_graph: int = 0, profile: int = 0,
-                 inflight: int = 1):
+                 inflight: int = 1, grid_updates: int = 5):
         self.cfg = RenderConfig(width, height, max_depth, mode, rr_depth, film_kahan, spp, use_graph, profile,
-                                inflight)
+                                inflight, grid_updates)
+        self.scene = scene
         h = C.c_void_p()
         check(lib().mt_job_create(ctx.h, scene.h, C.byref(self.cfg), C.byref(h)))
         self.h = h
@@ -161,6 +168,13 @@ class Job:
     def wait(self):
         check(lib().mt_film_wait(self.h))
         self._pending = []
+
+    def grid(self):
+        """The job's light grid: (func, sat, accum), each nu * nv float32."""
+        nu, nv = self.scene.grid[0], self.scene.grid[1]
+        out = [np.zeros(nu * nv, np.float32) for _ in range(3)]
+        check(lib().mt_job_grid_read(self.h, _p(out[0]), _p(out[1]), _p(out[2])))
+        return tuple(out)
 
     def clear(self):
         check(lib().mt_film_clear(self.h))

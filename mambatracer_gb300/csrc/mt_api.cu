@@ -35,6 +35,12 @@ __attribute__((visibility("hidden"))) int fail(int code, const char* fmt, ...) {
 }
 }  // namespace mt
 
+int quiesce(mt_context* ctx) {
+  join_jobs(ctx);
+  CU(cudaStreamSynchronize(ctx->stream));
+  return MT_OK;
+}
+
 void join_jobs(mt_context* ctx) {
   for (mt_job* j : ctx->jobs) {
     for (JobSlot& s : j->slots)
@@ -300,7 +306,9 @@ extern "C" int mt_scene_set_materials(mt_scene* s, const void* materials, int nm
     if ((F[i].mat & 0xFFFF) >= nmaterials) return fail(MT_ERR_INVALID, "face %d needs material %d", i, F[i].mat & 0xFFFF);
   std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CU(cudaSetDevice(s->ctx->device));
-  CU(cudaStreamSynchronize(s->ctx->stream));
+  int q = quiesce(s->ctx);
+  if (q) return q;
+  ++s->version;
   s->h_materials.assign((const uint8_t*)materials, (const uint8_t*)materials + 144 * (size_t)nmaterials);
   s->nmat = nmaterials;
   int r = upload(&s->d_materials, materials, (size_t)nmaterials);
@@ -315,7 +323,7 @@ extern "C" int mt_scene_destroy(mt_scene* s) {
   {
     std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
     cudaSetDevice(s->ctx->device);
-    cudaStreamSynchronize(s->ctx->stream);
+    quiesce(s->ctx);
     free_scene(s);
   }
   delete s;
@@ -542,7 +550,9 @@ extern "C" int mt_bvh_build(mt_scene* s, int32_t* nodes_out, float* bounds_out, 
   if (depth_out) *depth_out = b.max_depth;
   std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CU(cudaSetDevice(s->ctx->device));
-  CU(cudaStreamSynchronize(s->ctx->stream));
+  int q = quiesce(s->ctx);
+  if (q) return q;
+  ++s->version;
   return import_bvh(s, nodes.data(), bounds.data(), 2 * n - 1);
 }
 
@@ -572,7 +582,9 @@ extern "C" int mt_bvh_import(mt_scene* s, const int32_t* nodes, const float* bou
   if (!s || !nodes || !bounds) return fail(MT_ERR_INVALID, "NULL argument");
   std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CU(cudaSetDevice(s->ctx->device));
-  CU(cudaStreamSynchronize(s->ctx->stream));
+  int q = quiesce(s->ctx);
+  if (q) return q;
+  ++s->version;
   return import_bvh(s, nodes, bounds, nnodes);
 }
 
@@ -588,7 +600,9 @@ extern "C" int mt_env_set(mt_scene* s, const float* rgb, int w, int h) {
   if (!s || !rgb || w <= 0 || h <= 0) return fail(MT_ERR_INVALID, "bad environment map");
   std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CU(cudaSetDevice(s->ctx->device));
-  CU(cudaStreamSynchronize(s->ctx->stream));
+  int q = quiesce(s->ctx);
+  if (q) return q;
+  ++s->version;
   size_t n = (size_t)w * h;
   int r = upload(&s->d_env_rgb, rgb, n);
   if (!r) { dfree(s->d_env_lum); r = dalloc(&s->d_env_lum, n); }
@@ -608,7 +622,9 @@ extern "C" int mt_env_set_with_sat(mt_scene* s, const float* rgb, const float* l
   if (!s || !rgb || !lum || !sat || w <= 0 || h <= 0) return fail(MT_ERR_INVALID, "bad environment map");
   std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CU(cudaSetDevice(s->ctx->device));
-  CU(cudaStreamSynchronize(s->ctx->stream));
+  int q = quiesce(s->ctx);
+  if (q) return q;
+  ++s->version;
   size_t n = (size_t)w * h;
   int r = upload(&s->d_env_rgb, rgb, n);
   if (!r) r = upload(&s->d_env_lum, lum, n);
@@ -623,6 +639,11 @@ extern "C" int mt_env_set_with_sat(mt_scene* s, const float* rgb, const float* l
 
 extern "C" int mt_env_clear(mt_scene* s) {
   if (!s) return fail(MT_ERR_INVALID, "NULL scene");
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  int q = quiesce(s->ctx);
+  if (q) return q;
+  ++s->version;
   s->env_present = 0;
   return MT_OK;
 }
@@ -643,7 +664,15 @@ extern "C" int mt_env_read(mt_scene* s, float* lum, double* sat64, float* sat32)
 }
 
 extern "C" int mt_env_grid_config(mt_scene* s, int nu, int nv, int rx, int ry, int enable) {
-  if (!s || nu <= 0 || nv <= 0 || rx <= 0 || ry <= 0 || nu % rx || nv % ry) return fail(MT_ERR_INVALID, "bad grid");
+  if (!s || nu <= 0 || nv <= 0 || nu % rx || nv % ry || enable < 0 || enable > 2) return fail(MT_ERR_INVALID, "bad grid");
+  if (!((rx == 8 || rx == 16 || rx == 32) && (ry == 8 || ry == 16 || ry == 32)))
+    return fail(MT_ERR_INVALID, "tiles per cell must be 8, 16 or 32 along each axis");
+  if ((long long)nu * nv > (1ll << 28)) return fail(MT_ERR_INVALID, "grid of %d x %d is too large", nu, nv);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  int q = quiesce(s->ctx);
+  if (q) return q;
+  ++s->version;
   s->grid_nu = nu;
   s->grid_nv = nv;
   s->grid_rx = rx;

@@ -70,7 +70,6 @@ struct DevEnv {
   float* grid_accum;
   int grid_on;
   int nu, nv, rx, ry;
-  float4 camera_pos;
 };
 
 // Per-pass control block in device memory (zeroed at the start of each pass).
@@ -97,7 +96,8 @@ struct PassParams {
   int mode;
   int rr_depth;
   int kahan;
-  int pad;
+  int grid_accum;        // 1: environment hits add their luminance into the light grid
+  float cam_pos[4];      // camera position (LightGrid.cameraPosition)
   int seeds[2 * (1 + 2 * kMaxDepth)];  // mode 0: allocateState() seed pairs
 };
 

@@ -553,5 +553,93 @@ __device__ __forceinline__ V radiance_env(const DevEnv& E, V d, float* pdfA) {
   return c;
 }
 
+
+// ------------------------------------------------------ adaptive light grid
+// LightGrid.cl:39-343 and the grid versions of the environment light,
+// illuminateEnvironmentLight1 / getRadianceEnvironmentLight1 (Light.cl:140-268).
+// The grid holds nu x nv values: (nu/rx) x (nv/ry) cells of rx x ry tiles; a
+// shading point's cell is the direction camera -> point, a tile a sub-region of
+// the environment map. The tile is drawn from the cell's SAT, then the texel
+// from the tile's region of the full-map SAT. The reference leaves the tile's
+// probability out of the direction pdf and never calls these versions; here
+// the pdf is pdfLL * pdfSS (tile density over the cell's tile square times
+// texel density over the tile), the density of the direction over the map's
+// uv square when tiles divide the map, which mt_job_create checks.
+// Cell lookups take the direction from the xyz lanes.
+__device__ __forceinline__ int grid_cell(const DevEnv& E, const float* cam, V p) {
+  const int cw = E.nu / E.rx, ch = E.nv / E.ry;
+  V d = normalize3(mk(p.x - cam[0], p.y - cam[1], p.z - cam[2], 0.f));
+  int x, y;
+  sph_xy(cw, ch, d, &x, &y);
+  return sph_index(cw, ch, x, y);
+}
+// Offset of a cell's first tile in the grid arrays (subgridGlobalIndex2,
+// LightGrid.cl:107-110: cell (cx, cy) starts at (cx * rx, cy * ry)). Each cell
+// holds its own SAT, so a cell is sampled as the region (0, 0, rx, ry) of the
+// arrays offset to its first tile with row pitch nu: reads left of or above
+// the cell give 0 as getSubgridValueSAT's range check does (LightGrid.cl:142-147).
+__device__ __forceinline__ size_t grid_cell_base(const DevEnv& E, int cell) {
+  const int cw = E.nu / E.rx;
+  return (size_t)((cell / cw) * E.ry) * E.nu + (size_t)((cell % cw) * E.rx);
+}
+// getSubgridUnitBound + getSubRegionFromUnitBound (LightGrid.cl:157-165,
+// SAT.cl:28-44): tile (tx, ty) of rx x ry as a region of the w x h map.
+__device__ __forceinline__ Region env_tile_region(const DevEnv& E, int tx, int ty) {
+  const float ux0 = (float)tx / (float)E.rx, uy0 = (float)ty / (float)E.ry;
+  const float ux1 = (float)(tx + 1) / (float)E.rx, uy1 = (float)(ty + 1) / (float)E.ry;
+  const int x0 = (int)((float)E.w * ux0), y0 = (int)((float)E.h * uy0);
+  const int x1 = (int)((float)E.w * ux1), y1 = (int)((float)E.h * uy1);
+  return Region{E.w, E.h, x0, y0, x1 - x0, y1 - y0};
+}
+__device__ __forceinline__ V illuminate_env_grid(const DevEnv& E, const float* cam, V p, V s, V* dir, float* dist,
+                                                 float* pdfW) {
+  const size_t base = grid_cell_base(E, grid_cell(E, cam, p));
+  const Region rc{E.nu, E.nv, 0, 0, E.rx, E.ry};
+  float uvLL[2], pdfLL, uvSS[2], pdfSS;
+  int offLL[2], offSS[2];
+  sample_cont(rc, s.x, s.y, uvLL, offLL, &pdfLL, E.grid_sat + base, E.grid_func + base);
+  *dist = kFloatMax;
+  *pdfW = 0.f;
+  if (!(pdfLL > 0.f)) return zero4();  // empty cell: the BSDF sample covers it alone
+  const Region rt = env_tile_region(E, offLL[0], offLL[1]);
+  sample_cont(rt, s.z, s.w, uvSS, offSS, &pdfSS, E.sat, E.lum);
+  if (!(pdfSS > 0.f)) return zero4();
+  V d = sph_dir(uvSS[0], uvSS[1]);
+  *dir = d;
+  int x, y;
+  sph_xy(E.w, E.h, d, &x, &y);
+  V c = ldg4(E.rgb + sph_index(E.w, E.h, x, y));
+  float sinT = sinf(uvSS[1] * kPi);
+  *pdfW = (pdfLL * pdfSS) / (2.f * kPi * kPi * sinf(uvSS[1] * kPi));
+  if (sinT == 0.f) *pdfW = 0.f;
+  return c;
+}
+// pdf of direction d under illuminate_env_grid from shading point p, and the
+// radiance; the tile is the one holding d's texel, and the sine term takes
+// v = y / h over the whole map (the reference's unused version divides by the
+// tile's height, Light.cl:253). accumulate: add the texel's
+// luminance into the grid's accumulation array at (cell, tile)
+// (getRadianceEnvironmentLight1 with accumLightGrid, Light.cl:35-38).
+__device__ __forceinline__ V radiance_env_grid(const DevEnv& E, const float* cam, V p, V d, float* pdfA,
+                                               bool accumulate) {
+  int x, y;
+  sph_xy(E.w, E.h, d, &x, &y);
+  V c = ldg4(E.rgb + sph_index(E.w, E.h, x, y));
+  const int xc = x > E.w - 1 ? E.w - 1 : (x < 0 ? 0 : x), yc = y > E.h - 1 ? E.h - 1 : (y < 0 ? 0 : y);
+  const int tx = xc / (E.w / E.rx), ty = yc / (E.h / E.ry);
+  const size_t base = grid_cell_base(E, grid_cell(E, cam, p));
+  const Region rc{E.nu, E.nv, 0, 0, E.rx, E.ry};
+  const float pdfLL =
+      pdf_cond(rc, tx, ty, E.grid_sat + base, E.grid_func + base) * pdf_marg(rc, ty, E.grid_sat + base);
+  const Region rt = env_tile_region(E, tx, ty);
+  const float pdfSS = pdf_cond(rt, xc, yc, E.sat, E.lum) * pdf_marg(rt, yc, E.sat);
+  const float v = (float)y / (float)E.h;
+  float pdf = (pdfLL * pdfSS) / (2.f * kPi * kPi * sinf(v * kPi));
+  *pdfA = pdf > 0.f ? pdf : 0.f;  // also maps NaN from an empty cell or tile to 0
+  if (accumulate)
+    atomicAdd(E.grid_accum + base + (size_t)ty * E.nu + tx, luminance(c.x, c.y, c.z));
+  return c;
+}
+
 }  // namespace dv
 }  // namespace mt

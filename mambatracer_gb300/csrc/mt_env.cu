@@ -120,7 +120,36 @@ int grid_sat_t(cudaStream_t st, const float* func, T* out, int nu, int nv, int r
   return 0;
 }
 
+// Initial grid func: every cell's tile (tx, ty) gets the environment luminance
+// summed over the tile's region of the map (the noise-free version of the
+// reference's per-tile luminance histogram, CAdaptiveEnvironment.java:77),
+// from the FP64 SAT when there is one, else the FP32 SAT.
+__global__ void k_grid_init_func(const double* __restrict__ sat64, const float* __restrict__ sat32, int w, int h,
+                                 int nu, int nv, int rx, int ry, float* __restrict__ func) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)nu * nv) return;
+  const int tx = (int)(i % nu) % rx, ty = (int)(i / nu) % ry;
+  const int x0 = (int)((float)w * ((float)tx / (float)rx)), y0 = (int)((float)h * ((float)ty / (float)ry));
+  const int x1 = (int)((float)w * ((float)(tx + 1) / (float)rx)) - 1;
+  const int y1 = (int)((float)h * ((float)(ty + 1) / (float)ry)) - 1;
+  auto at64 = [&](int x, int y) { return (x < 0 || y < 0) ? 0.0 : sat64[(size_t)y * w + x]; };
+  auto at32 = [&](int x, int y) { return (x < 0 || y < 0) ? 0.f : sat32[(size_t)y * w + x]; };
+  float v;
+  if (sat64)
+    v = (float)(at64(x1, y1) - at64(x0 - 1, y1) - at64(x1, y0 - 1) + at64(x0 - 1, y0 - 1));
+  else
+    v = at32(x0 - 1, y0 - 1) + at32(x1, y1) - at32(x1, y0 - 1) - at32(x0 - 1, y1);  // SAT.cl:149-156 order
+  func[i] = v;
+}
+
 }  // namespace
+
+int launch_grid_init(cudaStream_t st, const double* sat64, const float* sat32, int w, int h, int nu, int nv, int rx,
+                     int ry, float* func) {
+  size_t n = (size_t)nu * nv;
+  k_grid_init_func<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(sat64, sat32, w, h, nu, nv, rx, ry, func);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
 
 int launch_env_build(cudaStream_t st, const float4* rgb, int w, int h, float* lum, double* sat64, float* sat32) {
   int n = w * h;

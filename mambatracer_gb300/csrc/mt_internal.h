@@ -93,7 +93,8 @@ struct mt_scene {
   float* d_env_sat = nullptr;
   double* d_env_sat64 = nullptr;
   int env_w = 0, env_h = 0, env_present = 0;
-  int grid_nu = 1600, grid_nv = 1600, grid_rx = 16, grid_ry = 32, grid_on = 0;
+  int grid_nu = 1600, grid_nv = 1600, grid_rx = 16, grid_ry = 32, grid_on = 0;  // grid_on: 0, 1 FP32, 2 FP64 SAT
+  unsigned version = 0;  // bumped when device arrays or the grid configuration change
 
   DevScene view() const {
     DevScene s{};
@@ -137,6 +138,7 @@ struct JobSlot {
   cudaStream_t stream = nullptr;
   cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr, done = nullptr;
   cudaGraphExec_t graph = nullptr;
+  unsigned graph_version = 0;  // scene version the graph was captured against
 };
 
 struct mt_job {
@@ -172,7 +174,20 @@ struct mt_job {
   Read reads[kMaxReads];        // pending reads, oldest at r_head
   int r_head = 0, r_count = 0;
   const float4* film() const { return nslots > 1 ? d_film : slots[0].fb.film; }
+  // adaptive light grid (mode 1, scene grid on, environment present)
+  unsigned scene_version = 0;
+  int grid_on = 0, grid_fp64 = 0;
+  int nu = 0, nv = 0, rx = 0, ry = 0;
+  float* d_grid_func = nullptr;
+  float* d_grid_sat = nullptr;
+  float* d_grid_accum = nullptr;
+  double* d_grid_sat64 = nullptr;
+  int grid_frames = 0;           // frames that have accumulated into the grid since it was set up
+  cudaEvent_t grid_ev = nullptr;  // recorded after the last grid update
 };
 
 // Makes the context stream wait for every job stream's submitted work.
 void join_jobs(mt_context* ctx);
+// Waits for all work on the context and its jobs' streams, before device arrays
+// that frames read are freed or rewritten.
+int quiesce(mt_context* ctx);

@@ -57,6 +57,7 @@ void camera_constants(const CamF& c, int W, int H, PassParams& pp) {
   pp.inv_h = 1.f / dimy;
   pp.dim_w = dimx;
   pp.dim_h = dimy;
+  for (int i = 0; i < 4; ++i) pp.cam_pos[i] = c.position[i];
 }
 
 // Adds one frame's film (rendered from zero into its slot's film) into the
@@ -117,6 +118,12 @@ void free_job(mt_job* j) {
   dfree(j->d_totals);
   dfree(j->d_film);
   dfree(j->d_film_c);
+  dfree(j->d_grid_func);
+  dfree(j->d_grid_sat);
+  dfree(j->d_grid_accum);
+  dfree(j->d_grid_sat64);
+  if (j->grid_ev) cudaEventDestroy(j->grid_ev);
+  j->grid_ev = nullptr;
   if (j->rfork) cudaEventDestroy(j->rfork);
   j->rfork = nullptr;
   for (auto& rd : j->reads) {
@@ -139,6 +146,7 @@ int check_cfg(const mt_render_config* c) {
   if (c->mode != 0 && c->mode != 1) return fail(MT_ERR_INVALID, "mode %d", c->mode);
   if (c->spp < 1 || c->spp > 4096) return fail(MT_ERR_INVALID, "spp %d", c->spp);
   if (c->inflight < 0 || c->inflight > 4) return fail(MT_ERR_INVALID, "inflight %d (0..4)", c->inflight);
+  if (c->grid_updates < 0) return fail(MT_ERR_INVALID, "grid_updates %d", c->grid_updates);
   return MT_OK;
 }
 
@@ -171,6 +179,52 @@ int alloc_slot(JobSlot& s, size_t N, int spp, int max_depth, size_t status_strid
   return r;
 }
 
+// Sets up the job's light grid from the scene (CAdaptiveEnvironment.setHDRLuminance,
+// src/cl/algorithms/CAdaptiveEnvironment.java:69-84): initial func from the
+// environment map, accumulation cleared, per-cell SATs built. Runs on the
+// context stream with the job's frames finished.
+int setup_grid(mt_job* j) {
+  mt_scene* sc = j->scene;
+  mt_context* ctx = j->ctx;
+  const bool want = j->cfg.mode == 1 && sc->grid_on && sc->env_present;
+  const bool same = want && j->grid_on && j->nu == sc->grid_nu && j->nv == sc->grid_nv && j->rx == sc->grid_rx &&
+                    j->ry == sc->grid_ry && j->grid_fp64 == (sc->grid_on == 2);
+  if (!same) {
+    dfree(j->d_grid_func);
+    dfree(j->d_grid_sat);
+    dfree(j->d_grid_accum);
+    dfree(j->d_grid_sat64);
+    j->grid_on = 0;
+  }
+  j->grid_frames = 0;
+  if (!want) return MT_OK;
+  if (sc->env_w % sc->grid_rx || sc->env_h % sc->grid_ry)
+    return fail(MT_ERR_INVALID, "light-grid tiles (%d x %d) must divide the %d x %d environment map", sc->grid_rx,
+                sc->grid_ry, sc->env_w, sc->env_h);
+  const size_t n = (size_t)sc->grid_nu * sc->grid_nv;
+  int r = MT_OK;
+  if (!same) {
+    j->nu = sc->grid_nu;
+    j->nv = sc->grid_nv;
+    j->rx = sc->grid_rx;
+    j->ry = sc->grid_ry;
+    j->grid_fp64 = sc->grid_on == 2;
+    r = dalloc(&j->d_grid_func, n);
+    if (!r) r = dalloc(&j->d_grid_sat, n);
+    if (!r) r = dalloc(&j->d_grid_accum, n);
+    if (!r && j->grid_fp64) r = dalloc(&j->d_grid_sat64, n);
+    if (r) return r;
+  }
+  CU(cudaMemsetAsync(j->d_grid_accum, 0, n * 4, ctx->stream));
+  if (launch_grid_init(ctx->stream, sc->d_env_sat64, sc->d_env_sat, sc->env_w, sc->env_h, j->nu, j->nv, j->rx, j->ry,
+                       j->d_grid_func) ||
+      launch_grid_sat(ctx->stream, j->d_grid_func, j->d_grid_sat, j->d_grid_sat64, j->nu, j->nv, j->rx, j->ry,
+                      j->grid_fp64))
+    return fail(MT_ERR_CUDA, "light-grid set-up launch: %s", cudaGetErrorString(cudaGetLastError()));
+  j->grid_on = 1;
+  return MT_OK;
+}
+
 }  // namespace
 
 extern "C" int mt_job_create(mt_context* ctx, mt_scene* scene, const mt_render_config* cfg, mt_job** out) {
@@ -197,6 +251,12 @@ extern "C" int mt_job_create(mt_context* ctx, mt_scene* scene, const mt_render_c
     r = fail(MT_ERR_CUDA, "stream create");
   if (!r && cudaEventCreateWithFlags(&j->rfork, cudaEventDisableTiming) != cudaSuccess)
     r = fail(MT_ERR_CUDA, "event create");
+  if (!r && cudaEventCreateWithFlags(&j->grid_ev, cudaEventDisableTiming) != cudaSuccess)
+    r = fail(MT_ERR_CUDA, "event create");
+  if (!r) {
+    j->scene_version = scene->version;
+    r = setup_grid(j);
+  }
   for (auto& rd : j->reads)
     if (!r && cudaEventCreateWithFlags(&rd.ev, cudaEventDisableTiming) != cudaSuccess)
       r = fail(MT_ERR_CUDA, "event create");
@@ -259,6 +319,16 @@ int enqueue_frame(mt_job* j, JobSlot& s) {
   const mt_render_config& c = j->cfg;
   DevScene S = j->scene->view();
   DevEnv E = j->scene->env_view();
+  if (j->grid_on) {
+    E.grid_on = 1;
+    E.grid_func = j->d_grid_func;
+    E.grid_sat = j->d_grid_sat;
+    E.grid_accum = j->d_grid_accum;
+    E.nu = j->nu;
+    E.nv = j->nv;
+    E.rx = j->rx;
+    E.ry = j->ry;
+  }
   const size_t per_pass_events = 2 + 3 * (size_t)c.max_depth;
   if (j->nslots > 1) {
     const size_t N = (size_t)c.width * c.height;
@@ -288,10 +358,25 @@ extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_coun
   mt_context* ctx = j->ctx;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   CU(cudaSetDevice(ctx->device));
+  if (j->scene_version != j->scene->version) {
+    // The scene's arrays or grid configuration changed (the change waited for
+    // every frame): recapture the graphs and set the light grid up again.
+    for (JobSlot& t : j->slots)
+      if (t.graph) {
+        cudaGraphExecDestroy(t.graph);
+        t.graph = nullptr;
+      }
+    int r = setup_grid(j);
+    if (r) return r;
+    j->scene_version = j->scene->version;
+  }
   JobSlot& s = j->slots[j->next];
   // The slot's previous frame must have consumed its pinned parameters; frames
   // on the other slots keep running meanwhile.
   CU(cudaEventSynchronize(s.done));
+  // CDeviceGI.loop updates the grid after each of its first frames
+  // (src/cl/device/CDeviceGI.java:263-264): those frames accumulate.
+  const int accumulate = j->grid_on && j->grid_frames < c.grid_updates;
   CamF cam;
   std::memcpy(&cam, j->camera, 64);
   const int per_pass = 2 * (1 + 2 * c.max_depth);
@@ -305,12 +390,14 @@ extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_coun
     pp.mode = c.mode;
     pp.rr_depth = c.rr_depth;
     pp.kahan = c.film_kahan;
+    pp.grid_accum = accumulate;
     if (c.mode == 0) std::memcpy(pp.seeds, seeds + (size_t)per_pass * p, sizeof(int32_t) * per_pass);
   }
   // order after work already on the context stream (film clears, uploads)
   CU(cudaEventRecord(s.fork, ctx->stream));
   CU(cudaStreamWaitEvent(s.stream, s.fork, 0));
   if (j->nslots == 1) CU(cudaStreamWaitEvent(s.stream, j->rdone, 0));
+  if (j->grid_on) CU(cudaStreamWaitEvent(s.stream, j->grid_ev, 0));  // the last grid update
   CU(cudaEventRecord(s.ev0, s.stream));
   if (c.use_graph && !c.profile) {
     if (!s.graph) {
@@ -330,6 +417,17 @@ extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_coun
     if (r) return r;
   }
   CU(cudaEventRecord(s.ev1, s.stream));
+  if (accumulate) {
+    // CAdaptiveEnvironment.update (CAdaptiveEnvironment.java:128-137): func = accum,
+    // per-cell SATs rebuilt; later frames wait for it.
+    const size_t n = (size_t)j->nu * j->nv;
+    CU(cudaMemcpyAsync(j->d_grid_func, j->d_grid_accum, n * 4, cudaMemcpyDeviceToDevice, s.stream));
+    if (launch_grid_sat(s.stream, j->d_grid_func, j->d_grid_sat, j->d_grid_sat64, j->nu, j->nv, j->rx, j->ry,
+                        j->grid_fp64))
+      return fail(MT_ERR_CUDA, "light-grid update launch: %s", cudaGetErrorString(cudaGetLastError()));
+    CU(cudaEventRecord(j->grid_ev, s.stream));
+    ++j->grid_frames;
+  }
   if (j->nslots > 1) {
     // Add the frame into the job's film after the previous frame's add (frame
     // order) and after any film read still copying it out.
@@ -515,5 +613,20 @@ extern "C" int mt_film_clear(mt_job* j) {
   }
   CU(cudaMemsetAsync(j->d_totals, 0, 32, ctx->stream));
   j->frames = 0;
+  return MT_OK;
+}
+
+extern "C" int mt_job_grid_read(mt_job* j, float* func, float* sat, float* accum) {
+  if (!j) return fail(MT_ERR_INVALID, "NULL job");
+  if (!j->grid_on) return fail(MT_ERR_INVALID, "the job has no light grid (mode 1, scene grid on, environment set)");
+  mt_context* ctx = j->ctx;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  CU(cudaSetDevice(ctx->device));
+  join_jobs(ctx);
+  const size_t n = (size_t)j->nu * j->nv;
+  if (func) CU(cudaMemcpyAsync(func, j->d_grid_func, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (sat) CU(cudaMemcpyAsync(sat, j->d_grid_sat, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (accum) CU(cudaMemcpyAsync(accum, j->d_grid_accum, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
   return MT_OK;
 }

@@ -218,7 +218,11 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene S, DevEnv E, c
       }
     } else if (E.present) {  // LightHitPass environment branch, Render.cl:106-123
       float pdfW = 0.f;
-      V c = radiance_env(E, d, &pdfW);
+      V c;
+      if (MODE == 1 && E.grid_on)
+        c = radiance_env_grid(E, pp->cam_pos, ps, d, &pdfW, pp->grid_accum && !spec);
+      else
+        c = radiance_env(E, d, &pdfW);
       if (!zero3(c)) {
         if (MODE == 1 && S.nlights > 0) pdfW = pdfW * 0.5f;
         float w = 1.f;
@@ -287,7 +291,10 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene S, DevEnv E, c
       AreaLight L = get_area_light(S, Ml, tri);
       rad = illuminate_area(L, H.p, smp.x, smp.y, &dir, &dist, &pdfW);
     } else if (senv) {
-      rad = illuminate_env(E, smp, &dir, &dist, &pdfW);
+      if (MODE == 1 && E.grid_on)
+        rad = illuminate_env_grid(E, pp->cam_pos, H.p, smp, &dir, &dist, &pdfW);
+      else
+        rad = illuminate_env(E, smp, &dir, &dist, &pdfW);
     }
     if (!zero3(rad)) {
       float bpdf = 0.f, cosO = 0.f;

@@ -40,5 +40,9 @@ int launch_env_build(cudaStream_t st, const float4* rgb, int w, int h, float* lu
 // reference's Kogge-Stone order or FP64.
 int launch_grid_sat(cudaStream_t st, const float* func, float* sat32, double* sat64, int nu, int nv, int rx, int ry,
                     int fp64);
+// Initial light-grid func: each cell's tiles get the map's luminance summed over
+// the tile (from sat64 when not NULL, else sat32).
+int launch_grid_init(cudaStream_t st, const double* sat64, const float* sat32, int w, int h, int nu, int nv, int rx,
+                     int ry, float* func);
 
 }  // namespace mt

@@ -700,6 +700,14 @@ struct Env {
   const R* sat = nullptr;
   int w = 0, h = 0;
   bool present = false;
+  // adaptive light grid (mode 1): FP32 func and per-cell SAT of nu x nv values,
+  // (nu/rx) x (nv/ry) cells of rx x ry tiles; accum may be NULL
+  bool grid_on = false;
+  const float* gfunc = nullptr;
+  const float* gsat = nullptr;
+  float* gaccum = nullptr;
+  int nu = 0, nv = 0, rx = 0, ry = 0;
+  float cam[4] = {0, 0, 0, 0};
   SATRegion region() const { return SATRegion{w, h, 0, 0, w, h}; }
 };
 // Light.cl:195-227
@@ -729,6 +737,84 @@ template <class R> inline V4<R> radiance_env(const Env<R>& E, V4<R> d, R* pdfA) 
   R pdfXY = pdf_sat(reg, xc, yc, E.sat, E.lum);
   R v = R(y) / R(reg.strideY);
   *pdfA = pdfXY / (R(2) * PI_<R>() * PI_<R>() * sin_(v * PI_<R>()));
+  return c;
+}
+
+// ------------------------------------------------ adaptive light grid
+// LightGrid.cl:39-343 and the grid versions of the environment light
+// (illuminateEnvironmentLight1 / getRadianceEnvironmentLight1, Light.cl:140-268),
+// which the reference never calls. The restatement wires them in: the shading
+// point's cell is the direction camera -> point (subgridIndexFromCamera, xyz
+// lanes), the tile is drawn from the cell's SAT (sampleSubgridContinuous,
+// cell (cx, cy) starting at (cx * rx, cy * ry) as subgridGlobalIndex2), the texel
+// from the tile's region of the full-map SAT (getSubgridUnitBound +
+// getSubRegionFromUnitBound, SAT.cl:28-44), and the direction pdf is
+// pdfLL * pdfSS / (2 pi^2 sin) (the reference leaves out pdfLL). An empty cell
+// or tile gives no light sample and pdf 0.
+template <class R> inline int grid_cell(const Env<R>& E, V4<R> p) {
+  const int cw = E.nu / E.rx, ch = E.nv / E.ry;
+  V4<R> d = normalize3(V4<R>{p.x - R(E.cam[0]), p.y - R(E.cam[1]), p.z - R(E.cam[2]), R(0)});
+  return spherical_index(cw, ch, d);
+}
+// A cell holds its own SAT: it is sampled as region (0, 0, rx, ry) of the grid
+// arrays offset to its first tile (row pitch nu), so reads left of or above the
+// cell give 0 as getSubgridValueSAT's range check does (LightGrid.cl:142-147).
+template <class R> inline size_t grid_cell_base(const Env<R>& E, int cell) {
+  const int cw = E.nu / E.rx;
+  return (size_t)((cell / cw) * E.ry) * E.nu + (size_t)((cell % cw) * E.rx);
+}
+template <class R> inline SATRegion grid_cell_region(const Env<R>& E) { return SATRegion{E.nu, E.nv, 0, 0, E.rx, E.ry}; }
+template <class R> inline SATRegion env_tile_region(const Env<R>& E, int tx, int ty) {
+  const float ux0 = (float)tx / (float)E.rx, uy0 = (float)ty / (float)E.ry;
+  const float ux1 = (float)(tx + 1) / (float)E.rx, uy1 = (float)(ty + 1) / (float)E.ry;
+  const int x0 = (int)((float)E.w * ux0), y0 = (int)((float)E.h * uy0);
+  const int x1 = (int)((float)E.w * ux1), y1 = (int)((float)E.h * uy1);
+  return SATRegion{E.w, E.h, x0, y0, x1 - x0, y1 - y0};
+}
+template <class R> inline V4<R> illuminate_env_grid(const Env<R>& E, V4<R> p, V4<R> s, V4<R>* dir, R* dist, R* pdfW) {
+  const size_t base = grid_cell_base(E, grid_cell(E, p));
+  const SATRegion rc = grid_cell_region(E);
+  float uvLL[2], pdfLL[1];
+  int offLL[2];
+  sample_continuous<float>(rc, float(s.x), float(s.y), uvLL, offLL, pdfLL, E.gsat + base, E.gfunc + base);
+  *dist = KF(3.402823e+38);
+  *pdfW = R(0);
+  if (!(pdfLL[0] > 0.f)) return {R(0), R(0), R(0), R(0)};
+  const SATRegion rt = env_tile_region(E, offLL[0], offLL[1]);
+  R uv[2], pdfSS[1];
+  int off[2];
+  sample_continuous(rt, s.z, s.w, uv, off, pdfSS, E.sat, E.lum);
+  if (!(pdfSS[0] > R(0))) return {R(0), R(0), R(0), R(0)};
+  *dir = spherical_direction(uv[0], uv[1]);
+  int idx = spherical_index(E.w, E.h, *dir);
+  V4<R> c = ld4<R>(E.rgb + 4 * (size_t)idx);
+  R sinT = sin_(uv[1] * PI_<R>());
+  *pdfW = (R(pdfLL[0]) * pdfSS[0]) / (R(2) * PI_<R>() * PI_<R>() * sin_(uv[1] * PI_<R>()));
+  if (sinT == R(0)) *pdfW = R(0);
+  return c;
+}
+// The pdf of direction d under illuminate_env_grid from point p (tile = the one
+// holding d's texel; the sine term with v = y / h over the whole map), the
+// radiance, and the accumulation of the texel's luminance at (cell, tile).
+template <class R> inline V4<R> radiance_env_grid(const Env<R>& E, V4<R> p, V4<R> d, R* pdfA, bool accumulate) {
+  int x, y;
+  spherical_xy(E.w, E.h, d, &x, &y);
+  int idx = spherical_index(E.w, E.h, d);
+  V4<R> c = ld4<R>(E.rgb + 4 * (size_t)idx);
+  const int xc = x > E.w - 1 ? E.w - 1 : (x < 0 ? 0 : x), yc = y > E.h - 1 ? E.h - 1 : (y < 0 ? 0 : y);
+  const int tx = xc / (E.w / E.rx), ty = yc / (E.h / E.ry);
+  const size_t base = grid_cell_base(E, grid_cell(E, p));
+  const SATRegion rc = grid_cell_region(E);
+  const float pdfLL = pdf_cond(rc, tx, ty, E.gsat + base, E.gfunc + base) * pdf_marg(rc, ty, E.gsat + base);
+  const SATRegion rt = env_tile_region(E, tx, ty);
+  const R pdfSS = pdf_cond(rt, xc, yc, E.sat, E.lum) * pdf_marg(rt, yc, E.sat);
+  const R v = R(y) / R(E.h);
+  R pdf = (R(pdfLL) * pdfSS) / (R(2) * PI_<R>() * PI_<R>() * sin_(v * PI_<R>()));
+  *pdfA = pdf > R(0) ? pdf : R(0);
+  if (accumulate && E.gaccum) {
+    float* a = E.gaccum + base + (size_t)ty * E.nu + tx;
+    *a = *a + luminance(float(c.x), float(c.y), float(c.z));
+  }
   return c;
 }
 
@@ -813,6 +899,7 @@ struct RenderParams {
   int mode;          // 0: reference semantics; 1: benchmark-config semantics
   float frame_count; // State.frameCount (1 for the first frame)
   int rr_depth;      // mode 1: Russian roulette from this bounce on (0 = off)
+  bool grid_accum = false;  // mode 1 with the grid on: environment hits accumulate into it
 };
 
 // Config-mode seed pair of a (bounce, stage): stage 0 raygen, 1 light pick+sample,
@@ -928,7 +1015,9 @@ void render_frame(const Scene& S, const Env<R>& E, const CameraF& cam_in, const 
         is.hit = 0;
       } else if (E.present) {
         R pdfW;
-        V4<R> c = radiance_env(E, rays[j].d, &pdfW);
+        V4<R> c = (P.mode == 1 && E.grid_on)
+                      ? radiance_env_grid(E, pa.hitpoint, rays[j].d, &pdfW, P.grid_accum && !pa.lastSpecular)
+                      : radiance_env(E, rays[j].d, &pdfW);
         if (zero3(c)) continue;
         if (P.mode == 1 && S.nlights > 0) pdfW = pdfW * KF(0.5);
         R w = R(1);
@@ -978,7 +1067,8 @@ void render_frame(const Scene& S, const Env<R>& E, const CameraF& cam_in, const 
         AreaLight<R> L = get_area_light<R>(lp, S.mesh, tri);
         rad = illuminate_area_light(L, is.p, smp.x, smp.y, &dir, &dist, &pdfW);
       } else if (sample_env) {
-        rad = illuminate_env(E, smp, &dir, &dist, &pdfW);
+        rad = (P.mode == 1 && E.grid_on) ? illuminate_env_grid(E, is.p, smp, &dir, &dist, &pdfW)
+                                         : illuminate_env(E, smp, &dir, &dist, &pdfW);
       }
       if (!zero3(rad)) {
         R bsdfPdf = R(0), cosOut = R(0);
@@ -1427,12 +1517,14 @@ int or_bsdf_eval(const float* material, const float* n, const float* ng, const f
 // One frame. fp64 != 0 runs the FP64 instantiation (accum is then double*).
 // env_sat/env_lum: FP32 arrays for fp64 == 0, FP64 arrays otherwise.
 // ray_counts: [primary, extension, shadow].
-int or_render_frame(const void* camera, int width, int height, int max_depth, int mode, int rr_depth,
-                    const int* seeds, float frame_count, const float* points, const float* uvs,
-                    const float* normals, const int* faces, int nfaces, const float* materials,
-                    const int* nodes, const float* bounds, const float* envmap, const void* env_lum,
-                    const void* env_sat, int env_w, int env_h, int env_present, int fp64, void* accum,
-                    int* counts_out, long long* ray_counts) {
+int or_render_frame_grid(const void* camera, int width, int height, int max_depth, int mode, int rr_depth,
+                         const int* seeds, float frame_count, const float* points, const float* uvs,
+                         const float* normals, const int* faces, int nfaces, const float* materials,
+                         const int* nodes, const float* bounds, const float* envmap, const void* env_lum,
+                         const void* env_sat, int env_w, int env_h, int env_present, int fp64, void* accum,
+                         int* counts_out, long long* ray_counts, const float* grid_func, const float* grid_sat,
+                         float* grid_accum, int nu, int nv, int rx, int ry, const float* cam_pos, int grid_on,
+                         int grid_accumulate) {
   Scene S;
   S.mesh = mesh_of(points, uvs, normals, faces, nfaces);
   S.materials = reinterpret_cast<const SurfaceParameter*>(materials);
@@ -1442,8 +1534,20 @@ int or_render_frame(const void* camera, int width, int height, int max_depth, in
   S.nlights = or_light_list(faces, nfaces, materials, lf.data());
   S.light_faces = lf.data();
   RenderParams P{width, height, max_depth, mode, frame_count, rr_depth};
+  P.grid_accum = grid_accumulate != 0;
   RayCounts rc;
   const CameraF& cam = *static_cast<const CameraF*>(camera);
+  auto set_grid = [&](auto& E) {
+    E.grid_on = grid_on != 0 && env_present != 0;
+    E.gfunc = grid_func;
+    E.gsat = grid_sat;
+    E.gaccum = grid_accum;
+    E.nu = nu;
+    E.nv = nv;
+    E.rx = rx;
+    E.ry = ry;
+    if (cam_pos) for (int i = 0; i < 4; ++i) E.cam[i] = cam_pos[i];
+  };
   if (fp64) {
     Env<double> E;
     E.rgb = envmap;
@@ -1452,6 +1556,7 @@ int or_render_frame(const void* camera, int width, int height, int max_depth, in
     E.w = env_w;
     E.h = env_h;
     E.present = env_present != 0;
+    set_grid(E);
     render_frame<double>(S, E, cam, P, seeds, static_cast<double*>(accum), counts_out, &rc);
   } else {
     Env<float> E;
@@ -1461,10 +1566,106 @@ int or_render_frame(const void* camera, int width, int height, int max_depth, in
     E.w = env_w;
     E.h = env_h;
     E.present = env_present != 0;
+    set_grid(E);
     render_frame<float>(S, E, cam, P, seeds, static_cast<float*>(accum), counts_out, &rc);
   }
   if (ray_counts) { ray_counts[0] = rc.primary; ray_counts[1] = rc.extension; ray_counts[2] = rc.shadow; }
   return S.nlights;
+}
+
+int or_render_frame(const void* camera, int width, int height, int max_depth, int mode, int rr_depth,
+                    const int* seeds, float frame_count, const float* points, const float* uvs,
+                    const float* normals, const int* faces, int nfaces, const float* materials,
+                    const int* nodes, const float* bounds, const float* envmap, const void* env_lum,
+                    const void* env_sat, int env_w, int env_h, int env_present, int fp64, void* accum,
+                    int* counts_out, long long* ray_counts) {
+  return or_render_frame_grid(camera, width, height, max_depth, mode, rr_depth, seeds, frame_count, points, uvs,
+                              normals, faces, nfaces, materials, nodes, bounds, envmap, env_lum, env_sat, env_w,
+                              env_h, env_present, fp64, accum, counts_out, ray_counts, nullptr, nullptr, nullptr, 0,
+                              0, 0, 0, nullptr, 0, 0);
+}
+
+// Grid-guided environment sample (illuminate_env_grid) and pdf/radiance
+// (radiance_env_grid) for one shading point, FP32. pdf_ref_out: the pdf the
+// reference's illuminateEnvironmentLight1 returns (pdfSS / (2 pi^2 sin), no
+// tile probability); gidx_out: the grid entry of (cell, tile).
+void or_env_grid_illuminate(const float* envmap, const float* lum, const float* sat, int w, int h,
+                            const float* gfunc, const float* gsat, int nu, int nv, int rx, int ry, const float* cam4,
+                            const float* p4, const float* s4, float* dir_out, float* pdf_out, float* pdf_ref_out,
+                            float* contrib_out, int* gidx_out) {
+  Env<float> E;
+  E.rgb = envmap; E.lum = lum; E.sat = sat; E.w = w; E.h = h; E.present = true;
+  E.grid_on = true; E.gfunc = gfunc; E.gsat = gsat; E.nu = nu; E.nv = nv; E.rx = rx; E.ry = ry;
+  for (int i = 0; i < 4; ++i) E.cam[i] = cam4[i];
+  V4<float> p{p4[0], p4[1], p4[2], p4[3]}, s{s4[0], s4[1], s4[2], s4[3]};
+  V4<float> dir{0, 0, 0, 0};
+  float dist = 0, pdf = 0;
+  V4<float> c = illuminate_env_grid(E, p, s, &dir, &dist, &pdf);
+  const size_t base = grid_cell_base(E, grid_cell(E, p));
+  const SATRegion rc = grid_cell_region(E);
+  float uvLL[2], pdfLL[1];
+  int offLL[2];
+  sample_continuous<float>(rc, s.x, s.y, uvLL, offLL, pdfLL, gsat + base, gfunc + base);
+  *gidx_out = (int)(base + (size_t)offLL[1] * nu + offLL[0]);
+  *pdf_ref_out = 0.f;
+  if (pdfLL[0] > 0.f) {
+    const SATRegion rt = env_tile_region(E, offLL[0], offLL[1]);
+    float uv[2], pdfSS[1];
+    int off[2];
+    sample_continuous<float>(rt, s.z, s.w, uv, off, pdfSS, sat, lum);
+    *pdf_ref_out = pdfSS[0] / (2.f * PI_<float>() * PI_<float>() * sin_(uv[1] * PI_<float>()));
+  }
+  std::memcpy(dir_out, &dir, 16);
+  *pdf_out = pdf;
+  std::memcpy(contrib_out, &c, 16);
+}
+
+void or_env_grid_radiance(const float* envmap, const float* lum, const float* sat, int w, int h, const float* gfunc,
+                          const float* gsat, int nu, int nv, int rx, int ry, const float* cam4, const float* p4,
+                          const float* d4, float* pdf_out, float* contrib_out, int* gidx_out, float* accum_out) {
+  Env<float> E;
+  E.rgb = envmap; E.lum = lum; E.sat = sat; E.w = w; E.h = h; E.present = true;
+  E.grid_on = true; E.gfunc = gfunc; E.gsat = gsat; E.nu = nu; E.nv = nv; E.rx = rx; E.ry = ry;
+  for (int i = 0; i < 4; ++i) E.cam[i] = cam4[i];
+  std::vector<float> acc((size_t)nu * nv, 0.f);
+  E.gaccum = acc.data();
+  V4<float> p{p4[0], p4[1], p4[2], p4[3]}, d{d4[0], d4[1], d4[2], d4[3]};
+  float pdf = 0;
+  V4<float> c = radiance_env_grid(E, p, d, &pdf, true);
+  *pdf_out = pdf;
+  std::memcpy(contrib_out, &c, 16);
+  *gidx_out = -1;
+  *accum_out = 0.f;
+  for (size_t i = 0; i < acc.size(); ++i)
+    if (acc[i] != 0.f) {
+      *gidx_out = (int)i;
+      *accum_out = acc[i];
+    }
+}
+
+// Initial light-grid func: each cell's tile (tx, ty) holds the map's luminance
+// summed over the tile's region, from the FP64 SAT when given, else from the
+// FP32 SAT in SAT.cl:149-156's order. The reference fills it from a luminance
+// histogram of 500 samples per tile (CAdaptiveEnvironment.java:77, an
+// un-vendored library routine); the tile sum is that histogram's expectation.
+void or_grid_init_func(const double* sat64, const float* sat32, int w, int h, int nu, int nv, int rx, int ry,
+                       float* func) {
+  for (int gy = 0; gy < nv; ++gy)
+    for (int gx = 0; gx < nu; ++gx) {
+      const int tx = gx % rx, ty = gy % ry;
+      const int x0 = (int)((float)w * ((float)tx / (float)rx)), y0 = (int)((float)h * ((float)ty / (float)ry));
+      const int x1 = (int)((float)w * ((float)(tx + 1) / (float)rx)) - 1;
+      const int y1 = (int)((float)h * ((float)(ty + 1) / (float)ry)) - 1;
+      float v;
+      if (sat64) {
+        auto at = [&](int x, int y) { return (x < 0 || y < 0) ? 0.0 : sat64[(size_t)y * w + x]; };
+        v = (float)(at(x1, y1) - at(x0 - 1, y1) - at(x1, y0 - 1) + at(x0 - 1, y0 - 1));
+      } else {
+        auto at = [&](int x, int y) { return (x < 0 || y < 0) ? 0.f : sat32[(size_t)y * w + x]; };
+        v = at(x0 - 1, y0 - 1) + at(x1, y1) - at(x1, y0 - 1) - at(x0 - 1, y1);
+      }
+      func[(size_t)gy * nu + gx] = v;
+    }
 }
 
 }  // extern "C"

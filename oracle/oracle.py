@@ -62,6 +62,11 @@ class Oracle:
         L.or_render_frame.restype = I
         L.or_render_frame.argtypes = [P, I, I, I, I, I, P, F, P, P, P, P, I, P, P, P, P, P, P, I, I, I, I, P,
                                       P, P]
+        L.or_render_frame_grid.restype = I
+        L.or_render_frame_grid.argtypes = L.or_render_frame.argtypes + [P, P, P, I, I, I, I, P, I, I]
+        L.or_grid_init_func.argtypes = [P, P, I, I, I, I, I, I, P]
+        L.or_env_grid_illuminate.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P, P]
+        L.or_env_grid_radiance.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P]
 
 
 class RefOracle:
@@ -95,6 +100,8 @@ class RefOracle:
         L.ref_env_radiance.argtypes = [P, P, P, I, I, P, P, P]
         L.ref_lightgrid_sat.argtypes = [P, P, I, I, I, I]
         L.ref_lightgrid_sample.argtypes = [P, P, I, I, I, I, I, F, F, P, P, P]
+        L.ref_env_grid_illuminate.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P, P]
+        L.ref_env_grid_radiance.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P]
         L.ref_lightgrid_global_index.restype = I
         L.ref_lightgrid_global_index.argtypes = [I, I, I, I, I, I, I]
         L.ref_bsdf_sample.restype = I

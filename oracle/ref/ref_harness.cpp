@@ -331,6 +331,72 @@ void ref_env_radiance(const float* envmap, const float* lum, const float* sat, i
   std::free(lg);
 }
 
+// Grid versions of the environment light: illuminateEnvironmentLight1 and
+// getRadianceEnvironmentLight1 (Light.cl:140-268) on a grid whose func and SAT
+// are given, camera at cam4, shading point p4. The radiance call's
+// accumLightGrid is read back as the one accumulation entry it touched.
+void ref_env_grid_illuminate(const float* envmap, const float* lum, const float* sat, int w, int h,
+                             const float* gfunc, const float* gsat, int nu, int nv, int rx, int ry,
+                             const float* cam4, const float* p4, const float* sample4, float* dir_out,
+                             float* pdf_out, float* contrib_out, float* lum_out, int* gidx_out) {
+  LightGrid* lg = new_light_grid();
+  lg->isPresent = true;
+  lg->width = w;
+  lg->height = h;
+  lg->nu = nu;
+  lg->nv = nv;
+  lg->subgridRangeX = rx;
+  lg->subgridRangeY = ry;
+  lg->cameraPosition = clv_float4(cam4[0], cam4[1], cam4[2], cam4[3]);
+  std::memcpy(lg->func, gfunc, sizeof(float) * (size_t)nu * nv);
+  std::memcpy(lg->sat, gsat, sizeof(float) * (size_t)nu * nv);
+  EnvironmentLight el = getEnvironmentLight(lg, (float4*)envmap, (float*)lum, (float*)sat);
+  float4 s = clv_float4(sample4[0], sample4[1], sample4[2], sample4[3]);
+  float4 p = clv_float4(p4[0], p4[1], p4[2], p4[3]);
+  float4 dir;
+  float dist = 0, pdf = 0, lumv = 0;
+  int idx = 0;
+  float4 c = illuminateEnvironmentLight1(el, p, s, &dir, &dist, &pdf, &lumv, &idx);
+  std::memcpy(dir_out, &dir, 16);
+  *pdf_out = pdf;
+  std::memcpy(contrib_out, &c, 16);
+  *lum_out = lumv;
+  *gidx_out = idx;
+  std::free(lg);
+}
+
+void ref_env_grid_radiance(const float* envmap, const float* lum, const float* sat, int w, int h,
+                           const float* gfunc, const float* gsat, int nu, int nv, int rx, int ry, const float* cam4,
+                           const float* p4, const float* dir4, float* pdf_out, float* contrib_out, int* gidx_out,
+                           float* accum_out) {
+  LightGrid* lg = new_light_grid();
+  lg->isPresent = true;
+  lg->width = w;
+  lg->height = h;
+  lg->nu = nu;
+  lg->nv = nv;
+  lg->subgridRangeX = rx;
+  lg->subgridRangeY = ry;
+  lg->cameraPosition = clv_float4(cam4[0], cam4[1], cam4[2], cam4[3]);
+  std::memcpy(lg->func, gfunc, sizeof(float) * (size_t)nu * nv);
+  std::memcpy(lg->sat, gsat, sizeof(float) * (size_t)nu * nv);
+  EnvironmentLight el = getEnvironmentLight(lg, (float4*)envmap, (float*)lum, (float*)sat);
+  float4 d = clv_float4(dir4[0], dir4[1], dir4[2], dir4[3]);
+  float4 p = clv_float4(p4[0], p4[1], p4[2], p4[3]);
+  float pdf = 0;
+  float4 c = getRadianceEnvironmentLight1(el, d, p, &pdf);
+  *pdf_out = pdf;
+  std::memcpy(contrib_out, &c, 16);
+  *gidx_out = -1;
+  *accum_out = 0.f;
+  for (size_t i = 0; i < (size_t)nu * nv; ++i)
+    if (lg->accum[i] != 0.f) {
+      *gidx_out = (int)i;
+      *accum_out = lg->accum[i];
+    }
+  std::free(lg);
+}
+
 // Light-grid per-cell SAT: prefixSumRowSubgrid then prefixSumColSubgrid
 // (LightGrid.cl:347-400), launched as CAdaptiveEnvironment.java:86-87 does.
 void ref_lightgrid_sat(const float* func, float* sat_out, int nu, int nv, int rx, int ry) {

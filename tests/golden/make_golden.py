@@ -47,7 +47,12 @@ def golden_inputs():
     g["grid_func"] = rng.random(64 * 64).astype(np.float32)
     g["scan_in"] = (rng.random(1000) < 0.3).astype(np.int32)
     g["frame_seeds"] = rng.integers(2 ** 29, 2 ** 30, size=(2, 2 * (1 + 2 * 4))).astype(np.int32)
+    g["grid_p"] = rng.uniform(-1, 1, size=(500, 3))
+    g["grid_s"] = rng.random((500, 4)).astype(np.float32)
     return g
+
+
+GRID_CAM = np.array([0.1, 0.2, 2.5, 0.0], np.float32)
 
 
 def unit(v):
@@ -146,6 +151,25 @@ def main():
     gs = np.zeros(64 * 64, np.float32)
     ref.lib.ref_lightgrid_sat(ptr(g["grid_func"]), ptr(gs), 64, 64, 16, 32)
     out["grid_sat"] = gs
+
+    # grid versions of the environment light on the 64 x 64 grid (4 x 2 cells of 16 x 32 tiles)
+    gill = np.zeros((500, 11), np.float32)
+    grad = np.zeros((500, 7), np.float32)
+    for k in range(500):
+        p4 = np.append(g["grid_p"][k], 0.0).astype(np.float32)
+        dirv, pdf, c = np.zeros(4, np.float32), np.zeros(1, np.float32), np.zeros(4, np.float32)
+        lv, gi = np.zeros(1, np.float32), np.zeros(1, np.int32)
+        ref.lib.ref_env_grid_illuminate(ptr(env), ptr(lum), ptr(sat), 128, 64, ptr(g["grid_func"]), ptr(gs), 64, 64,
+                                        16, 32, ptr(GRID_CAM), ptr(p4), ptr(g["grid_s"][k]), ptr(dirv), ptr(pdf),
+                                        ptr(c), ptr(lv), ptr(gi))
+        gill[k, 0:4], gill[k, 4], gill[k, 5:9], gill[k, 9], gill[k, 10] = dirv, pdf[0], c, lv[0], gi[0]
+        pdf2, c2, gi2, acc = np.zeros(1, np.float32), np.zeros(4, np.float32), np.zeros(1, np.int32), \
+            np.zeros(1, np.float32)
+        ref.lib.ref_env_grid_radiance(ptr(env), ptr(lum), ptr(sat), 128, 64, ptr(g["grid_func"]), ptr(gs), 64, 64, 16,
+                                      32, ptr(GRID_CAM), ptr(p4), ptr(dirv), ptr(pdf2), ptr(c2), ptr(gi2), ptr(acc))
+        grad[k, 0], grad[k, 1:5], grad[k, 5], grad[k, 6] = pdf2[0], c2, gi2[0], acc[0]
+    out["grid_illuminate"] = gill
+    out["grid_radiance"] = grad
 
     sc_out = np.zeros(1000, np.int32)
     total = ref.lib.ref_scan_int(ptr(g["scan_in"]), 1000, ptr(sc_out), 128)

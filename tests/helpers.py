@@ -27,9 +27,22 @@ def env_tables(orc, envmap, w, h):
     return lum, sat
 
 
+def oracle_grid(orc, env, nu, nv, rx, ry):
+    """Initial light grid of an environment map: (func, per-cell SAT), both float32."""
+    envmap, ew, eh = env
+    lum, sat = env_tables(orc, envmap, ew, eh)
+    func = np.zeros(nu * nv, np.float32)
+    orc.lib.or_grid_init_func(None, ptr(sat), ew, eh, nu, nv, rx, ry, ptr(func))
+    gsat = np.zeros(nu * nv, np.float32)
+    orc.lib.or_lightgrid_sat(ptr(func), ptr(gsat), nu, nv, rx, ry)
+    return func, gsat
+
+
 def oracle_frames(orc, sc, nodes, bounds, W, H, depth, mode, rr, seeds_list, env=None, fp64=False, acc=None,
-                  first_frame=1):
-    """Run len(seeds_list) frames of the oracle; returns (accum, counts per frame, ray counts)."""
+                  first_frame=1, grid=None):
+    """Run len(seeds_list) frames of the oracle; returns (accum, counts per frame, ray counts).
+    grid: dict(func, sat, nu, nv, rx, ry[, accum]) turns on grid-guided environment sampling;
+    with an accum array, environment hits add into it."""
     if env is not None:
         envmap, ew, eh = env
         lum, sat = env_tables(orc, envmap, ew, eh)
@@ -51,10 +64,16 @@ def oracle_frames(orc, sc, nodes, bounds, W, H, depth, mode, rr, seeds_list, env
         c = np.zeros(depth, np.int32)
         rc = np.zeros(3, np.int64)
         s = None if seeds is None else np.ascontiguousarray(seeds, np.int32)
-        orc.lib.or_render_frame(ptr(cam), W, H, depth, mode, rr, ptr(s), float(first_frame + f), ptr(sc.points),
-                                ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces), sc.ntri, ptr(sc.materials), ptr(nodes),
-                                ptr(bounds), ptr(envmap), ptr(lum), ptr(sat), ew, eh, int(env is not None),
-                                int(fp64), ptr(acc), ptr(c), ptr(rc))
+        args = [ptr(cam), W, H, depth, mode, rr, ptr(s), float(first_frame + f), ptr(sc.points), ptr(sc.uvs),
+                ptr(sc.normals), ptr(sc.faces), sc.ntri, ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(envmap),
+                ptr(lum), ptr(sat), ew, eh, int(env is not None), int(fp64), ptr(acc), ptr(c), ptr(rc)]
+        if grid is None:
+            orc.lib.or_render_frame(*args)
+        else:
+            pos = np.ascontiguousarray(cam["position"].reshape(-1)[:4], np.float32)
+            gacc = grid.get("accum")
+            orc.lib.or_render_frame_grid(*args, ptr(grid["func"]), ptr(grid["sat"]), ptr(gacc), grid["nu"],
+                                         grid["nv"], grid["rx"], grid["ry"], ptr(pos), 1, int(gacc is not None))
         counts.append(c)
         rays += rc
     return acc, np.stack(counts), rays
@@ -66,4 +85,5 @@ def rel_rmse(a, b):
     return float(np.sqrt(np.mean((a - b) ** 2)) / max(np.sqrt(np.mean(b ** 2)), 1e-30))
 
 
-__all__ = ["oracle_trace", "oracle_any", "env_tables", "oracle_frames", "rel_rmse", "bvh_build", "ptr"]
+__all__ = ["oracle_trace", "oracle_any", "env_tables", "oracle_frames", "oracle_grid", "rel_rmse", "bvh_build",
+           "ptr"]

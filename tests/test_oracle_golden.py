@@ -164,3 +164,31 @@ def test_frames(orc, ginputs, golden):
     acc, counts, _ = oracle_frames(orc, room, nodes, bounds, 64, 48, 4, 0, 0, list(ginputs["frame_seeds"]))
     assert np.array_equal(counts, golden["frame_counts"])
     assert beq(acc, golden["frame_accum"])
+
+
+def test_grid_guided_env_light(orc, ginputs, golden):
+    """Grid versions of the environment light (illuminateEnvironmentLight1,
+    getRadianceEnvironmentLight1, Light.cl:140-268) on a 64 x 64 grid of 4 x 2 cells of
+    16 x 32 tiles over the 128 x 64 map: direction, radiance, the grid entry (cell, tile)
+    and the accumulated luminance equal the reference's; the tile-local pdf factor equals
+    the reference's pdf (the oracle's direction pdf also carries the tile density)."""
+    from tests.golden.make_golden import GRID_CAM
+    env = ginputs["env"]
+    lum, sat = golden["env_lum"], golden["env_sat"]
+    func, gsat = ginputs["grid_func"], golden["grid_sat"]
+    gill, grad = golden["grid_illuminate"], golden["grid_radiance"]
+    for k in range(500):
+        p4 = np.append(ginputs["grid_p"][k], 0.0).astype(np.float32)
+        d, pdf, pref, c, gi = (np.zeros(4, np.float32), np.zeros(1, np.float32), np.zeros(1, np.float32),
+                               np.zeros(4, np.float32), np.zeros(1, np.int32))
+        orc.lib.or_env_grid_illuminate(ptr(env), ptr(lum), ptr(sat), 128, 64, ptr(func), ptr(gsat), 64, 64, 16, 32,
+                                       ptr(GRID_CAM), ptr(p4), ptr(ginputs["grid_s"][k]), ptr(d), ptr(pdf), ptr(pref),
+                                       ptr(c), ptr(gi))
+        assert beq(d, gill[k, 0:4]) and beq(c, gill[k, 5:9]), k
+        assert beq(pref, gill[k, 4:5]), k
+        assert gi[0] == int(gill[k, 10]), k
+        pdf2, c2, gi2, acc = (np.zeros(1, np.float32), np.zeros(4, np.float32), np.zeros(1, np.int32),
+                              np.zeros(1, np.float32))
+        orc.lib.or_env_grid_radiance(ptr(env), ptr(lum), ptr(sat), 128, 64, ptr(func), ptr(gsat), 64, 64, 16, 32,
+                                     ptr(GRID_CAM), ptr(p4), ptr(d), ptr(pdf2), ptr(c2), ptr(gi2), ptr(acc))
+        assert beq(c2, grad[k, 1:5]) and gi2[0] == int(grad[k, 5]) and beq(acc, grad[k, 6:7]), k

@@ -101,3 +101,74 @@ def test_sat_sampling_regions(orc, ref):
             outs.append((uv, off, pdf, off2, pdf2))
         for a, b in zip(*outs):
             assert a.tobytes() == b.tobytes()
+
+
+def test_grid_guided_env_pieces(orc, ref):
+    """The grid versions of the environment light (illuminateEnvironmentLight1,
+    getRadianceEnvironmentLight1, Light.cl:140-268): cell, tile, texel, direction,
+    radiance and accumulation index equal the reference's; the direction pdf is the
+    reference's times the tile density pdfLL (left out in the reference), so the
+    tile-local factor is compared against the reference's pdf."""
+    from tests.helpers import oracle_grid
+    w, h, nu, nv, rx, ry = 512, 256, 320, 320, 16, 32
+    env = scenes.sky_env(w, h)
+    lum, sat = env_tables(orc, env, w, h)
+    func, gsat = oracle_grid(orc, (env, w, h), nu, nv, rx, ry)
+    rng = np.random.default_rng(7)
+    # make the cells differ: scale each cell's tiles by a random factor, zero a few tiles
+    cells = rng.uniform(0.2, 3.0, size=(nv // ry, nu // rx))
+    func = (func.reshape(nv // ry, ry, nu // rx, rx) * cells[:, None, :, None].astype(np.float32)).reshape(-1)
+    func[rng.choice(func.size, 2000, replace=False)] = 0.0
+    func = np.ascontiguousarray(func, np.float32)
+    orc.lib.or_lightgrid_sat(ptr(func), ptr(gsat), nu, nv, rx, ry)
+    cam = np.array([0.1, 0.2, 2.5, 0.0], np.float32)
+    n_pdf = 0
+    for k in range(400):
+        p = np.append(rng.uniform(-1, 1, 3), 0.0).astype(np.float32)
+        s4 = rng.random(4).astype(np.float32)
+        out = {}
+        for name, lib, fn in (("ref", ref.lib, "ref_env_grid_illuminate"), ("or", orc.lib, "or_env_grid_illuminate")):
+            d = np.zeros(4, np.float32)
+            c = np.zeros(4, np.float32)
+            pdf = np.zeros(1, np.float32)
+            extra = np.zeros(1, np.float32)
+            gi = np.zeros(1, np.int32)
+            if name == "ref":
+                getattr(lib, fn)(ptr(env), ptr(lum), ptr(sat), w, h, ptr(func), ptr(gsat), nu, nv, rx, ry, ptr(cam),
+                                 ptr(p), ptr(s4), ptr(d), ptr(pdf), ptr(c), ptr(extra), ptr(gi))
+                out[name] = (d, pdf[0], c, gi[0])
+            else:
+                getattr(lib, fn)(ptr(env), ptr(lum), ptr(sat), w, h, ptr(func), ptr(gsat), nu, nv, rx, ry, ptr(cam),
+                                 ptr(p), ptr(s4), ptr(d), ptr(pdf), ptr(extra), ptr(c), ptr(gi))
+                out[name] = (d, extra[0], c, gi[0], pdf[0])
+        r, o = out["ref"], out["or"]
+        if o[4] == 0.0:
+            continue  # an empty tile: the oracle gives no light sample, the reference divides by zero
+        n_pdf += 1
+        assert r[3] == o[3]
+        assert r[0].tobytes() == o[0].tobytes()
+        assert r[2].tobytes() == o[2].tobytes()
+        assert np.float32(r[1]).tobytes() == np.float32(o[1]).tobytes()
+        # radiance from the same point along the sampled direction: same tile, accumulation entry
+        pdf = np.zeros(1, np.float32)
+        c = np.zeros(4, np.float32)
+        gi = np.zeros(1, np.int32)
+        acc = np.zeros(1, np.float32)
+        ref.lib.ref_env_grid_radiance(ptr(env), ptr(lum), ptr(sat), w, h, ptr(func), ptr(gsat), nu, nv, rx, ry,
+                                      ptr(cam), ptr(p), ptr(o[0]), ptr(pdf), ptr(c), ptr(gi), ptr(acc))
+        pdf2 = np.zeros(1, np.float32)
+        c2 = np.zeros(4, np.float32)
+        gi2 = np.zeros(1, np.int32)
+        acc2 = np.zeros(1, np.float32)
+        orc.lib.or_env_grid_radiance(ptr(env), ptr(lum), ptr(sat), w, h, ptr(func), ptr(gsat), nu, nv, rx, ry,
+                                     ptr(cam), ptr(p), ptr(o[0]), ptr(pdf2), ptr(c2), ptr(gi2), ptr(acc2))
+        assert c.tobytes() == c2.tobytes()
+        assert gi[0] == gi2[0] and acc[0] == acc2[0]
+        # the sampled direction's pdf equals its evaluated pdf once each is multiplied by its
+        # sine term (sampling: the continuous v of the sample; evaluation: the texel row's top)
+        v = np.arccos(np.clip(np.float64(o[0][1]), -1, 1)) / np.pi
+        y = int(v * h)
+        if y > 0:  # row 0's sine term is 0: the evaluated pdf is infinite, as in the full-map version
+            a, b = pdf2[0] * np.sin(y / h * np.pi), o[4] * np.sin(v * np.pi)
+            assert abs(a - b) <= 1e-3 * b
+    assert n_pdf > 300
