@@ -40,22 +40,40 @@ ENV_W, ENV_H = 2048, 1024
 GRID = (1600, 1600, 16, 32)  # light grid: nu, nv, tiles per cell (reference defaults, CLightGrid.java)
 GRID_UPDATES = 5             # CDeviceGI.loop updates the grid after its first 5 frames
 METRIC = "Mrays/s (primary + extension + shadow rays traced, device-counted)"
-WORKLOAD = "soup1M_1920x1080_depth8_rr3_env2048x1024"
+# soup: the 1M-triangle soup at 1 spp (the headline configuration); stadium: the
+# 3.3M-triangle plane + displaced icosphere at 4 spp
+WORKLOADS = {
+    "soup": dict(name="soup1M_1920x1080_depth8_rr3_env2048x1024", spp=1,
+                 scene="1,000,000-triangle soup, centroids U[-1,1]^3, edges N(0,0.005^2), GGX r U[0.05,0.8], "
+                       "albedo U[0.2,0.9]"),
+    "stadium": dict(name="stadium3.3M_1920x1080_spp4_depth8_rr3_env2048x1024", spp=4,
+                    scene="200x200 ground plane of 2,000,000 triangles + icosphere level 8 (1,310,720 triangles, "
+                          "r 0.05) displaced by 3-octave value noise of amplitude 0.005; Lambert/GGX 50/50, "
+                          "r U[0.05,0.8], albedo U[0.2,0.9]"),
+}
+WORKLOAD = WORKLOADS["soup"]["name"]
+
+
+def make_scene(kind, small, width, height):
+    from mambatracer_gb300 import scenes
+    if kind == "stadium":
+        return scenes.stadium(quads=300 if small else 1000, level=6 if small else 8, width=width, height=height)
+    return scenes.soup(200_000 if small else NTRI, seed=1, width=width, height=height)
 
 
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def config_dict(width, height, ntri, world, inflight=1):
+def config_dict(kind, width, height, ntri, world, inflight=1, small=False):
+    w = WORKLOADS[kind]
     return {
-        "workload": WORKLOAD if (width, height, ntri) == (W_DEFAULT, H_DEFAULT, NTRI) else
-        f"soup{ntri}_{width}x{height}_depth{DEPTH}_rr{RR}_env{ENV_W}x{ENV_H}",
-        "scene": f"{ntri}-triangle soup, centroids U[-1,1]^3, edges N(0,0.005^2), GGX r U[0.05,0.8], albedo U[0.2,0.9]",
+        "workload": w["name"] if not small else f"{kind}{ntri}_{width}x{height}_depth{DEPTH}_rr{RR}_env{ENV_W}x{ENV_H}",
+        "scene": w["scene"] if not small else f"{ntri}-triangle {kind} (reduced)",
         "environment": f"{ENV_W}x{ENV_H} FP32 lat-long sky gradient + 0.5 deg Gaussian sun (peak 5e4); SAT built in FP64",
         "light_grid": (f"{GRID[0]}x{GRID[1]} grid of {GRID[2]}x{GRID[3]}-tile cells, FP64 per-cell SATs, updated from "
                        f"environment hits after each of the first {GRID_UPDATES} warm-up frames, then fixed"),
-        "resolution": f"{width}x{height}", "spp_per_step": 1, "max_depth": DEPTH, "rr_from_bounce": RR,
+        "resolution": f"{width}x{height}", "spp_per_step": w["spp"], "max_depth": DEPTH, "rr_from_bounce": RR,
         "rng": "per-pixel seed pixel ^ 0x9E3779B9 into the reference WangHash chain",
         "film": "FP32 Kahan-compensated", "launch": "CUDA graph per frame" + (f", {inflight} frames in flight on separate streams" if inflight > 1 else ""),
         "l2": "no flush: per-step working set (path state + queues ~420 MB, BVH+triangles 112 MB) exceeds the 129 MB L2",
@@ -160,10 +178,10 @@ def cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, second
     return total["rays"], time.perf_counter() - t0, total["frames"]
 
 
-def cpu_scene(orc, ntri):
+def cpu_scene(orc, kind):
     from mambatracer_gb300 import scenes
     from oracle.oracle import bvh_build, ptr
-    sc = scenes.soup(ntri, seed=1)
+    sc = make_scene(kind, False, W_DEFAULT, H_DEFAULT)
     nodes, bounds, _, _ = bvh_build(orc, sc)
     env = scenes.sky_env(ENV_W, ENV_H)
     lum = np.zeros(ENV_W * ENV_H, np.float32)
@@ -212,8 +230,10 @@ def run_gpu(args):
     from mambatracer_gb300 import api, build, scenes
     build.build()
 
-    width, height, ntri = (640, 360, 200_000) if args.small else (W_DEFAULT, H_DEFAULT, NTRI)
-    sc = scenes.soup(ntri, seed=1, width=width, height=height)
+    width, height = (640, 360) if args.small else (W_DEFAULT, H_DEFAULT)
+    spp = WORKLOADS[args.workload]["spp"]
+    sc = make_scene(args.workload, args.small, width, height)
+    ntri = sc.ntri
     env = scenes.sky_env(ENV_W, ENV_H)
     ctx = api.Context(local)
     S = api.Scene(ctx, sc)
@@ -221,14 +241,15 @@ def run_gpu(args):
     S.set_env(env, ENV_W, ENV_H)
     S.grid_config(*GRID, enable=2)  # grid-guided environment sampling, FP64 per-cell SATs
     job = api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, use_graph=1,
-                  inflight=args.inflight, grid_updates=min(GRID_UPDATES, args.warmup))
+                  inflight=args.inflight, grid_updates=min(GRID_UPDATES, args.warmup), spp=spp)
     cam = sc.camera.copy()
     job.set_camera(cam)
 
     from mambatracer_gb300.dist import frame_number
 
     def frame_no(step):
-        return frame_number(step, rank, world)
+        # State.frameCount of the step's first pass; passes of one step take consecutive counts
+        return 1.0 + (frame_number(step, rank, world) - 1.0) * spp
 
     def barrier():
         if world > 1:
@@ -330,7 +351,7 @@ def run_gpu(args):
         t_b1 = per_kernel["trace_closest_b1"]
         traffic, traffic_src = None, None
         tp = os.path.join(ROOT, "profiles", "trace_closest_soup1M_1080p.json")
-        if not args.small and os.path.exists(tp):
+        if not args.small and args.workload == "soup" and os.path.exists(tp):
             tj = json.load(open(tp))
             traffic, traffic_src = tj["dram_bytes_per_launch"], tj["source"]
         achieved = alg_bytes / (t_b1 * 1e-3) / 1e9
@@ -360,12 +381,12 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (procedural soup and sky; no dataset)",
-            "config": config_dict(width, height, ntri, world, args.inflight),
+            "config": config_dict(args.workload, width, height, ntri, world, args.inflight, args.small),
             "rays_per_step": round(total_rays / args.steps / world), "rays_split": rays.tolist(),
             "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e,
-            "gpu_launches": args.steps * (2 + 3 * DEPTH + (1 if args.inflight > 1 else 0)), "clocks": clk,
+            "gpu_launches": args.steps * (spp * (2 + 3 * DEPTH) + (1 if args.inflight > 1 else 0)), "clocks": clk,
             "inflight_frames": args.inflight,
-            "msamples_per_s": round(width * height * args.steps * world / (ms * 1e-3) / 1e6, 2),
+            "msamples_per_s": round(width * height * spp * args.steps * world / (ms * 1e-3) / 1e6, 2),
             "bvh_depth": S.depth, "alg_bytes_seconds": round(t_alg, 1),
         }
     job.close()
@@ -387,7 +408,7 @@ def run_reference(args):
     ob.build()
     orc = Oracle()
     threads = os.cpu_count() or 1
-    sc, nodes, bounds, env, lum, sat = cpu_scene(orc, NTRI)
+    sc, nodes, bounds, env, lum, sat = cpu_scene(orc, args.workload)
     grid = cpu_grid(orc, sat)
     width, height = W_DEFAULT // 4, H_DEFAULT // 4
     for _ in range(args.warmup):
@@ -404,7 +425,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (procedural soup and sky; no dataset)",
-        "config": config_dict(W_DEFAULT, H_DEFAULT, NTRI, world),
+        "config": config_dict(args.workload, W_DEFAULT, H_DEFAULT, sc.ntri, world),
         "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -423,6 +444,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="small case for profiler captures")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--inflight", type=int, default=4, help="frames kept in flight on separate streams (1..4)")
+    ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

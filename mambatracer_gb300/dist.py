@@ -1,6 +1,6 @@
 """Multi-GPU host logic: replicas with disjoint frame numbers, no collective on
-the data path (pixels, samples and jobs are independent; SURVEY-style weak
-scaling). Only the timing/ray totals are reduced, after the timed region.
+the data path (pixels, samples and jobs are independent: weak scaling). Only
+the timing/ray totals are reduced, after the timed region.
 
 frame_number(step, rank, world) gives every rank its own State.frameCount
 stream, so N ranks rendering K steps produce N*K distinct passes of one image

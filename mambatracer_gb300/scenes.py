@@ -167,6 +167,101 @@ def soup(ntri=1_000_000, seed=1, width=1920, height=1080, extent=1.0, edge_sigma
                  materials=_palette_materials(), camera=cam, name=f"soup{ntri}")
 
 
+def _icosphere(level: int):
+    """Unit icosphere: the icosahedron's 20 faces split 4-way `level` times, new
+    vertices at normalised edge midpoints (shared between neighbouring faces)."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = np.array([(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+                  (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)], np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array([(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+                  (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+                  (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)], np.int64)
+    for _ in range(level):
+        nv = v.shape[0]
+        e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+        key = np.minimum(e[:, 0], e[:, 1]) * nv + np.maximum(e[:, 0], e[:, 1])
+        uniq, inv = np.unique(key, return_inverse=True)
+        a, b = uniq // nv, uniq % nv
+        mid = v[a] + v[b]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        v = np.concatenate([v, mid])
+        m = (nv + inv).reshape(3, -1)  # midpoints of edges (0,1), (1,2), (2,0) per face
+        m01, m12, m20 = m[0], m[1], m[2]
+        f = np.concatenate([np.stack([f[:, 0], m01, m20], 1), np.stack([f[:, 1], m12, m01], 1),
+                            np.stack([f[:, 2], m20, m12], 1), np.stack([m01, m12, m20], 1)])
+    return v, f
+
+
+def _value_noise(p: np.ndarray, seed: int, octaves: int = 3, base_freq: float = 4.0) -> np.ndarray:
+    """Value noise in [-1, 1]: random lattice values (seeded hash of the integer
+    lattice point) blended trilinearly with smoothstep weights, octaves at doubling
+    frequency and halving amplitude, normalised by the amplitude sum."""
+    out = np.zeros(p.shape[0], np.float64)
+    amp_sum = 0.0
+    for o in range(octaves):
+        freq, amp = base_freq * 2 ** o, 0.5 ** o
+        q = p * freq
+        i0 = np.floor(q).astype(np.int64)
+        t = q - i0
+        w = t * t * (3.0 - 2.0 * t)
+        acc = np.zeros(p.shape[0], np.float64)
+        for dx in (0, 1):
+            for dy in (0, 1):
+                for dz in (0, 1):
+                    h = ((i0[:, 0] + dx) * 73856093) ^ ((i0[:, 1] + dy) * 19349663) ^ ((i0[:, 2] + dz) * 83492791)
+                    h = (h ^ (seed * 2654435761 + o * 97531)) & 0xFFFFFFFF
+                    h = (h * 2246822519) & 0xFFFFFFFF
+                    h ^= h >> 13
+                    h = (h * 3266489917) & 0xFFFFFFFF
+                    h ^= h >> 16
+                    val = h.astype(np.float64) / 4294967295.0 * 2.0 - 1.0
+                    wx = w[:, 0] if dx else 1.0 - w[:, 0]
+                    wy = w[:, 1] if dy else 1.0 - w[:, 1]
+                    wz = w[:, 2] if dz else 1.0 - w[:, 2]
+                    acc += wx * wy * wz * val
+        out += amp * acc
+        amp_sum += amp
+    return out / amp_sum
+
+
+def _mixed_materials(levels=64):
+    """64 x 64 GGX palette (roughness x albedo) followed by 64 Lambert albedos."""
+    lam = [_material((a, a, a)) for a in (0.2 + 0.7 * (i + 0.5) / levels for i in range(levels))]
+    return np.concatenate([_palette_materials(levels), np.stack(lam)])
+
+
+def stadium(seed=2, quads=1000, size=200.0, level=8, radius=0.05, noise_amp=0.005, width=1920, height=1080) -> Scene:
+    """Teapot in a stadium: a size x size ground plane at y = 0 of quads x quads
+    quads (2 * quads^2 triangles) and an icosphere of the given subdivision level
+    (20 * 4^level triangles) of radius `radius`, displaced along the normal by
+    3-octave value noise of amplitude `noise_amp`, resting on the plane. Per
+    triangle: Lambert or GGX with equal probability, roughness U[0.05, 0.8] and
+    albedo U[0.2, 0.9] (64-level palette). The camera looks at the sphere from
+    about five radii away; the plane runs to the horizon."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    g = np.linspace(-size / 2, size / 2, quads + 1)
+    gx, gz = np.meshgrid(g, g, indexing="xy")
+    plane = np.stack([gx.ravel(), np.zeros(gx.size), gz.ravel()], 1)
+    r0 = np.arange(quads)[:, None] * (quads + 1) + np.arange(quads)[None, :]
+    a, b, c, d = r0.ravel(), r0.ravel() + 1, r0.ravel() + quads + 1, r0.ravel() + quads + 2
+    ptri = np.concatenate([np.stack([a, c, b], 1), np.stack([b, c, d], 1)])  # normals +y
+    sv, sf = _icosphere(level)
+    disp = radius + noise_amp * _value_noise(sv, seed)
+    center = np.array([0.0, radius + noise_amp, 0.0])
+    sphere = center + sv * disp[:, None]
+    pts = np.concatenate([plane, sphere]).astype(np.float32)
+    tri = np.concatenate([ptri, sf + plane.shape[0]]).astype(np.int32)
+    n = tri.shape[0]
+    ggx = rng.random(n) < 0.5
+    ri = rng.integers(0, 64, size=n)
+    ai = rng.integers(0, 64, size=n)
+    mat = np.where(ggx, ri * 64 + ai, 64 * 64 + ai)
+    cam = make_camera((0.16, 0.09, 0.2), (0.0, 0.05, 0.0), (0.0, 1.0, 0.0), 40.0, width, height)
+    return Scene(points=_points(pts), faces=_faces(tri, mat), materials=_mixed_materials(), camera=cam,
+                 name=f"stadium{n}")
+
+
 def sky_env(width=2048, height=1024, sun_elev_deg=30.0, sun_azim_deg=40.0, sun_sigma_deg=0.5,
             sun_peak=5.0e4) -> np.ndarray:
     """FP32 RGB lat-long map (float4 texels, w = 1) in the reference's mapping

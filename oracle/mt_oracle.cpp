@@ -1400,7 +1400,7 @@ void or_env_lum_sat(const float* envmap, int w, int h, float* lum, float* sat) {
   }
 }
 
-// FP64 inclusive SAT of the same luminance (the spec precision of the env SAT build).
+// FP64 inclusive SAT of the same luminance (the precision the GPU's environment SAT build uses).
 void or_env_sat_fp64(const float* lum, int w, int h, double* sat) {
   for (int y = 0; y < h; ++y) {
     double row = 0;

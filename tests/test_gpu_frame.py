@@ -5,7 +5,7 @@ counts equal the oracle's exactly; the film differs only where CUDA's sinf,
 cosf, powf, acosf, atan2f round differently from the host C library (the
 reference's own results depend on its OpenCL device's versions), so it is
 compared with a relative RMSE tolerance of 1e-5 and at least 80 % of pixels
-bit-identical. Benchmark semantics (mode 1) are compared the same way, and the
+bit-identical (50 % on the open-sky stadium). Benchmark semantics (mode 1) are compared the same way, and the
 FP32 Kahan film against the FP64 oracle within 1e-3 relative RMSE.
 """
 import threading
@@ -41,10 +41,13 @@ def seeds_for(depth, frames, seed=5):
     return [rng.integers(2 ** 29, 2 ** 30, size=2 * (1 + 2 * depth)).astype(np.int32) for _ in range(frames)]
 
 
-@pytest.mark.parametrize("which", ["room", "soup_env"])
+@pytest.mark.parametrize("which", ["room", "soup_env", "stadium_env"])
 def test_reference_mode(ctx, orc, which):
     if which == "room":
         sc, W, H, depth, env = scenes.box_room(128, 96), 128, 96, 4, None
+    elif which == "stadium_env":
+        sc = scenes.stadium(quads=60, level=4, width=96, height=64)
+        W, H, depth, env = 96, 64, 6, (scenes.sky_env(512, 256), 512, 256)
     else:
         sc = scenes.soup(100000, seed=2, extent=0.8, edge_sigma=0.01)
         W, H, depth, env = 96, 64, 6, (scenes.sky_env(512, 256), 512, 256)
@@ -62,7 +65,9 @@ def test_reference_mode(ctx, orc, which):
         assert np.array_equal(rays, orays)
     film = J.film()
     assert rel_rmse(film, acc) < FILM_RMSE_TOL
-    assert np.mean(np.all(film == acc, axis=1)) > 0.8
+    # pixels whose paths never met a transcendental that rounds differently stay bit-identical;
+    # the stadium's open sky sends most paths through the environment lookups (acosf, atan2f)
+    assert np.mean(np.all(film == acc, axis=1)) > (0.5 if which == "stadium_env" else 0.8)
     J.close()
     S.close()
 
@@ -151,7 +156,7 @@ def test_inflight_frames_match_one_stream(ctx, orc, inflight):
 
 
 def test_fp64_oracle_image_error(ctx, orc):
-    """Spec bound: FP32 GPU film (Kahan) within 1e-3 relative RMSE of the FP64
+    """Image-error bound: FP32 GPU film (Kahan) within 1e-3 relative RMSE of the FP64
     oracle at matched spp (same pixel-keyed random numbers)."""
     sc = scenes.box_room(64, 64)
     S, nodes, bounds = setup(ctx, orc, sc)

@@ -80,6 +80,27 @@ def test_frame_soup_with_env(orc, ref):
     assert acc_a.tobytes() == acc_b.tobytes()
 
 
+def test_frame_stadium_with_env(orc, ref):
+    """The plane + icosphere scene (shared edges on the plane, a dense cluster on it)."""
+    sc = scenes.stadium(quads=40, level=3, width=48, height=32)
+    nodes, bounds, depth, _ = bvh_build(orc, sc)
+    env = scenes.sky_env(256, 128)
+    lum, sat = env_tables(orc, env, 256, 128)
+    cam = sc.camera.copy()
+    acc_a = np.zeros((48 * 32, 4), np.float32)
+    acc_b = acc_a.copy()
+    seeds = np.random.default_rng(4).integers(2 ** 29, 2 ** 30, size=2 * (1 + 2 * 6)).astype(np.int32)
+    ca, cb = np.zeros(6, np.int32), np.zeros(6, np.int32)
+    ref.lib.ref_render_frame(ptr(cam), 48, 32, 6, ptr(seeds), 1.0, ptr(sc.points), ptr(sc.uvs), ptr(sc.normals),
+                             ptr(sc.faces), sc.ntri, ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(env), ptr(lum),
+                             ptr(sat), 256, 128, 1, ptr(acc_a), ptr(ca))
+    orc.lib.or_render_frame(ptr(cam), 48, 32, 6, 0, 0, ptr(seeds), 1.0, ptr(sc.points), ptr(sc.uvs), ptr(sc.normals),
+                            ptr(sc.faces), sc.ntri, ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(env), ptr(lum),
+                            ptr(sat), 256, 128, 1, 0, ptr(acc_b), ptr(cb), None)
+    assert ca[0] > 500 and np.array_equal(ca, cb)
+    assert acc_a.tobytes() == acc_b.tobytes()
+
+
 def test_sat_sampling_regions(orc, ref):
     """sampleContinuous / sampleDiscrete / getPdfSAT on sub-regions (SAT.cl:158-342)."""
     env = scenes.sky_env(64, 32)
