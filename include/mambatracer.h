@@ -192,6 +192,16 @@ int mt_film_read(mt_job* job, float* rgba, int resolve);
 int mt_film_read_async(mt_job* job, float* rgba, int resolve);
 int mt_film_wait(mt_job* job);
 int mt_film_clear(mt_job* job);
+/* The displayed image: CImage.processImage + CDeviceGI.updateImage
+ * (src/cl/image/CImage.java:124-136, src/cl/device/CDeviceGI.java:355-362,
+ * src/cl/kernel/Image.cl:29-118): film / frame count, Reinhard on the luminance
+ * scaled by exposure / (log-average luminance), gamma, packed as ARGB ints
+ * (width * height). Pixels with zero luminance keep their previous value
+ * (opaque black after job creation or mt_film_clear). The log-average is taken
+ * over the current film on every call (the reference's float scan for it is
+ * defective and runs on its first two frames only); log_average (may be NULL)
+ * receives it. Reference defaults: exposure 0.18, gamma 2.2. */
+int mt_image_argb(mt_job* job, int32_t* argb, float exposure, float gamma, float* log_average);
 /* Rays traced so far: [primary, extension, shadow], and the live queue length
  * after each bounce of the last pass (max_depth ints). */
 int mt_job_stats(mt_job* job, int64_t* rays3, int32_t* counts);

@@ -75,6 +75,7 @@ SIGNATURES = {
     "mt_film_read": (I, [P, P, I]),
     "mt_film_read_async": (I, [P, P, I]),
     "mt_job_grid_read": (I, [P, P, P, P]),
+    "mt_image_argb": (I, [P, P, F, F, P]),
     "mt_film_wait": (I, [P]),
     "mt_film_clear": (I, [P]),
     "mt_job_stats": (I, [P, P, P]),

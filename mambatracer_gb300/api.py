@@ -169,6 +169,13 @@ class Job:
         check(lib().mt_film_wait(self.h))
         self._pending = []
 
+    def image(self, exposure: float = 0.18, gamma: float = 2.2):
+        """The displayed ARGB image (int32 per pixel) and the log-average luminance."""
+        out = np.zeros(self.width * self.height, np.int32)
+        la = C.c_float()
+        check(lib().mt_image_argb(self.h, _p(out), float(exposure), float(gamma), C.byref(la)))
+        return out, la.value
+
     def grid(self):
         """The job's light grid: (func, sat, accum), each nu * nv float32."""
         nu, nv = self.scene.grid[0], self.scene.grid[1]

@@ -184,7 +184,16 @@ struct mt_job {
   double* d_grid_sat64 = nullptr;
   int grid_frames = 0;           // frames that have accumulated into the grid since it was set up
   cudaEvent_t grid_ev = nullptr;  // recorded after the last grid update
+  // displayed image (mt_image_argb), allocated on first use
+  int32_t* d_argb = nullptr;
+  float4* d_fb = nullptr;
+  double* d_tone_part = nullptr;
+  int* d_tone_cnt = nullptr;
+  float* d_tone_tot = nullptr;
 };
+
+// Resets the job's ARGB image to opaque black (InitIntDataRGB), on the context stream.
+void image_reset(mt_job* j);
 
 // Makes the context stream wait for every job stream's submitted work.
 void join_jobs(mt_context* ctx);

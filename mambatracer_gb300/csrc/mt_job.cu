@@ -122,6 +122,11 @@ void free_job(mt_job* j) {
   dfree(j->d_grid_sat);
   dfree(j->d_grid_accum);
   dfree(j->d_grid_sat64);
+  dfree(j->d_argb);
+  dfree(j->d_fb);
+  dfree(j->d_tone_part);
+  dfree(j->d_tone_cnt);
+  dfree(j->d_tone_tot);
   if (j->grid_ev) cudaEventDestroy(j->grid_ev);
   j->grid_ev = nullptr;
   if (j->rfork) cudaEventDestroy(j->rfork);
@@ -612,6 +617,7 @@ extern "C" int mt_film_clear(mt_job* j) {
     CU(cudaMemsetAsync(j->d_film_c, 0, N * 16, ctx->stream));
   }
   CU(cudaMemsetAsync(j->d_totals, 0, 32, ctx->stream));
+  image_reset(j);
   j->frames = 0;
   return MT_OK;
 }

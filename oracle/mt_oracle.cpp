@@ -1643,6 +1643,73 @@ void or_env_grid_radiance(const float* envmap, const float* lum, const float* sa
     }
 }
 
+// CImage.processImage (CImage.java:124-136, Image.cl:29-118, RGBSpace.cl:9-106):
+// averageAccum -> log-average luminance over pixels with Lw > 0 of
+// log(0.01 + Lw) -> Reinhard on the exposure-scaled luminance, applied through
+// xyY -> gamma -> ARGB. Pixels with Lw <= 0 keep their ARGB value. The total
+// is an FP64 sum rounded to FP32 (the reference sums with its float prefix
+// scan, whose lane-0 read of aux[-1] and int truncation in GET_FLOAT make the
+// total ill-defined) and is recomputed on every call (the reference keeps the
+// total of its first two frames). totals_out: {total log luminance, count}.
+void or_tonemap(const float* accum, int n, float frame_count, float exposure, float gamma, int* argb,
+                float* framebuf_out, float* totals_out) {
+  std::vector<float> fb(4 * (size_t)(n > 0 ? n : 1));
+  double tot = 0.0;
+  int cnt = 0;
+  for (int i = 0; i < n; ++i) {
+    const float* a = accum + 4 * (size_t)i;
+    float* f = fb.data() + 4 * (size_t)i;
+    f[0] = a[0] / frame_count;
+    f[1] = a[1] / frame_count;
+    f[2] = a[2] / frame_count;
+    f[3] = 1.f;
+    float Lw = luminance(f[0], f[1], f[2]);
+    if (Lw > 0.f) {
+      tot += (double)std::log(0.01f + Lw);
+      ++cnt;
+    }
+  }
+  const float total = (float)tot;
+  if (totals_out) {
+    totals_out[0] = total;
+    totals_out[1] = (float)cnt;
+  }
+  float logavg = total / (float)cnt;
+  logavg = std::exp(logavg);
+  const float ig = 1.f / gamma;
+  for (int i = 0; i < n; ++i) {
+    float* c = fb.data() + 4 * (size_t)i;
+    float L = luminance(c[0], c[1], c[2]);
+    if (L > 0.f) {
+      float scaled = exposure * L / logavg;
+      float Y = scaled / (1.f + scaled);  // toneSimpleReinhard
+      if (std::isinf(Y) || std::isnan(Y) || Y < 0.000001f) Y = 0.f;  // check, Util.cl:381-387
+      float X_ = 0.5893f * c[0] + 0.1789f * c[1] + 0.1831f * c[2];
+      float Y_ = 0.2904f * c[0] + 0.6051f * c[1] + 0.1045f * c[2];
+      float Z_ = 0.0000f * c[0] + 0.0684f * c[1] + 1.0202f * c[2];
+      float x = 0.f, y = 0.f;
+      float XYZ = X_ + Y_ + Z_;
+      if (!(XYZ < 1e-6f)) {
+        float s = 1.f / XYZ;
+        x = X_ * s;
+        y = Y_ * s;
+      }
+      float X = y < 1e-6f ? 0.f : Y * (x / y);
+      float Z = y < 1e-6f ? 0.f : (Y * (1 - x - y)) / y;
+      c[0] = 1.967f * X - 0.548f * Y - 0.297f * Z;
+      c[1] = -0.955f * X + 1.938f * Y - 0.027f * Z;
+      c[2] = 0.064f * X - 0.130f * Y + 0.982f * Z;
+      c[3] = 1.f;
+      c[0] = std::pow(c[0], ig);
+      c[1] = std::pow(c[1], ig);
+      c[2] = std::pow(c[2], ig);
+      auto q = [](float v) { return (int)(std::fmin(std::fmax(v, 0.f), 1.f) * 255.0f); };
+      argb[i] = (q(c[3]) << 24) | (q(c[0]) << 16) | (q(c[1]) << 8) | q(c[2]);
+    }
+  }
+  if (framebuf_out) std::memcpy(framebuf_out, fb.data(), 16 * (size_t)n);
+}
+
 // Initial light-grid func: each cell's tile (tx, ty) holds the map's luminance
 // summed over the tile's region, from the FP64 SAT when given, else from the
 // FP32 SAT in SAT.cl:149-156's order. The reference fills it from a luminance

@@ -67,6 +67,7 @@ class Oracle:
         L.or_grid_init_func.argtypes = [P, P, I, I, I, I, I, I, P]
         L.or_env_grid_illuminate.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P, P]
         L.or_env_grid_radiance.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P]
+        L.or_tonemap.argtypes = [P, I, F, F, F, P, P, P]
 
 
 class RefOracle:
@@ -102,6 +103,8 @@ class RefOracle:
         L.ref_lightgrid_sample.argtypes = [P, P, I, I, I, I, I, F, F, P, P, P]
         L.ref_env_grid_illuminate.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P, P]
         L.ref_env_grid_radiance.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P]
+        L.ref_average_accum.argtypes = [P, F, I, P, P, P]
+        L.ref_update_frame_image.argtypes = [P, P, F, I, I, F, F]
         L.ref_lightgrid_global_index.restype = I
         L.ref_lightgrid_global_index.argtypes = [I, I, I, I, I, I, I]
         L.ref_bsdf_sample.restype = I

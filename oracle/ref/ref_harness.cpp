@@ -397,6 +397,27 @@ void ref_env_grid_radiance(const float* envmap, const float* lum, const float* s
   std::free(lg);
 }
 
+// CImage.processImage's per-pixel kernels (Image.cl:29-118): averageAccum
+// (frame buffer, log luminance and its predicate per pixel) and
+// updateFrameImage with given totals (the reference computes them with its
+// float prefix sum, whose defects are left out here).
+void ref_average_accum(const float* accum, float frame_count, int n, float* framebuf_out, float* loglw_out,
+                       int* count_out) {
+  float fc = frame_count;
+  int len = n;
+  run_serial(n, [&] {
+    averageAccum((float4*)accum, &fc, (float4*)framebuf_out, loglw_out, count_out, &len);
+  });
+}
+
+void ref_update_frame_image(float* framebuf, int* argb, float total_log, int total_number, int n, float exposure,
+                            float gamma) {
+  int len = n;
+  float tl = total_log, ex = exposure, ga = gamma;
+  int tn = total_number;
+  run_serial(n, [&] { updateFrameImage((float4*)framebuf, argb, &tl, &tn, &len, &ex, &ga); });
+}
+
 // Light-grid per-cell SAT: prefixSumRowSubgrid then prefixSumColSubgrid
 // (LightGrid.cl:347-400), launched as CAdaptiveEnvironment.java:86-87 does.
 void ref_lightgrid_sat(const float* func, float* sat_out, int nu, int nv, int rx, int ry) {

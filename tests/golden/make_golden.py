@@ -49,6 +49,9 @@ def golden_inputs():
     g["frame_seeds"] = rng.integers(2 ** 29, 2 ** 30, size=(2, 2 * (1 + 2 * 4))).astype(np.int32)
     g["grid_p"] = rng.uniform(-1, 1, size=(500, 3))
     g["grid_s"] = rng.random((500, 4)).astype(np.float32)
+    film = (rng.exponential(1.0, size=(64 * 48, 4)) * rng.choice([0.0, 0.3, 3.0, 40.0], size=(64 * 48, 1)))
+    film[:, 3] = 7.0
+    g["tone_film"] = film.astype(np.float32)
     return g
 
 
@@ -170,6 +173,17 @@ def main():
         grad[k, 0], grad[k, 1:5], grad[k, 5], grad[k, 6] = pdf2[0], c2, gi2[0], acc[0]
     out["grid_illuminate"] = gill
     out["grid_radiance"] = grad
+
+    # CImage.processImage per-pixel kernels on a 7-frame film, with the exact totals
+    film = g["tone_film"]
+    fb = np.zeros_like(film)
+    loglw = np.zeros(film.shape[0], np.float32)
+    cnt = np.zeros(film.shape[0], np.int32)
+    ref.lib.ref_average_accum(ptr(film), 7.0, film.shape[0], ptr(fb), ptr(loglw), ptr(cnt))
+    total = np.float32(loglw.astype(np.float64).sum())
+    argb = np.full(film.shape[0], -16777216, np.int32)  # InitIntDataRGB: opaque black
+    ref.lib.ref_update_frame_image(ptr(fb), ptr(argb), float(total), int(cnt.sum()), film.shape[0], 0.18, 2.2)
+    out["tone_loglw"], out["tone_count"], out["tone_argb"] = loglw, cnt, argb
 
     sc_out = np.zeros(1000, np.int32)
     total = ref.lib.ref_scan_int(ptr(g["scan_in"]), 1000, ptr(sc_out), 128)

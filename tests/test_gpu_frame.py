@@ -196,3 +196,33 @@ def test_device_gi_thread(ctx, orc):
     assert np.isfinite(img).all() and img[:, :3].mean() > 0
     dev.job.close()
     S.close()
+
+
+def test_image_argb(ctx, orc):
+    """The displayed ARGB image (CImage.processImage) of the GPU film against the oracle's
+    tonemap of the same film: Reinhard, xyY, gamma and packing per pixel; CUDA's logf/expf/powf
+    may move a channel by one 8-bit step."""
+    from tests.helpers import ptr
+    sc = scenes.box_room(64, 64)
+    S, _, _ = setup(ctx, orc, sc)
+    J = api.Job(ctx, S, 64, 64, max_depth=4, mode=1, rr_depth=3, film_kahan=1, spp=4)
+    J.set_camera(sc.camera)
+    img0, la0 = J.image()
+    assert (img0 == np.int32(-16777216)).all() and la0 == 0.0  # opaque black before any frame
+    J.render(None, 1.0)
+    J.render(None, 5.0)
+    img, la = J.image(exposure=0.18, gamma=2.2)
+    film = J.film()
+    ref = np.full(64 * 64, -16777216, np.int32)
+    tot = np.zeros(2, np.float32)
+    orc.lib.or_tonemap(ptr(film), 64 * 64, 8.0, 0.18, 2.2, ptr(ref), None, ptr(tot))
+    assert abs(la - np.exp(tot[0] / tot[1])) <= 1e-5 * la
+    a = img.view(np.uint8).reshape(-1, 4).astype(np.int32)
+    b = ref.view(np.uint8).reshape(-1, 4).astype(np.int32)
+    assert np.abs(a - b).max() <= 1
+    assert np.mean(img == ref) > 0.99
+    assert np.unique(img).size > 100
+    J.clear()
+    assert (J.image()[0] == np.int32(-16777216)).all()
+    J.close()
+    S.close()

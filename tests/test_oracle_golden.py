@@ -192,3 +192,20 @@ def test_grid_guided_env_light(orc, ginputs, golden):
         orc.lib.or_env_grid_radiance(ptr(env), ptr(lum), ptr(sat), 128, 64, ptr(func), ptr(gsat), 64, 64, 16, 32,
                                      ptr(GRID_CAM), ptr(p4), ptr(d), ptr(pdf2), ptr(c2), ptr(gi2), ptr(acc))
         assert beq(c2, grad[k, 1:5]) and gi2[0] == int(grad[k, 5]) and beq(acc, grad[k, 6:7]), k
+
+
+def test_tonemap(orc, ginputs, golden):
+    """CImage.processImage (Image.cl:29-118, RGBSpace.cl:9-106): averageAccum's log
+    luminance and predicate per pixel, and updateFrameImage's ARGB (Reinhard through xyY,
+    gamma 2.2, exposure 0.18) given the exact log-luminance total; zero pixels keep the
+    initial opaque black."""
+    film = ginputs["tone_film"]
+    n = film.shape[0]
+    argb = np.full(n, -16777216, np.int32)
+    fb = np.zeros_like(film)
+    tot = np.zeros(2, np.float32)
+    orc.lib.or_tonemap(ptr(film), n, 7.0, 0.18, 2.2, ptr(argb), ptr(fb), ptr(tot))
+    loglw = golden["tone_loglw"]
+    assert tot[1] == golden["tone_count"].sum()
+    assert tot[0] == np.float32(loglw.astype(np.float64).sum())
+    assert beq(argb, golden["tone_argb"])

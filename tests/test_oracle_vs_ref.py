@@ -193,3 +193,24 @@ def test_grid_guided_env_pieces(orc, ref):
             a, b = pdf2[0] * np.sin(y / h * np.pi), o[4] * np.sin(v * np.pi)
             assert abs(a - b) <= 1e-3 * b
     assert n_pdf > 300
+
+
+def test_tonemap_frame(orc, ref):
+    """The ARGB image of a rendered box-room film: oracle == reference per-pixel kernels."""
+    from tests.helpers import oracle_frames
+    sc = scenes.box_room(64, 48)
+    nodes, bounds, _, _ = bvh_build(orc, sc)
+    acc, _, _ = oracle_frames(orc, sc, nodes, bounds, 64, 48, 4, 1, 3, [None] * 3)
+    n = acc.shape[0]
+    argb = np.full(n, -16777216, np.int32)
+    tot = np.zeros(2, np.float32)
+    orc.lib.or_tonemap(ptr(acc), n, 3.0, 0.18, 2.2, ptr(argb), None, ptr(tot))
+    fb = np.zeros_like(acc)
+    loglw = np.zeros(n, np.float32)
+    cnt = np.zeros(n, np.int32)
+    ref.lib.ref_average_accum(ptr(acc), 3.0, n, ptr(fb), ptr(loglw), ptr(cnt))
+    assert tot[0] == np.float32(loglw.astype(np.float64).sum()) and tot[1] == cnt.sum()
+    rargb = np.full(n, -16777216, np.int32)
+    ref.lib.ref_update_frame_image(ptr(fb), ptr(rargb), float(tot[0]), int(cnt.sum()), n, 0.18, 2.2)
+    assert cnt.sum() > n // 2
+    assert argb.tobytes() == rargb.tobytes()
