@@ -43,7 +43,8 @@ extern "C" {
 #define MT_ERR_NOMEM -3     /* device allocation failed / over budget */
 #define MT_ERR_DEPTH -4     /* BVH deeper than the 64-level traversal stack */
 #define MT_ERR_DEVICE -5    /* a kernel latched an error (bounded wait expired) */
-#define MT_ERR_BUSY -6      /* served mode: admission refused, retry later */
+#define MT_ERR_BUSY -6      /* served mode: admission refused, retry later; a scene still in use */
+#define MT_ERR_TIMEOUT -7   /* served mode: a wait ran out before the request finished */
 
 typedef struct mt_context mt_context;
 typedef struct mt_buffer mt_buffer;
@@ -258,6 +259,53 @@ int mt_trace_any(mt_scene* scene, const void* rays, int n, int32_t* occluded_out
 /* Device-resident variant for benchmarks: rays/outputs are mt_buffers. */
 int mt_trace_closest_dev(mt_scene* scene, mt_buffer* rays, int n, mt_buffer* t_out, mt_buffer* prim_out,
                          float* ms_out);
+
+/* ---------------------------------------------------------------- served mode
+ * Many render requests of different scenes, resolutions and sample counts run
+ * concurrently on one GPU (the reference renders one job at a time,
+ * CDeviceGI.loop, src/cl/device/CDeviceGI.java:214-271). A request renders spp
+ * benchmark-semantics passes (mode 1) of one camera and returns its
+ * accumulated film. A scheduler thread admits requests first come, first
+ * served onto `lanes` preallocated lanes (stream + path state for the largest
+ * frame) within a budget of path-state bytes (196 B per pixel; 0 = no limit);
+ * no device memory is allocated while requests run. Scenes used by queued or
+ * running requests cannot be destroyed (MT_ERR_BUSY). */
+typedef struct mt_server mt_server;
+typedef struct mt_server_config {
+  int lanes;                 /* requests in flight at once (1..64) */
+  int max_width, max_height; /* largest frame (its pixel count bounds every request) */
+  int max_spp;               /* largest spp per request */
+  int max_depth;             /* bounces per path */
+  int rr_depth;              /* Russian roulette from this bounce on (0 = off) */
+  int film_kahan;            /* compensated film sums */
+  int pad_;
+  uint64_t budget_bytes;     /* admission budget of path state + film, 0 = unlimited */
+} mt_server_config;
+typedef struct mt_served_stats {
+  int64_t completed, cancelled, failed, queued, running, max_queue;
+  int64_t rays[3];  /* primary, extension, shadow rays traced by the server */
+  double p50_ms, p95_ms, p99_ms, max_ms;  /* latency, submission to film delivered, of completed requests */
+  double span_ms;   /* first submission to last completion */
+} mt_served_stats;
+int mt_server_create(mt_context* ctx, const mt_server_config* cfg, mt_server** out);
+/* Cancels queued requests, waits for running ones, frees the lanes. */
+int mt_server_destroy(mt_server* server);
+/* Queues a request; film_out (width * height float4, pinned or pageable host
+ * memory, may be NULL) receives the accumulated film of its spp passes, whose
+ * State.frameCount run from frame_count. No reference counterpart (the
+ * reference's host drives its single device directly). */
+int mt_job_submit(mt_server* server, mt_scene* scene, const void* camera, int width, int height, int spp,
+                  float frame_count, float* film_out, int64_t* id_out);
+/* state: 0 queued, 1 running, 2 done, 3 cancelled, 4 failed; latency_ms: -1
+ * until done. */
+int mt_job_poll(mt_server* server, int64_t id, int* state, double* latency_ms);
+/* A queued request is dropped; a running one finishes but delivers nothing. */
+int mt_job_cancel(mt_server* server, int64_t id);
+/* Waits for a request (timeout_ms < 0: no limit; MT_ERR_TIMEOUT when it runs out). */
+int mt_job_wait(mt_server* server, int64_t id, double timeout_ms);
+/* Waits until no request is queued or running. */
+int mt_server_drain(mt_server* server);
+int mt_server_stats(mt_server* server, mt_served_stats* out);
 
 #ifdef __cplusplus
 }

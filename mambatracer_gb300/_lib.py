@@ -29,6 +29,18 @@ class RenderConfig(C.Structure):
                 ("grid_updates", C.c_int)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("lanes", C.c_int), ("max_width", C.c_int), ("max_height", C.c_int), ("max_spp", C.c_int),
+                ("max_depth", C.c_int), ("rr_depth", C.c_int), ("film_kahan", C.c_int), ("pad_", C.c_int),
+                ("budget_bytes", C.c_uint64)]
+
+
+class ServedStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("cancelled", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64),
+                ("running", C.c_int64), ("max_queue", C.c_int64), ("rays", C.c_int64 * 3), ("p50_ms", C.c_double),
+                ("p95_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double), ("span_ms", C.c_double)]
+
+
 P = C.c_void_p
 I = C.c_int
 F = C.c_float
@@ -76,6 +88,14 @@ SIGNATURES = {
     "mt_film_read_async": (I, [P, P, I]),
     "mt_job_grid_read": (I, [P, P, P, P]),
     "mt_image_argb": (I, [P, P, F, F, P]),
+    "mt_server_create": (I, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
+    "mt_server_destroy": (I, [P]),
+    "mt_job_submit": (I, [P, P, P, I, I, I, F, P, C.POINTER(C.c_int64)]),
+    "mt_job_poll": (I, [P, C.c_int64, PI, C.POINTER(C.c_double)]),
+    "mt_job_cancel": (I, [P, C.c_int64]),
+    "mt_job_wait": (I, [P, C.c_int64, C.c_double]),
+    "mt_server_drain": (I, [P]),
+    "mt_server_stats": (I, [P, C.POINTER(ServedStats)]),
     "mt_film_wait": (I, [P]),
     "mt_film_clear": (I, [P]),
     "mt_job_stats": (I, [P, P, P]),

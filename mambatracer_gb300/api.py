@@ -13,7 +13,7 @@ import threading
 import numpy as np
 
 from . import layout
-from ._lib import RenderConfig, check, lib
+from ._lib import RenderConfig, ServedStats, ServerConfig, check, lib
 
 
 def _p(a):
@@ -310,3 +310,61 @@ class DeviceGI:
         if self._thread:
             self._thread.join()
             self._thread = None
+
+
+class Server:
+    """Served mode: concurrent render requests (mt_job_submit / poll / cancel / wait).
+    A request renders `spp` benchmark-semantics passes of one camera; its film lands in
+    the float32 array given at submission (kept alive here until the request ends)."""
+
+    QUEUED, RUNNING, DONE, CANCELLED, FAILED = range(5)
+
+    def __init__(self, ctx: Context, lanes: int = 8, max_width: int = 1920, max_height: int = 1080,
+                 max_spp: int = 64, max_depth: int = 8, rr_depth: int = 3, film_kahan: int = 1,
+                 budget_bytes: int = 0):
+        self.cfg = ServerConfig(lanes, max_width, max_height, max_spp, max_depth, rr_depth, film_kahan, 0,
+                                budget_bytes)
+        h = C.c_void_p()
+        check(lib().mt_server_create(ctx.h, C.byref(self.cfg), C.byref(h)))
+        self.h = h
+        self._films = {}
+
+    def submit(self, scene: Scene, camera: np.ndarray, width: int, height: int, spp: int,
+               frame_count: float = 1.0, film: bool = True) -> int:
+        cam = np.ascontiguousarray(camera)
+        assert cam.dtype == layout.CAMERA
+        out = np.zeros((width * height, 4), np.float32) if film else None
+        rid = C.c_int64()
+        check(lib().mt_job_submit(self.h, scene.h, _p(cam), width, height, spp, float(frame_count), _p(out),
+                                  C.byref(rid)))
+        self._films[rid.value] = out
+        return rid.value
+
+    def poll(self, rid: int):
+        st, lat = C.c_int(), C.c_double()
+        check(lib().mt_job_poll(self.h, rid, C.byref(st), C.byref(lat)))
+        return st.value, lat.value
+
+    def cancel(self, rid: int):
+        check(lib().mt_job_cancel(self.h, rid))
+
+    def wait(self, rid: int, timeout_ms: float = -1.0):
+        check(lib().mt_job_wait(self.h, rid, float(timeout_ms)))
+        return self._films.get(rid)
+
+    def film(self, rid: int):
+        return self._films.get(rid)
+
+    def drain(self):
+        check(lib().mt_server_drain(self.h))
+
+    def stats(self) -> dict:
+        st = ServedStats()
+        check(lib().mt_server_stats(self.h, C.byref(st)))
+        return {f: (list(getattr(st, f)) if f == "rays" else getattr(st, f)) for f, _ in ServedStats._fields_}
+
+    def close(self):
+        if self.h:
+            check(lib().mt_server_destroy(self.h))
+            self.h = None
+

@@ -38,6 +38,7 @@ __attribute__((visibility("hidden"))) int fail(int code, const char* fmt, ...) {
 int quiesce(mt_context* ctx) {
   join_jobs(ctx);
   CU(cudaStreamSynchronize(ctx->stream));
+  servers_sync(ctx);
   return MT_OK;
 }
 
@@ -320,6 +321,7 @@ extern "C" int mt_scene_light_count(const mt_scene* s) { return s ? s->nlights :
 
 extern "C" int mt_scene_destroy(mt_scene* s) {
   if (!s) return fail(MT_ERR_INVALID, "NULL scene");
+  if (s->refs.load() > 0) return fail(MT_ERR_BUSY, "scene used by %d served requests", s->refs.load());
   {
     std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
     cudaSetDevice(s->ctx->device);

@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -16,6 +17,7 @@
 using namespace mt;
 
 struct mt_job;
+struct mt_server;
 
 // ------------------------------------------------------------------ errors
 namespace mt {
@@ -62,6 +64,7 @@ struct mt_context {
   int* cs_words = nullptr;
   size_t cs_tiles = 0;
   std::vector<mt_job*> jobs;  // jobs whose streams join into `stream`
+  std::vector<mt_server*> servers;  // served-mode schedulers on this context
 };
 
 struct mt_buffer {
@@ -95,6 +98,7 @@ struct mt_scene {
   int env_w = 0, env_h = 0, env_present = 0;
   int grid_nu = 1600, grid_nv = 1600, grid_rx = 16, grid_ry = 32, grid_on = 0;  // grid_on: 0, 1 FP32, 2 FP64 SAT
   unsigned version = 0;  // bumped when device arrays or the grid configuration change
+  std::atomic<int> refs{0};  // served requests queued or running on this scene
 
   DevScene view() const {
     DevScene s{};
@@ -195,8 +199,14 @@ struct mt_job {
 // Resets the job's ARGB image to opaque black (InitIntDataRGB), on the context stream.
 void image_reset(mt_job* j);
 
+// Per-pass camera constants of InitCameraRayDataJitter from a 64-byte
+// CameraStruct, for a width x height frame.
+void camera_constants(const void* cam64, int W, int H, PassParams& pp);
+
 // Makes the context stream wait for every job stream's submitted work.
 void join_jobs(mt_context* ctx);
 // Waits for all work on the context and its jobs' streams, before device arrays
 // that frames read are freed or rewritten.
 int quiesce(mt_context* ctx);
+// Waits for the requests running on the context's servers' lanes.
+void servers_sync(mt_context* ctx);

@@ -9,15 +9,17 @@
 #include "mt_internal.h"
 
 namespace {
-
-struct CamF {
+struct CamF {  // CameraStruct, Util.cl:78-85
   float position[4], lookat[4], up[4], dimension[2], fov, pad;
 };
+}  // namespace
 
 // Camera constants of InitCameraRayDataJitter (Initialize.cl:129-172) and
 // camera_transform (Matrix.cl:216-241), computed once per pass on the host in
 // FP32 with the reference's operation order.
-void camera_constants(const CamF& c, int W, int H, PassParams& pp) {
+void camera_constants(const void* cam64, int W, int H, PassParams& pp) {
+  CamF c;
+  std::memcpy(&c, cam64, sizeof(CamF));
   auto dot4 = [](const float* a, const float* b) { return ((a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]) + a[3] * b[3]; };
   auto norm4 = [&](float* v) {
     float l = std::sqrt(dot4(v, v));
@@ -59,6 +61,8 @@ void camera_constants(const CamF& c, int W, int H, PassParams& pp) {
   pp.dim_h = dimy;
   for (int i = 0; i < 4; ++i) pp.cam_pos[i] = c.position[i];
 }
+
+namespace {
 
 // Adds one frame's film (rendered from zero into its slot's film) into the
 // job's film. With Kahan adds on, the slot film's value is film - film_c and
@@ -382,12 +386,10 @@ extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_coun
   // CDeviceGI.loop updates the grid after each of its first frames
   // (src/cl/device/CDeviceGI.java:263-264): those frames accumulate.
   const int accumulate = j->grid_on && j->grid_frames < c.grid_updates;
-  CamF cam;
-  std::memcpy(&cam, j->camera, 64);
   const int per_pass = 2 * (1 + 2 * c.max_depth);
   for (int p = 0; p < c.spp; ++p) {
     PassParams& pp = s.h_pp[p];
-    camera_constants(cam, c.width, c.height, pp);
+    camera_constants(j->camera, c.width, c.height, pp);
     pp.frame_count = frame_count + (float)p;
     pp.width = c.width;
     pp.height = c.height;

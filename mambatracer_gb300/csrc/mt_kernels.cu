@@ -13,6 +13,8 @@
 // with every queue on the device, so a pass needs no host round trip.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "mt_device.cuh"
 #include "mt_kernels.h"
 #include "mt_scan.cuh"
@@ -401,7 +403,9 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
   const int N = width * height;
   static int bps = 0;
   if (bps == 0) bps = trace_blocks_per_sm();
-  const int trace_grid = num_sms * bps;
+  // persistent traversal: one resident wave, or fewer blocks for a small frame
+  // (a queue never exceeds the frame's pixels), leaving SMs to other streams
+  const int trace_grid = std::max(1, std::min(num_sms * bps, (N + kTraceThreads - 1) / kTraceThreads));
   const int tiles = (N + kShadeThreads - 1) / kShadeThreads;
   int e = 0;
   if (ev) cudaEventRecord(ev[e++], st);
