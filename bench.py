@@ -398,6 +398,121 @@ def run_gpu(args):
         print(json.dumps(out), flush=True)
 
 
+# --------------------------------------------------- batched and served
+def request_list(kind, rng, duration, rate):
+    """Requests (arrival s, scene key, width, height, spp, camera seed) of the batched
+    configuration (64 jobs at t = 0: soup and stadium alternately, 4 spp) or the served
+    one (Poisson arrivals: box room, soup or stadium uniformly, spp in {1, 4, 16, 64});
+    pixel counts log-uniform between the configuration's smallest frame and 1920 x 1080,
+    aspect 16:9 when the frame is wide enough."""
+    out = []
+    if kind == "batched":
+        lo, n = 128 * 128, 64
+        times = np.zeros(n)
+    else:
+        lo = 64 * 64
+        gaps = rng.exponential(1.0 / rate, size=int(rate * duration * 1.5) + 16)
+        times = np.cumsum(gaps)
+        times = times[times < duration]
+        n = len(times)
+    hi = 1920 * 1080
+    for k in range(n):
+        px = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        w = int(min(1920, max(8, round(np.sqrt(px * 16 / 9)))))
+        h = int(min(1080, max(8, round(px / w))))
+        if kind == "batched":
+            key, spp = ("soup", "stadium")[k % 2], 4
+        else:
+            key, spp = ("room", "soup", "stadium")[int(rng.integers(0, 3))], int(rng.choice([1, 4, 16, 64]))
+        out.append((float(times[k]), key, w, h, spp, int(rng.integers(0, 2 ** 31))))
+    return out
+
+
+def sphere_camera(seed, width, height, radius=3.0):
+    from mambatracer_gb300 import layout
+    g = np.random.default_rng(seed).normal(size=3)
+    pos = radius * g / np.linalg.norm(g)
+    up = (0.0, 1.0, 0.0) if abs(pos[1]) < 0.99 * radius else (1.0, 0.0, 0.0)
+    return layout.make_camera(tuple(pos), (0.0, 0.0, 0.0), up, 45.0, width, height)
+
+
+def run_requests(ctx, S, reqs, lanes, budget, api):
+    """Submits every request at its arrival time to a server with `lanes` lanes, waits
+    for all; returns the server's stats and wall seconds."""
+    srv = api.Server(ctx, lanes=lanes, max_width=1920, max_height=1080, max_spp=64, max_depth=DEPTH, rr_depth=RR,
+                     film_kahan=1, budget_bytes=budget)
+    t0 = time.perf_counter()
+    for k, (t, key, w, h, spp, cseed) in enumerate(reqs):
+        now = time.perf_counter() - t0
+        if t > now:
+            time.sleep(t - now)
+        srv.submit(S[key], sphere_camera(cseed, w, h), w, h, spp, float(1 + 64 * k), film=False)
+    srv.drain()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    return st, wall
+
+
+def run_served(args):
+    """Batched (64 uneven jobs at once) or served (Poisson arrivals) rendering through
+    the served-mode scheduler, against the same requests run one at a time."""
+    from mambatracer_gb300 import api, build, scenes
+    build.build()
+    ctx = api.Context(0)
+    env = scenes.sky_env(ENV_W, ENV_H)
+    S = {}
+    depth_of = {}
+    keys = ("soup", "stadium") if args.workload == "batched" else ("room", "soup", "stadium")
+    for key in keys:
+        sc = scenes.box_room(64, 64) if key == "room" else make_scene(key, False, W_DEFAULT, H_DEFAULT)
+        sc_h = api.Scene(ctx, sc)
+        sc_h.build_bvh()
+        depth_of[key] = sc_h.depth
+        if key != "room":
+            sc_h.set_env(env, ENV_W, ENV_H)
+        S[key] = sc_h
+    rng = np.random.default_rng(3 if args.workload == "batched" else 4)
+    reqs = request_list(args.workload, rng, args.duration, args.rate)
+    budget = int(150e9)
+    # warm-up: a few small requests through a one-lane server
+    run_requests(ctx, S, [(0.0, k, 64, 64, 1, 1) for k in keys], 1, budget, api)
+    res = {}
+    for name, lanes in (("concurrent", args.lanes), ("sequential", 1)):
+        st, wall = run_requests(ctx, S, reqs, lanes, budget, api)
+        rays = int(sum(st["rays"]))
+        res[name] = {"lanes": lanes, "mrays_per_s": round(rays / (st["span_ms"] * 1e-3) / 1e6, 2),
+                     "p50_ms": round(st["p50_ms"], 2), "p95_ms": round(st["p95_ms"], 2),
+                     "p99_ms": round(st["p99_ms"], 2), "max_ms": round(st["max_ms"], 2),
+                     "span_s": round(st["span_ms"] * 1e-3, 3), "wall_s": round(wall, 3),
+                     "completed": st["completed"], "max_queue": st["max_queue"], "rays": st["rays"]}
+    pixels = sum(w * h * spp for _, _, w, h, spp, _ in reqs)
+    out = {
+        "metric": METRIC, "value": res["concurrent"]["mrays_per_s"], "unit": "Mrays/s", "n_gpus": 1,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic (procedural scenes and sky; no dataset)",
+        "workload": args.workload, "requests": len(reqs), "samples": pixels,
+        "latency_ms": {k: res["concurrent"][k] for k in ("p50_ms", "p95_ms", "p99_ms", "max_ms")},
+        "concurrent": res["concurrent"], "sequential": res["sequential"],
+        "speedup_vs_sequential": round(res["concurrent"]["mrays_per_s"] / res["sequential"]["mrays_per_s"], 3),
+        "config": {
+            "requests": ("64 jobs submitted at once, soup and stadium alternately, 4 spp" if args.workload == "batched"
+                         else f"Poisson arrivals at {args.rate}/s for {args.duration} s, box room / soup / stadium "
+                              "uniformly, spp in {1, 4, 16, 64}"),
+            "resolution": ("pixel count log-uniform 128^2..1920x1080" if args.workload == "batched"
+                           else "pixel count log-uniform 64^2..1920x1080"),
+            "camera": "uniform on a sphere of radius 3 around the origin, looking at it, fov 45",
+            "max_depth": DEPTH, "rr_from_bounce": RR, "semantics": "benchmark (mode 1), full-map environment sampling",
+            "admission_budget_bytes": budget, "bvh_depth": depth_of,
+            "latency": "submission to film in host memory (pinned staging), host clock",
+            "equal_error": "the sequential run renders the same requests with the same spp",
+        },
+    }
+    for sc_h in S.values():
+        sc_h.close()
+    ctx.close()
+    print(json.dumps(out), flush=True)
+
+
 # ------------------------------------------------------- reference arm
 def run_reference(args):
     rank, world, _ = dist_env()
@@ -444,12 +559,17 @@ def main():
     ap.add_argument("--small", action="store_true", help="small case for profiler captures")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--inflight", type=int, default=4, help="frames kept in flight on separate streams (1..4)")
-    ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS) + ["batched", "served"])
+    ap.add_argument("--lanes", type=int, default=16, help="batched/served: requests in flight")
+    ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
+    ap.add_argument("--duration", type=float, default=60.0, help="served: seconds of arrivals")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload in ("batched", "served"):
+        run_served(args)
     else:
         run_gpu(args)
 
