@@ -92,6 +92,7 @@ extern "C" int mt_ctx_destroy(mt_context* ctx) {
   dfree(ctx->d_scratch);
   dfree(ctx->cs_status);
   dfree(ctx->cs_words);
+  dfree(ctx->d_plain_err);
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   cudaStreamDestroy(ctx->stream);
@@ -122,6 +123,15 @@ extern "C" int mt_finish(mt_context* ctx) {
   CU(cudaSetDevice(ctx->device));
   join_jobs(ctx);
   CU(cudaStreamSynchronize(ctx->stream));
+  if (ctx->d_plain_err) {
+    int e = 0;
+    CU(cudaMemcpy(&e, ctx->d_plain_err, 4, cudaMemcpyDeviceToHost));
+    if (e) {
+      CU(cudaMemset(ctx->d_plain_err, 0, 4));
+      return fail(MT_ERR_DEVICE, "a kernel launched by name met %s", e == 1 ? "an index out of range in its buffers"
+                                                                           : "a BVH deeper than 64 levels");
+    }
+  }
   return MT_OK;
 }
 
@@ -782,24 +792,6 @@ extern "C" int mt_trace_closest_dev(mt_scene* s, mt_buffer* rays, int n, mt_buff
 }
 
 // ------------------------------------------------- kernels by name (stubs)
-struct mt_kernel {
-  mt_context* ctx;
-  std::string name;
-};
-extern "C" const char* mt_kernel_names(void) { return ""; }
-extern "C" int mt_kernel_create(mt_context* ctx, const char* name, mt_kernel** out) {
-  (void)ctx;
-  (void)out;
-  return fail(MT_ERR_INVALID, "unknown kernel '%s'", name ? name : "(null)");
-}
-extern "C" int mt_kernel_set_arg_buf(mt_kernel* k, int, mt_buffer*) { return k ? MT_OK : fail(MT_ERR_INVALID, "NULL"); }
-extern "C" int mt_kernel_set_arg_local(mt_kernel* k, int, size_t) { return k ? MT_OK : fail(MT_ERR_INVALID, "NULL"); }
-extern "C" int mt_launch_1d(mt_kernel* k, size_t, size_t) { return k ? MT_OK : fail(MT_ERR_INVALID, "NULL"); }
-extern "C" int mt_kernel_destroy(mt_kernel* k) {
-  delete k;
-  return MT_OK;
-}
-
 // ------------------------------------------------------------- compaction
 extern "C" int mt_compact_isects(mt_context* ctx, const void* isects_in, const int32_t* pixels_in, int n,
                                  void* isects_out, int32_t* pixels_out, int32_t* count_io) {

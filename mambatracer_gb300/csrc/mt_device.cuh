@@ -199,6 +199,7 @@ struct Bsdf {
   V fix;          // localDirFix
   int mat;        // -1 = invalid
   float pd, pg;   // diffuse / glossy probabilities
+  const Material* pm;  // parameters (the scene's material, or a path's copy of it)
 };
 __device__ __forceinline__ const Material& matl(const DevScene& S, int m) { return S.materials[m]; }
 
@@ -213,7 +214,8 @@ __device__ __forceinline__ Bsdf setup_bsdf(const DevScene& S, V d, V n, int mat)
     return b;
   }
   b.mat = mat;
-  const Material& M = matl(S, mat);
+  b.pm = S.materials + mat;
+  const Material& M = *b.pm;
   V cd = muls(M.diffuse_color, M.diffuse_param.x);
   V cg = muls(M.glossy_color, M.glossy_param.x);
   float ad = luminance(cd.x, cd.y, cd.z), ag = luminance(cg.x, cg.y, cg.z);
@@ -301,13 +303,13 @@ __device__ __forceinline__ V sample_diffuse(const DevScene& S, const Bsdf& b, fl
   float un = ret.z * 1.f / kPi;
   *gen = ret;
   *pdfW += un * b.pd;
-  V c = matl(S, b.mat).diffuse_color;
+  V c = b.pm->diffuse_color;
   return mk(c.x * 1.f / kPi, c.y * 1.f / kPi, c.z * 1.f / kPi, 1.f);
 }
 // Bsdf.cl:396-432
 __device__ __forceinline__ V sample_glossy(const DevScene& S, const Bsdf& b, float sx, float sy, V* gen, float* pdfW) {
   if (b.fix.z < kEpsCos) return zero4();
-  const Material& M = matl(S, b.mat);
+  const Material& M = *b.pm;
   float ax = M.glossy_param.y, ay = M.glossy_param.z;
   V wh = sample_vndf(b.fix, ax, ay, sx, sy);
   V wo = add(neg(b.fix), smul(2.f * dot4(b.fix, wh), wh));
@@ -326,14 +328,14 @@ __device__ __forceinline__ V eval_diffuse(const DevScene& S, const Bsdf& b, V ge
   if (b.pd == 0.f) return zero4();
   if (b.fix.z < kEpsCos || gen.z < kEpsCos) return zero4();
   *pdfW += b.pd * fmaxf(0.f, gen.z * 1.f / kPi);
-  V c = matl(S, b.mat).diffuse_color;
+  V c = b.pm->diffuse_color;
   return mk(c.x * 1.f / kPi, c.y * 1.f / kPi, c.z * 1.f / kPi, 1.f);
 }
 // Bsdf.cl:469-507
 __device__ __forceinline__ V eval_glossy(const DevScene& S, const Bsdf& b, V gen, float* pdfW) {
   if (b.pg == 0.f) return zero4();
   if (b.fix.z < kEpsCos || gen.z < kEpsCos) return zero4();
-  const Material& M = matl(S, b.mat);
+  const Material& M = *b.pm;
   float ax = M.glossy_param.y, ay = M.glossy_param.z;
   V wh = normalize4(add(b.fix, gen));
   float cI = fabsf(b.fix.z), cO = fabsf(gen.z);

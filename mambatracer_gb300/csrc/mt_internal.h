@@ -65,6 +65,7 @@ struct mt_context {
   size_t cs_tiles = 0;
   std::vector<mt_job*> jobs;  // jobs whose streams join into `stream`
   std::vector<mt_server*> servers;  // served-mode schedulers on this context
+  int* d_plain_err = nullptr;       // error latched by kernels launched by name
 };
 
 struct mt_buffer {

@@ -1651,8 +1651,18 @@ void or_env_grid_radiance(const float* envmap, const float* lum, const float* sa
 // scan, whose lane-0 read of aux[-1] and int truncation in GET_FLOAT make the
 // total ill-defined) and is recomputed on every call (the reference keeps the
 // total of its first two frames). totals_out: {total log luminance, count}.
+void or_tonemap_with_total(const float* accum, int n, float frame_count, float exposure, float gamma,
+                           const float* totals_in, int* argb, float* framebuf_out, float* totals_out);
+
 void or_tonemap(const float* accum, int n, float frame_count, float exposure, float gamma, int* argb,
                 float* framebuf_out, float* totals_out) {
+  or_tonemap_with_total(accum, n, frame_count, exposure, gamma, nullptr, argb, framebuf_out, totals_out);
+}
+
+// The same with the log-luminance total and count given (totals_in = {total,
+// count}), as updateFrameImage receives them from its scans; NULL computes them.
+void or_tonemap_with_total(const float* accum, int n, float frame_count, float exposure, float gamma,
+                           const float* totals_in, int* argb, float* framebuf_out, float* totals_out) {
   std::vector<float> fb(4 * (size_t)(n > 0 ? n : 1));
   double tot = 0.0;
   int cnt = 0;
@@ -1669,7 +1679,11 @@ void or_tonemap(const float* accum, int n, float frame_count, float exposure, fl
       ++cnt;
     }
   }
-  const float total = (float)tot;
+  float total = (float)tot;
+  if (totals_in) {
+    total = totals_in[0];
+    cnt = (int)totals_in[1];
+  }
   if (totals_out) {
     totals_out[0] = total;
     totals_out[1] = (float)cnt;

@@ -68,6 +68,7 @@ class Oracle:
         L.or_env_grid_illuminate.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P, P]
         L.or_env_grid_radiance.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P]
         L.or_tonemap.argtypes = [P, I, F, F, F, P, P, P]
+        L.or_tonemap_with_total.argtypes = [P, I, F, F, F, P, P, P, P]
 
 
 class RefOracle:
