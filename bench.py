@@ -513,6 +513,80 @@ def run_served(args):
     print(json.dumps(out), flush=True)
 
 
+# ------------------------------------------------------ plain wavefront
+def run_plain(args):
+    """The reference's own loop through the kernel-by-name layer (one launch per
+    reference kernel, reference buffer layouts, host-driven) against the fused path
+    on the same frames: reference semantics (seeds per allocateState call, no
+    Russian roulette), the 1M soup and sky at 1920 x 1080, depth 8. Both trace the
+    same rays (their films are bit-identical), counted by the fused path."""
+    from mambatracer_gb300 import api, build, plain, scenes
+    from oracle.oracle import Oracle, bvh_build, ptr
+    build.build()
+    orc = Oracle()
+    ctx = api.Context(0)
+    sc = make_scene("soup", False, W_DEFAULT, H_DEFAULT)
+    nodes, bounds, _, _ = bvh_build(orc, sc)
+    env = scenes.sky_env(ENV_W, ENV_H)
+    lum = np.zeros(ENV_W * ENV_H, np.float32)
+    sat = np.zeros(ENV_W * ENV_H, np.float32)
+    orc.lib.or_env_lum_sat(ptr(env), ENV_W, ENV_H, ptr(lum), ptr(sat))
+    rng = np.random.default_rng(17)
+    frames = args.warmup + args.steps
+    seeds = [rng.integers(2 ** 29, 2 ** 30, size=2 * (1 + 2 * DEPTH)).astype(np.int32) for _ in range(frames)]
+    dev = plain.PlainDeviceGI(ctx, sc, nodes, bounds, W_DEFAULT, H_DEFAULT, max_depth=DEPTH,
+                              env=(env, lum, sat, ENV_W, ENV_H))
+    dev.set_camera(sc.camera)
+    for f in range(args.warmup):
+        dev.frame(seeds[f], float(f + 1))
+    ctx.finish()
+    t0 = time.perf_counter()
+    for f in range(args.warmup, frames):
+        dev.frame(seeds[f], float(f + 1))
+    ctx.finish()
+    t_plain = time.perf_counter() - t0
+    dev.free()
+    S = api.Scene(ctx, sc)
+    S.import_bvh(nodes, bounds)
+    S.set_env_with_sat(env, lum, sat, ENV_W, ENV_H)
+    res = {}
+    for name, inflight in (("fused", 1), ("fused_inflight4", 4)):
+        J = api.Job(ctx, S, W_DEFAULT, H_DEFAULT, max_depth=DEPTH, mode=0, film_kahan=0, use_graph=1,
+                    inflight=inflight)
+        J.set_camera(sc.camera)
+        for f in range(args.warmup):
+            J.render(seeds[f], float(f + 1))
+        ctx.finish()
+        J.clear()
+        ctx.finish()
+        ctx.record(0)
+        for f in range(args.warmup, frames):
+            J.render(seeds[f], float(f + 1))
+        ctx.record(1)
+        ctx.finish()
+        res[name] = (ctx.elapsed_ms(0, 1) * 1e-3, int(J.total_rays().sum()))
+        J.close()
+    rays = res["fused"][1]
+    out = {
+        "metric": METRIC, "workload": "plain", "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "dtype": "f32", "data": "synthetic (procedural soup and sky; no dataset)",
+        "value": round(rays / t_plain / 1e6, 2),
+        "plain_ms_per_frame": round(t_plain / args.steps * 1e3, 3),
+        "fused_mrays_per_s": round(rays / res["fused"][0] / 1e6, 2),
+        "fused_ms_per_frame": round(res["fused"][0] / args.steps * 1e3, 3),
+        "fused_inflight4_mrays_per_s": round(res["fused_inflight4"][1] / res["fused_inflight4"][0] / 1e6, 2),
+        "speedup_fused_vs_plain": round(t_plain / res["fused"][0], 3),
+        "rays_per_frame": rays // args.steps,
+        "config": {"scene": WORKLOADS["soup"]["scene"], "resolution": f"{W_DEFAULT}x{H_DEFAULT}", "max_depth": DEPTH,
+                   "semantics": "reference (mode 0): allocateState seeds, no Russian roulette, Q1/Q2 kept",
+                   "plain": "mambatracer_gb300.plain: CDeviceGI.loop + CCompact through mt_launch_1d, wall clock",
+                   "fused": "mt_render_frame, one CUDA graph per frame, device clock"},
+    }
+    S.close()
+    ctx.close()
+    print(json.dumps(out), flush=True)
+
+
 # ------------------------------------------------------- reference arm
 def run_reference(args):
     rank, world, _ = dist_env()
@@ -559,7 +633,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="small case for profiler captures")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--inflight", type=int, default=4, help="frames kept in flight on separate streams (1..4)")
-    ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS) + ["batched", "served"])
+    ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS) + ["batched", "served", "plain"])
     ap.add_argument("--lanes", type=int, default=16, help="batched/served: requests in flight")
     ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="served: seconds of arrivals")
@@ -570,6 +644,8 @@ def main():
         run_reference(args)
     elif args.workload in ("batched", "served"):
         run_served(args)
+    elif args.workload == "plain":
+        run_plain(args)
     else:
         run_gpu(args)
 
