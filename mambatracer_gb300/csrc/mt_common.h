@@ -10,7 +10,9 @@ namespace mt {
 
 constexpr int kMaxDepth = 32;        // bounces per pass (reference: 15)
 constexpr int kStackDepth = 64;      // traversal stack = the reference's 64-bit bitstack
-constexpr int kTraceThreads = 128;   // threads per traversal CTA
+constexpr int kTraceThreads = 128;
+constexpr int kTraceMinBlocksClosest = 12;  // register bounds of the traversal kernels
+constexpr int kTraceMinBlocksShadow = 8;   // threads per traversal CTA
 constexpr int kShadeThreads = 256;   // threads per shade CTA (one compaction tile)
 
 // Device error codes latched in Ctrl::error.

@@ -466,41 +466,48 @@ __device__ __forceinline__ float pdf_marg(const Region& r, int y, const float* s
   float last = sat_range(r, r.minX, r.minY, last_x(r), last_y(r), sat);
   return (fi * (float)(r.sx * r.sy)) / last;
 }
-// SAT.cl:244-259, :275-290, :313-323
+// SAT.cl:244-259, :275-290, :313-323. The region total and the chosen row's
+// integral are read once instead of at every search step (same values, same
+// divisions, so the same result as the reference's per-step recomputation).
 __device__ __forceinline__ void sample_cont(const Region& r, float u0, float u1, float* uv, int* off, float* pdf,
                                             const float* sat, const float* f) {
   float p1, p0;
+  const float last = sat_range(r, r.minX, r.minY, last_x(r), last_y(r), sat);
+  auto marg = [&](int y) { return sat_range(r, r.minX, r.minY, last_x(r), y - 1, sat) / last; };
   {
     int b = r.minY, e = r.minY + r.sy;
     while (b != e) {
       int mid = b + (e - b) / 2;
-      float mv = marg_(r, mid, sat);
+      float mv = marg(mid);
       bool right = !(u1 < mv);
       b = right ? mid + 1 : b;
       e = right ? e : mid;
     }
     int o = b - 1 > 0 ? b - 1 : 0;
     off[1] = o;
-    float m0 = marg_(r, o, sat);
-    float du = (u1 - m0) / (marg_(r, o + 1, sat) - marg_(r, o, sat));
-    p1 = pdf_marg(r, o, sat);
+    float m0 = marg(o);
+    float du = (u1 - m0) / (marg(o + 1) - marg(o));
+    const float fi = sat_range(r, r.minX, o, last_x(r), o, sat);
+    p1 = (fi * (float)(r.sx * r.sy)) / last;  // pdf_marg
     uv[1] = ((float)o + du) / (float)r.nv;
   }
   {
     int y = off[1];
+    const float fi = sat_range(r, r.minX, y, last_x(r), y, sat);
+    auto cond = [&](int x) { return sat_range(r, r.minX, y, x - 1, y, sat) / fi; };
     int b = r.minX, e = r.minX + r.sx;
     while (b != e) {
       int mid = b + (e - b) / 2;
-      float mv = cond_(r, mid, y, sat);
+      float mv = cond(mid);
       bool right = !(u0 < mv);
       b = right ? mid + 1 : b;
       e = right ? e : mid;
     }
     int o = b - 1 > 0 ? b - 1 : 0;
     off[0] = o;
-    float c0 = cond_(r, o, y, sat);
-    float du = (u0 - c0) / (cond_(r, o + 1, y, sat) - cond_(r, o, y, sat));
-    p0 = pdf_cond(r, o, y, sat, f);
+    float c0 = cond(o);
+    float du = (u0 - c0) / (cond(o + 1) - cond(o));
+    p0 = func_at(r, o, y, f) / fi;  // pdf_cond
     uv[0] = ((float)o + du) / (float)r.nu;
   }
   pdf[0] = p0 * p1;

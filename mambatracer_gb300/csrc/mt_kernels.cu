@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "mt_device.cuh"
 #include "mt_kernels.h"
@@ -128,7 +129,11 @@ struct ShadowResolve {
 constexpr int kSteps = 32;
 }  // namespace
 
-__global__ void __launch_bounds__(kTraceThreads, 8) k_trace_closest(DevScene S, Ctrl* ctrl, int b, FrameBufs fb) {
+// MINB: resident blocks per SM the register allocation is bounded for (the
+// traversal is latency-bound: more resident warps hide more load latency, at
+// the price of registers).
+template <int MINB>
+__global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_closest(DevScene S, Ctrl* ctrl, int b, FrameBufs fb) {
   const int count = ctrl->count[b];
   bool overflow = false;
   tr::trace_persistent<false, kSteps>(S, count, &ctrl->work[2 * b], QueueRays{fb.q_o[(b + 1) & 1], fb.q_d[(b + 1) & 1]},
@@ -136,8 +141,9 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_closest(DevScene S, 
   if (overflow) atomicExch(&ctrl->error, kDevErrStack);
 }
 
-__global__ void __launch_bounds__(kTraceThreads, 8) k_trace_shadow(DevScene S, Ctrl* ctrl, int b, int mode, FrameBufs fb,
-                                                                   int kahan) {
+template <int MINB>
+__global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_shadow(DevScene S, Ctrl* ctrl, int b, int mode,
+                                                                      FrameBufs fb, int kahan) {
   // mode 0: shadow slots are the compacted survivor slots (flagged by pixel >= 0)
   const int count = mode == 0 ? ctrl->count[b + 1] : ctrl->shadow[b];
   bool overflow = false;
@@ -390,10 +396,36 @@ __global__ void k_accumulate(const Ctrl* ctrl, int max_depth, int n_pixels, unsi
 
 // ---------------------------------------------------------------- launchers
 namespace {
+// Register bounds of the traversal kernels (resident 128-thread blocks per SM):
+// measured best on the 1M soup, 12 for closest hits (42 registers, a few bytes
+// of spill) and 8 for shadow rays. MT_TRACE_MINB / MT_SHADOW_MINB (8, 12 or 16)
+// select another build of either.
+int env_minb(const char* name, int dflt) {
+  const char* e = std::getenv(name);
+  int x = e ? std::atoi(e) : dflt;
+  return (x == 8 || x == 12 || x == 16) ? x : dflt;
+}
+int trace_minb() {
+  static int v = env_minb("MT_TRACE_MINB", kTraceMinBlocksClosest);
+  return v;
+}
+int shadow_minb() {
+  static int v = env_minb("MT_SHADOW_MINB", kTraceMinBlocksShadow);
+  return v;
+}
+template <int MINB>
 int trace_blocks_per_sm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest, kTraceThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest<MINB>, kTraceThreads, 0);
   return n > 0 ? n : 1;
+}
+template <int MINB>
+void launch_traces(cudaStream_t st, int grid, const DevScene& S, Ctrl* ctrl, int b, int mode, FrameBufs fb, int kahan,
+                   bool closest) {
+  if (closest)
+    k_trace_closest<MINB><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb);
+  else
+    k_trace_shadow<MINB><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan);
 }
 }  // namespace
 
@@ -401,18 +433,25 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
                 int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb, unsigned long long* status,
                 size_t status_stride, int num_sms, cudaEvent_t* ev, unsigned long long* totals) {
   const int N = width * height;
-  static int bps = 0;
-  if (bps == 0) bps = trace_blocks_per_sm();
+  static int bps[17] = {};
+  auto trace = [&](bool closest, int b) {
+    const int minb = closest ? trace_minb() : shadow_minb();
+    if (bps[minb] == 0)
+      bps[minb] = minb == 16 ? trace_blocks_per_sm<16>() : minb == 12 ? trace_blocks_per_sm<12>() : trace_blocks_per_sm<8>();
+    const int grid = std::max(1, std::min(num_sms * bps[minb], (N + kTraceThreads - 1) / kTraceThreads));
+    if (minb == 16) launch_traces<16>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
+    else if (minb == 12) launch_traces<12>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
+    else launch_traces<8>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
+  };
   // persistent traversal: one resident wave, or fewer blocks for a small frame
   // (a queue never exceeds the frame's pixels), leaving SMs to other streams
-  const int trace_grid = std::max(1, std::min(num_sms * bps, (N + kTraceThreads - 1) / kTraceThreads));
   const int tiles = (N + kShadeThreads - 1) / kShadeThreads;
   int e = 0;
   if (ev) cudaEventRecord(ev[e++], st);
   k_raygen<<<(N + 255) / 256, 256, 0, st>>>(d_pp, ctrl, fb);
   if (ev) cudaEventRecord(ev[e++], st);
   for (int b = 1; b <= max_depth; ++b) {
-    k_trace_closest<<<trace_grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb);
+    trace(true, b);
     if (ev) cudaEventRecord(ev[e++], st);
     unsigned long long* stb = status + (size_t)(b - 1) * status_stride;
     if (mode == 0)
@@ -420,7 +459,7 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
     else
       k_shade<1><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
     if (ev) cudaEventRecord(ev[e++], st);
-    k_trace_shadow<<<trace_grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan);
+    trace(false, b);
     if (ev) cudaEventRecord(ev[e++], st);
   }
   if (totals) k_accumulate<<<1, 32, 0, st>>>(ctrl, max_depth, N, totals);
