@@ -12,7 +12,8 @@ constexpr int kMaxDepth = 32;        // bounces per pass (reference: 15)
 constexpr int kStackDepth = 64;      // traversal stack = the reference's 64-bit bitstack
 constexpr int kTraceThreads = 128;
 constexpr int kTraceMinBlocksClosest = 12;  // register bounds of the traversal kernels
-constexpr int kTraceMinBlocksShadow = 8;   // threads per traversal CTA
+constexpr int kTraceMinBlocksShadow = 8;
+constexpr int kShadeMinBlocks = 4;  // register bound of the shading kernel (256-thread blocks per SM)   // threads per traversal CTA
 constexpr int kShadeThreads = 256;   // threads per shade CTA (one compaction tile)
 
 // Device error codes latched in Ctrl::error.

@@ -165,8 +165,8 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_shadow(DevScene S
 // mode 1 (benchmark semantics): samples are keyed on the pixel, Russian
 // roulette runs after the BSDF sample, and the survivors and shadow rays are
 // compacted together afterwards.
-template <int MODE>
-__global__ void __launch_bounds__(kShadeThreads) k_shade(DevScene S, DevEnv E, const PassParams* __restrict__ pp,
+template <int MODE, int MINB>
+__global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEnv E, const PassParams* __restrict__ pp,
                                                          Ctrl* ctrl, int b, FrameBufs fb,
                                                          unsigned long long* status) {
   __shared__ unsigned long long sh[kShadeThreads / 32 + 1];
@@ -413,6 +413,16 @@ int shadow_minb() {
   static int v = env_minb("MT_SHADOW_MINB", kTraceMinBlocksShadow);
   return v;
 }
+// Resident 256-thread blocks per SM the benchmark-semantics shading kernel is
+// bounded for (MT_SHADE_MINB: 3, 4 or 5).
+int shade_minb() {
+  static int v = [] {
+    const char* e = std::getenv("MT_SHADE_MINB");
+    int x = e ? std::atoi(e) : kShadeMinBlocks;
+    return (x == 3 || x == 4 || x == 5) ? x : kShadeMinBlocks;
+  }();
+  return v;
+}
 template <int MINB>
 int trace_blocks_per_sm() {
   int n = 0;
@@ -454,10 +464,15 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
     trace(true, b);
     if (ev) cudaEventRecord(ev[e++], st);
     unsigned long long* stb = status + (size_t)(b - 1) * status_stride;
+    const int sm = shade_minb();
     if (mode == 0)
-      k_shade<0><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+      k_shade<0, 3><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+    else if (sm == 4)
+      k_shade<1, 4><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+    else if (sm == 5)
+      k_shade<1, 5><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
     else
-      k_shade<1><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+      k_shade<1, 3><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
     if (ev) cudaEventRecord(ev[e++], st);
     trace(false, b);
     if (ev) cudaEventRecord(ev[e++], st);
