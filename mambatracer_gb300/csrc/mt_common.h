@@ -10,11 +10,11 @@ namespace mt {
 
 constexpr int kMaxDepth = 32;        // bounces per pass (reference: 15)
 constexpr int kStackDepth = 64;      // traversal stack = the reference's 64-bit bitstack
-constexpr int kTraceThreads = 128;
-constexpr int kTraceMinBlocksClosest = 12;  // register bounds of the traversal kernels
+constexpr int kTraceThreads = 128;   // threads per traversal CTA
+constexpr int kTraceMinBlocksClosest = 12;  // register bounds of the traversal kernels (CTAs per SM)
 constexpr int kTraceMinBlocksShadow = 8;
-constexpr int kShadeMinBlocks = 4;  // register bound of the shading kernel (256-thread blocks per SM)   // threads per traversal CTA
 constexpr int kShadeThreads = 256;   // threads per shade CTA (one compaction tile)
+constexpr int kShadeMinBlocks = 4;   // register bound of the shading kernel (CTAs per SM)
 
 // Device error codes latched in Ctrl::error.
 constexpr int kDevErrLookback = 1;   // decoupled look-back wait expired
