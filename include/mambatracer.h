@@ -193,6 +193,14 @@ int mt_film_read(mt_job* job, float* rgba, int resolve);
 int mt_film_read_async(mt_job* job, float* rgba, int resolve);
 int mt_film_wait(mt_job* job);
 int mt_film_clear(mt_job* job);
+/* The preview device's frame (CDeviceRT.loop, src/cl/device/CDeviceRT.java:176-197,
+ * src/cl/kernel/Raytrace.cl): unjittered camera rays, closest hit, quick
+ * colour (emission, or diffuse colour x cosine to the camera) or the
+ * environment texel with gamma 2.2, as ARGB ints; group (may be NULL): the hit's
+ * material index per pixel, -1 on a miss (updateGroupbufferShadeImage). Host
+ * arrays of width * height ints; waits for the result. */
+int mt_preview_frame(mt_scene* scene, const void* camera, int width, int height, int32_t* argb, int32_t* group);
+
 /* The displayed image: CImage.processImage + CDeviceGI.updateImage
  * (src/cl/image/CImage.java:124-136, src/cl/device/CDeviceGI.java:355-362,
  * src/cl/kernel/Image.cl:29-118): film / frame count, Reinhard on the luminance

@@ -88,6 +88,7 @@ SIGNATURES = {
     "mt_film_read_async": (I, [P, P, I]),
     "mt_job_grid_read": (I, [P, P, P, P]),
     "mt_image_argb": (I, [P, P, F, F, P]),
+    "mt_preview_frame": (I, [P, P, I, I, P, P]),
     "mt_server_create": (I, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
     "mt_server_destroy": (I, [P]),
     "mt_job_submit": (I, [P, P, P, I, I, I, F, P, C.POINTER(C.c_int64)]),

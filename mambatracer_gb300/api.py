@@ -104,6 +104,15 @@ class Scene:
         check(lib().mt_env_grid_config(self.h, nu, nv, rx, ry, enable))
         self.grid = (nu, nv, rx, ry, enable)
 
+    def preview(self, camera: np.ndarray, width: int, height: int):
+        """The preview device's frame (CDeviceRT): ARGB ints and the material group per pixel."""
+        cam = np.ascontiguousarray(camera)
+        assert cam.dtype == layout.CAMERA
+        argb = np.zeros(width * height, np.int32)
+        group = np.zeros(width * height, np.int32)
+        check(lib().mt_preview_frame(self.h, _p(cam), width, height, _p(argb), _p(group)))
+        return argb, group
+
     @property
     def light_count(self) -> int:
         return lib().mt_scene_light_count(self.h)

@@ -844,6 +844,145 @@ __global__ void k_grid_init(GridHdr* g, int which_mask, int copy_func) {  // ini
     if (which_mask & (1 << w)) gv(g, w)[id] = 0.f;
 }
 
+// ---------------------------------------------------------- preview device
+// Raytrace.cl (CDeviceRT): unjittered camera rays, a BSDF per pixel, quick
+// shading, the environment as background, the material group per pixel.
+
+// InitCameraRayData (Raytrace.cl:1-31): no jitter, no length check
+__global__ void k_rt_camera_rays(PassParams pp, RRay* rays, int cap) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= cap) return;
+  const int W = pp.width;
+  const float px = (float)(id % W), py = (float)(id / W);
+  V d = normalize4(mk(pp.cam_a * (2.f * px / pp.dim_w - 1.f), -2.f * py / pp.dim_h + 1.f, -pp.cam_d, 0.f));
+  const float* m = pp.cam_m;
+  V z = zero4();
+  V m0 = mk(m[0], m[1], m[2], m[3]), m1 = mk(m[4], m[5], m[6], m[7]), m2 = mk(m[8], m[9], m[10], m[11]),
+    m3 = mk(m[12], m[13], m[14], m[15]);
+  V o = mk(dot3(m0, z) + m0.w, dot3(m1, z) + m1.w, dot3(m2, z) + m2.w, dot3(m3, z) + m3.w);
+  if (!(o.w == 1.f)) o = mk(o.x / o.w, o.y / o.w, o.z / o.w, 0.f);
+  o.w = 0.f;
+  V dw = mk(dot4(m0, d), dot4(m1, d), dot4(m2, d), 0.f);
+  init_ray(rays + id, o, dw, 0.001f, CUDART_INF_F);
+}
+
+// SetupBSDFRaytrace (Raytrace.cl:34-50): the whole Bsdf per pixel; an invalid
+// one keeps materialID -1 with its material's parameters
+__global__ void k_rt_setup_bsdf(const RIsect* isects, const RRay* rays, RBsdf* bsdfs, const Material* materials,
+                                int nmat, int cap, int* err) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= cap) return;
+  const RIsect& is = isects[id];
+  if (!is.hit) return;
+  if (is.mat < 0 || is.mat >= nmat) {
+    latch(err, kErrIndex);
+    return;
+  }
+  DevScene S{};
+  S.materials = materials;
+  const Bsdf b = setup_bsdf(S, v4(rays[id].d), v4(is.n), is.mat);
+  RBsdf& o = bsdfs[id];
+  o.param = materials[is.mat];
+  o.frame.mX = f4(b.frame.mX);
+  o.frame.mY = f4(b.frame.mY);
+  o.frame.mZ = f4(b.frame.mZ);
+  o.localDirFix = f4(b.fix);
+  o.localGeomN = f4(local_coord(b.frame, v4(is.ng)));
+  o.materialID = b.mat;
+  o.diffProb = b.pd;
+  o.glossyProb = b.pg;
+}
+
+// textureInitPassRT / updateToTextureColorRT (Raytrace.cl:52-145)
+__global__ void k_rt_texture_pass(const RBsdf* bsdfs, const RIsect* isects, RTex* tex, int cap) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= cap) return;
+  const RBsdf& b = bsdfs[id];
+  if (is_emitter(b.param)) return;
+  RTex* t = tex + id;
+  t->parameters.x = b.materialID;
+  const int ux = __float_as_int(isects[id].uv.x), uy = __float_as_int(isects[id].uv.y);
+  t->diffuse = b.param.isDiffuseTexture ? make_int4(ux, uy, t->diffuse.z, 1) : make_int4(t->diffuse.x, t->diffuse.y, t->diffuse.z, 0);
+  t->glossy = b.param.isGlossyTexture ? make_int4(ux, uy, t->glossy.z, 1) : make_int4(t->glossy.x, t->glossy.y, t->glossy.z, 0);
+  t->roughness = b.param.isRoughnessTexture ? make_int4(ux, uy, t->roughness.z, 1)
+                                            : make_int4(t->roughness.x, t->roughness.y, t->roughness.z, 0);
+}
+__global__ void k_rt_texture_color(RBsdf* bsdfs, const RTex* tex, int cap) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= cap) return;
+  Material& P = bsdfs[id].param;
+  const RTex& t = tex[id];
+  if (t.diffuse.w) P.diffuse_color = argb_f4(t.diffuse.z);
+  if (t.glossy.w) P.glossy_color = argb_f4(t.glossy.z);
+  if (t.roughness.w) {
+    const float4 c = argb_f4(t.roughness.z);
+    P.glossy_param.y = c.x;
+    P.glossy_param.z = c.y;
+  }
+}
+
+// getQuickSurfaceColor (Material.cl:33-43) packed by getIntARGB with w = 1
+__device__ __forceinline__ int quick_argb(const Material& P, float coeff) {
+  V c = is_emitter(P) ? v4(P.emission_color) : muls(v4(P.diffuse_color), coeff);
+  return argb_int(c.x, c.y, c.z, 1.f);
+}
+// backgroundShade's colour (Raytrace.cl:175-204): the texel with gamma 2.2
+__device__ __forceinline__ int background_argb(const float4* env, int w, int h, V d) {
+  int x, y;
+  sph_xy(w, h, d, &x, &y);
+  const float4 e = env[sph_index(w, h, x, y)];
+  const float ig = 1.f / 2.2f;
+  return argb_int(powf(e.x, ig), powf(e.y, ig), powf(e.z, ig), e.w);
+}
+
+// fastShade (Raytrace.cl:147-173)
+__global__ void k_rt_fast_shade(const RIsect* isects, const RBsdf* bsdfs, int* argb, int cap) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= cap || !isects[id].hit) return;
+  argb[id] = quick_argb(bsdfs[id].param, bsdfs[id].localDirFix.z);
+}
+// backgroundShade (Raytrace.cl:175-204)
+__global__ void k_rt_background(const RIsect* isects, int* argb, const RRay* rays, const float4* env,
+                                const GridHdr* grid, int cap) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= cap || isects[id].hit) return;
+  argb[id] = grid->isPresent ? background_argb(env, grid->width, grid->height, v4(rays[id].d))
+                             : argb_int(0.f, 0.f, 0.f, 1.f);
+}
+// updateGroupbufferShadeImage (Raytrace.cl:206-220)
+__global__ void k_rt_group(const RIsect* isects, int* group, int cap) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= cap) return;
+  group[id] = isects[id].hit ? (isects[id].mat & 0xFFFF) : -1;
+}
+// findBound (Util.cl:830-884): bound of the faces whose material index is the
+// group's; float min/max through ordered integer atomics (one atomic per lane)
+__device__ __forceinline__ void atomic_min_f(float* a, float v) {
+  if (v >= 0.f) atomicMin(reinterpret_cast<int*>(a), __float_as_int(v));
+  else atomicMax(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_f(float* a, float v) {
+  if (v >= 0.f) atomicMax(reinterpret_cast<int*>(a), __float_as_int(v));
+  else atomicMin(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+__global__ void k_find_bound(const int* group, MeshArgs M, const int* size, float* bound, int cap, int* err) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= min(*size, cap)) return;
+  if (!face_ok(M, id)) {
+    latch(err, kErrIndex);
+    return;
+  }
+  const Face& F = M.faces[id];
+  if ((F.mat & 0xFFFF) != group[0]) return;
+  const float4 p1 = M.points[F.vx], p2 = M.points[F.vy], p3 = M.points[F.vz];
+  atomic_min_f(bound + 0, fminf(fminf(p1.x, p2.x), p3.x));
+  atomic_min_f(bound + 1, fminf(fminf(p1.y, p2.y), p3.y));
+  atomic_min_f(bound + 2, fminf(fminf(p1.z, p2.z), p3.z));
+  atomic_max_f(bound + 3, fmaxf(fmaxf(p1.x, p2.x), p3.x));
+  atomic_max_f(bound + 4, fmaxf(fmaxf(p1.y, p2.y), p3.y));
+  atomic_max_f(bound + 5, fmaxf(fmaxf(p1.z, p2.z), p3.z));
+}
+
 }  // namespace plain
 }  // namespace mt
 
@@ -861,6 +1000,7 @@ enum KernelId {
   kLocalScanFloat, kGroupScanFloat, kGlobalScanFloat, kGlobalTotalFloat,
   kIdentifyLights, kPrepareLights,
   kGridRowScan, kGridColScan, kGridInit, kGridInitFuncSat, kGridCalcFunc,
+  kRtCameraRays, kRtSetupBsdf, kRtTexturePass, kRtTextureColor, kRtFastShade, kRtBackground, kRtGroup, kFindBound,
   kNumKernels
 };
 
@@ -881,6 +1021,8 @@ const Spec kSpecs[kNumKernels] = {
     {"identifyMeshLights", 4}, {"prepareLightInfo", 4},
     {"prefixSumRowSubgrid", 2}, {"prefixSumColSubgrid", 2}, {"initLightGrid", 1}, {"initFuncAndSat", 1},
     {"calculateFunc", 1},
+    {"InitCameraRayData", 2}, {"SetupBSDFRaytrace", 4}, {"textureInitPassRT", 3}, {"updateToTextureColorRT", 2},
+    {"fastShade", 3}, {"backgroundShade", 6}, {"updateGroupbufferShadeImage", 3}, {"findBound", 7},
 };
 
 std::string names_list() {
@@ -1245,6 +1387,57 @@ extern "C" int mt_launch_1d(mt_kernel* k, size_t global, size_t local) {
       k_grid_init<<<nb, 256, 0, st>>>(ptr<GridHdr>(k, 0), k->id == kGridInit ? 7 : 6, k->id == kGridCalcFunc);
       break;
     }
+    case kRtCameraRays: {
+      unsigned char cam[64];
+      if (int r = read_host(ctx, cam, k->args[0], 64)) return r;
+      float dim[2];
+      std::memcpy(dim, cam + 48, 8);
+      const int W = (int)dim[0], H = (int)dim[1];
+      if (W <= 0 || H <= 0) return fail(MT_ERR_INVALID, "camera dimension %g x %g", dim[0], dim[1]);
+      PassParams pp{};
+      camera_constants(cam, W, H, pp);
+      pp.width = W;
+      pp.height = H;
+      k_rt_camera_rays<<<B, T, 0, st>>>(pp, ptr<RRay>(k, 1), capn(1, sizeof(RRay)));
+      break;
+    }
+    case kRtSetupBsdf:
+      k_rt_setup_bsdf<<<B, T, 0, st>>>(ptr<RIsect>(k, 0), ptr<RRay>(k, 1), ptr<RBsdf>(k, 2), ptr<Material>(k, 3),
+                                       count_of<Material>(k, 3),
+                                       std::min({capn(0, sizeof(RIsect)), capn(1, sizeof(RRay)), capn(2, sizeof(RBsdf))}),
+                                       err);
+      break;
+    case kRtTexturePass:
+      k_rt_texture_pass<<<B, T, 0, st>>>(ptr<RBsdf>(k, 0), ptr<RIsect>(k, 1), ptr<RTex>(k, 2),
+                                         std::min({capn(0, sizeof(RBsdf)), capn(1, sizeof(RIsect)), capn(2, sizeof(RTex))}));
+      break;
+    case kRtTextureColor:
+      k_rt_texture_color<<<B, T, 0, st>>>(ptr<RBsdf>(k, 0), ptr<RTex>(k, 1),
+                                          std::min(capn(0, sizeof(RBsdf)), capn(1, sizeof(RTex))));
+      break;
+    case kRtFastShade:
+      k_rt_fast_shade<<<B, T, 0, st>>>(ptr<RIsect>(k, 0), ptr<RBsdf>(k, 1), ptr<int>(k, 2),
+                                       std::min({capn(0, sizeof(RIsect)), capn(1, sizeof(RBsdf)), capn(2, 4)}));
+      break;
+    case kRtBackground: {
+      if (int r = grid_of(5)) return r;
+      GridHdr h;
+      if (int r = read_host(ctx, &h, k->args[5], sizeof(h))) return r;
+      if (h.isPresent && (h.width <= 0 || h.height <= 0 || (size_t)h.width * h.height * 16 > k->args[4]->bytes))
+        return fail(MT_ERR_INVALID, "environment of %d x %d does not fit its buffer", h.width, h.height);
+      k_rt_background<<<B, T, 0, st>>>(ptr<RIsect>(k, 0), ptr<int>(k, 2), ptr<RRay>(k, 3), ptr<float4>(k, 4),
+                                       ptr<GridHdr>(k, 5),
+                                       std::min({capn(0, sizeof(RIsect)), capn(2, 4), capn(3, sizeof(RRay))}));
+      break;
+    }
+    case kRtGroup:
+      k_rt_group<<<B, T, 0, st>>>(ptr<RIsect>(k, 0), ptr<int>(k, 2), std::min(capn(0, sizeof(RIsect)), capn(2, 4)));
+      break;
+    case kFindBound:
+      if (k->args[6]->bytes < 24) return fail(MT_ERR_INVALID, "group bound buffer holds 6 floats");
+      k_find_bound<<<B, T, 0, st>>>(ptr<int>(k, 0), mesh_args(k, 1, 2, 3, 4, -1), ptr<int>(k, 5), ptr<float>(k, 6),
+                                    capn(4, sizeof(Face)), err);
+      break;
     default:
       return fail(MT_ERR_INVALID, "kernel id %d", k->id);
   }

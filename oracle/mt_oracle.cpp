@@ -1585,6 +1585,57 @@ int or_render_frame(const void* camera, int width, int height, int max_depth, in
                               0, 0, 0, nullptr, 0, 0);
 }
 
+// The preview device's frame (CDeviceRT.loop, src/cl/device/CDeviceRT.java:176-197,
+// kernels of Raytrace.cl): unjittered camera rays, closest hit, quick surface
+// colour (getQuickSurfaceColor, Material.cl:33-43: emission, or diffuse colour x
+// the cosine localDirFix.z) or the environment texel with gamma 2.2
+// (backgroundShade), packed as ARGB; group = the hit's material index, -1 on a
+// miss (updateGroupbufferShadeImage). A hit whose BSDF is invalid is shaded with
+// its material's parameters (the reference reads an unset parameter block; the
+// cosine below 1e-6 makes the colour black either way).
+void or_preview(const void* camera, int width, int height, const float* points, const float* uvs,
+                const float* normals, const int* faces, int nfaces, const float* materials, const int* nodes,
+                const float* bounds, const float* envmap, int ew, int eh, int env_present, int* argb, int* group) {
+  CameraF cam = *static_cast<const CameraF*>(camera);
+  cam.dimension[0] = (float)width;
+  cam.dimension[1] = (float)height;
+  Mesh m = mesh_of(points, uvs, normals, faces, nfaces);
+  const SurfaceParameter* mats = reinterpret_cast<const SurfaceParameter*>(materials);
+  auto pack = [](float r, float g, float b, float a) {
+    auto q = [](float v) { return (int)(std::fmin(std::fmax(v, 0.f), 1.f) * 255.0f); };
+    return (q(a) << 24) | (q(r) << 16) | (q(g) << 8) | q(b);
+  };
+  for (int id = 0; id < width * height; ++id) {
+    Ray<float> r;
+    camera_ray(cam, id, 0.5f, 0.5f, r);
+    int child = -1;
+    bool hit = intersect_mesh(r, &child, m, reinterpret_cast<const BVHNode*>(nodes),
+                              reinterpret_cast<const BoundingBox*>(bounds), false, nullptr);
+    if (hit) {
+      Isect<float> is;
+      hit_record(r, child, m, is);
+      Bsdf<float> b = setup_bsdf(r.d, is, mats);
+      const float coeff = b.localDirFix.z;
+      const SurfaceParameter* p = mats + is.mat;
+      V4<float> c;
+      if (is_emitter(p)) c = col<float>(p->emission_color);
+      else c = col<float>(p->diffuse_color) * coeff;
+      argb[id] = pack(c.x, c.y, c.z, 1.f);
+      group[id] = is.mat;
+    } else {
+      if (env_present) {
+        int idx = spherical_index(ew, eh, r.d);
+        const float* e = envmap + 4 * (size_t)idx;
+        const float ig = 1.f / 2.2f;
+        argb[id] = pack(std::pow(e[0], ig), std::pow(e[1], ig), std::pow(e[2], ig), e[3]);
+      } else {
+        argb[id] = pack(0.f, 0.f, 0.f, 1.f);
+      }
+      group[id] = -1;
+    }
+  }
+}
+
 // Grid-guided environment sample (illuminate_env_grid) and pdf/radiance
 // (radiance_env_grid) for one shading point, FP32. pdf_ref_out: the pdf the
 // reference's illuminateEnvironmentLight1 returns (pdfSS / (2 pi^2 sin), no

@@ -69,6 +69,7 @@ class Oracle:
         L.or_env_grid_radiance.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P]
         L.or_tonemap.argtypes = [P, I, F, F, F, P, P, P]
         L.or_tonemap_with_total.argtypes = [P, I, F, F, F, P, P, P, P]
+        L.or_preview.argtypes = [P, I, I, P, P, P, P, I, P, P, P, P, I, I, I, P, P]
 
 
 class RefOracle:
@@ -105,6 +106,7 @@ class RefOracle:
         L.ref_env_grid_illuminate.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P, P]
         L.ref_env_grid_radiance.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P]
         L.ref_average_accum.argtypes = [P, F, I, P, P, P]
+        L.ref_preview.argtypes = [P, I, I, P, P, P, P, I, P, P, P, P, I, I, I, P, P]
         L.ref_update_frame_image.argtypes = [P, P, F, I, I, F, F]
         L.ref_lightgrid_global_index.restype = I
         L.ref_lightgrid_global_index.argtypes = [I, I, I, I, I, I, I]

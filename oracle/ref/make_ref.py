@@ -2,9 +2,9 @@
 
 Test infrastructure only. Reads MambaTracer's kernel sources where they lie
 (/root/reference/src/cl/kernel), concatenates them in the order of
-src/cl/kernel/CSource.java:18-38, applies one mechanical rewrite (OpenCL vector
+src/cl/kernel/CSource.java:18-38, applies mechanical rewrites (OpenCL vector
 literals "(float4)(a, b, c, d)" become calls "clv_float4(a, b, c, d)", since C++
-parses the former as a cast of a comma expression), and compiles the result
+parses the former as a cast of a comma expression; the two below), and compiles the result
 together with oracle/ref/ref_harness.cpp through the shim oracle/ref/clshim.h.
 
 Everything it writes goes to oracle/_ref/ (git-ignored). When the reference tree
@@ -36,6 +36,11 @@ _VEC_LITERAL = re.compile(r"\((float|int)([234])\)\s*\(")
 # rewrite starts such a local with nu = nv = INT_MAX, the value under which the
 # reference's own bounds checks pass and the region covers the full map.
 _UNSET_REGION = re.compile(r"SATRegion region;(\s*\n\s*setRegion\(&region)")
+# "a.xyz = f(...).xyz;" (Raytrace.cl:170) assigns three lanes in OpenCL; the
+# shim's swizzle proxies would copy all four, so the right-hand side is
+# converted to a three-lane value first. Only operator-free right-hand sides
+# ending in .xyz match.
+_SWIZZLE_COPY = re.compile(r"\.xyz(\s*)=(\s*)([A-Za-z_][\w.\[\]]*(?:\([^;+*/]*\))?\.xyz)\s*;")
 
 
 def write_tu() -> str:
@@ -47,6 +52,7 @@ def write_tu() -> str:
         parts.append(f'#line 1 "{path}"\n')
         text = _VEC_LITERAL.sub(r"clv_\1\2(", text)
         text = _UNSET_REGION.sub(r"SATRegion region = clshim_unset_region();\1", text)
+        text = _SWIZZLE_COPY.sub(r".xyz\1=\2(float3)(\3);", text)
         parts.append(text)
         parts.append("\n")
     os.makedirs(OUT, exist_ok=True)

@@ -418,6 +418,36 @@ void ref_update_frame_image(float* framebuf, int* argb, float total_log, int tot
   run_serial(n, [&] { updateFrameImage((float4*)framebuf, argb, &tl, &tn, &len, &ex, &ga); });
 }
 
+// The preview device's frame (CDeviceRT.loop, src/cl/device/CDeviceRT.java:176-197):
+// InitCameraRayData, IntersectPrimitives, SetupBSDFRaytrace, backgroundShade,
+// fastShade, updateGroupbufferShadeImage (Raytrace.cl) without the texture pass.
+void ref_preview(const void* camera, int width, int height, const float* points, const float* uvs,
+                 const float* normals, const int* faces, int nfaces, const float* materials, const int* nodes,
+                 const float* bounds, const float* envmap, int ew, int eh, int env_present, int* argb, int* group) {
+  CameraStruct cam = *(const CameraStruct*)camera;
+  cam.dimension.x = (float)width;
+  cam.dimension.y = (float)height;
+  const int n = width * height;
+  std::vector<Ray> rays(n);
+  std::vector<Intersection> isects(n);
+  std::vector<Bsdf> bsdfs(n);
+  int count = n, size = nfaces;
+  LightGrid* lg = new_light_grid();
+  lg->isPresent = env_present != 0;
+  lg->width = ew;
+  lg->height = eh;
+  run_serial(n, [&] { InitCameraRayData(&cam, rays.data()); });
+  run_serial(n, [&] {
+    IntersectPrimitives(rays.data(), isects.data(), &count, (float4*)points, (float2*)uvs, (float4*)normals,
+                        (Face*)faces, &size, (BVHNode*)nodes, (BoundingBox*)bounds);
+  });
+  run_serial(n, [&] { SetupBSDFRaytrace(isects.data(), rays.data(), bsdfs.data(), (Material*)materials); });
+  run_serial(n, [&] { backgroundShade(isects.data(), &cam, argb, rays.data(), (float4*)envmap, lg); });
+  run_serial(n, [&] { fastShade(isects.data(), bsdfs.data(), argb); });
+  run_serial(n, [&] { updateGroupbufferShadeImage(isects.data(), &cam, group); });
+  std::free(lg);
+}
+
 // Light-grid per-cell SAT: prefixSumRowSubgrid then prefixSumColSubgrid
 // (LightGrid.cl:347-400), launched as CAdaptiveEnvironment.java:86-87 does.
 void ref_lightgrid_sat(const float* func, float* sat_out, int nu, int nv, int rx, int ry) {

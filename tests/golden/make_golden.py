@@ -209,6 +209,12 @@ def main():
         counts.append(c)
     out["frame_accum"] = acc
     out["frame_counts"] = np.stack(counts)
+    # the preview device's frame of the room (Raytrace.cl): ARGB and material group
+    pa = np.zeros(64 * 48, np.int32)
+    pg = np.zeros(64 * 48, np.int32)
+    ref.lib.ref_preview(ptr(cam), 64, 48, ptr(room.points), ptr(room.uvs), ptr(room.normals), ptr(room.faces),
+                        room.ntri, ptr(room.materials), ptr(rn), ptr(rb), ptr(z), 1, 1, 0, ptr(pa), ptr(pg))
+    out["preview_argb"], out["preview_group"] = pa, pg
     np.savez_compressed(OUT, **out)
     print(OUT, os.path.getsize(OUT), "bytes")
 

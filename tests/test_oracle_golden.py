@@ -209,3 +209,16 @@ def test_tonemap(orc, ginputs, golden):
     assert tot[1] == golden["tone_count"].sum()
     assert tot[0] == np.float32(loglw.astype(np.float64).sum())
     assert beq(argb, golden["tone_argb"])
+
+
+def test_preview_frame(orc, ginputs, golden):
+    """The preview device's frame (Raytrace.cl) of the room: ARGB and material group per pixel."""
+    from oracle.oracle import bvh_build
+    room = ginputs["room"]
+    rn, rb, _, _ = bvh_build(orc, room)
+    z = np.zeros(4, np.float32)
+    argb = np.zeros(64 * 48, np.int32)
+    group = np.zeros(64 * 48, np.int32)
+    orc.lib.or_preview(ptr(room.camera), 64, 48, ptr(room.points), ptr(room.uvs), ptr(room.normals), ptr(room.faces),
+                       room.ntri, ptr(room.materials), ptr(rn), ptr(rb), ptr(z), 1, 1, 0, ptr(argb), ptr(group))
+    assert beq(argb, golden["preview_argb"]) and beq(group, golden["preview_group"])

@@ -214,3 +214,27 @@ def test_tonemap_frame(orc, ref):
     ref.lib.ref_update_frame_image(ptr(fb), ptr(rargb), float(tot[0]), int(cnt.sum()), n, 0.18, 2.2)
     assert cnt.sum() > n // 2
     assert argb.tobytes() == rargb.tobytes()
+
+
+@pytest.mark.parametrize("which", ["room", "soup_env"])
+def test_preview_frame(orc, ref, which):
+    """The preview device's frame (Raytrace.cl): ARGB and material group per pixel."""
+    if which == "room":
+        sc, W, H, env = scenes.box_room(64, 48), 64, 48, None
+    else:
+        sc, W, H = scenes.soup(20000, seed=7, extent=0.8, edge_sigma=0.02), 64, 48
+        env = scenes.sky_env(256, 128)
+    nodes, bounds, _, _ = bvh_build(orc, sc)
+    envmap = env if env is not None else np.zeros((1, 4), np.float32)
+    ew, eh = (256, 128) if env is not None else (1, 1)
+    out = {}
+    for name, lib, fn in (("ref", ref.lib, "ref_preview"), ("or", orc.lib, "or_preview")):
+        argb = np.zeros(W * H, np.int32)
+        group = np.zeros(W * H, np.int32)
+        getattr(lib, fn)(ptr(sc.camera), W, H, ptr(sc.points), ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces), sc.ntri,
+                         ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(envmap), ew, eh, int(env is not None),
+                         ptr(argb), ptr(group))
+        out[name] = (argb, group)
+    assert out["ref"][1].tobytes() == out["or"][1].tobytes()
+    assert out["ref"][0].tobytes() == out["or"][0].tobytes()
+    assert (out["or"][1] >= 0).sum() > W * H // 4 and np.unique(out["or"][0]).size > 20
