@@ -6,9 +6,9 @@
 // other is deferred; leaves are single triangles tested with Moller-Trumbore
 // (Primitive.cl:3-29) and accepted when tMin < t < tMax (Util.cl:552-555).
 // The reference backtracks with a 64-bit bitstack and parent/sibling links; a
-// stack of deferred children in shared memory visits the same nodes in the same
-// order without re-reading parents. Identical order and identical arithmetic
-// give identical hit ids, including ties.
+// per-thread stack of deferred children (local memory) visits the same nodes in
+// the same order without re-reading parents. Identical order and identical
+// arithmetic give identical hit ids, including ties.
 #pragma once
 #include "mt_device.cuh"
 
@@ -76,40 +76,6 @@ __device__ __forceinline__ float tri_t(const RayT& r, float4 p1, float4 e1, floa
   return t;
 }
 
-struct NodeBoxes {
-  float lx0, lx1, ly0, ly1, lz0, lz1;
-  float rx0, rx1, ry0, ry1, rz0, rz1;
-  int left, right;
-};
-
-template <int TOP>
-__device__ __forceinline__ NodeBoxes load_node(const float4* __restrict__ nodes, const float4* smem_top, int rec) {
-  float4 n0, n1, n2, n3;
-  if (TOP > 0 && rec < TOP) {
-    n0 = smem_top[4 * rec + 0];
-    n1 = smem_top[4 * rec + 1];
-    n2 = smem_top[4 * rec + 2];
-    n3 = smem_top[4 * rec + 3];
-  } else {
-    const float4* p = nodes + 4 * (size_t)rec;
-    n0 = __ldg(p + 0);
-    n1 = __ldg(p + 1);
-    n2 = __ldg(p + 2);
-    n3 = __ldg(p + 3);
-  }
-  NodeBoxes b;
-  b.lx0 = n0.x; b.lx1 = n0.y; b.ly0 = n0.z; b.ly1 = n0.w;
-  b.rx0 = n1.x; b.rx1 = n1.y; b.ry0 = n1.z; b.ry1 = n1.w;
-  b.lz0 = n2.x; b.lz1 = n2.y; b.rz0 = n2.z; b.rz1 = n2.w;
-  b.left = __float_as_int(n3.x);
-  b.right = __float_as_int(n3.y);
-  return b;
-}
-
-struct TraceStats {
-  unsigned int interior, tris;
-};
-
 // Branch-free slab test for rays whose origin and 1/d are finite. With no
 // NaN possible, the reference's comparison chain (Util.cl:707-732) reduces to
 // max(near) <= min(far) on the three axes (near <= far holds per axis for a
@@ -136,9 +102,20 @@ __device__ __forceinline__ bool ray_is_finite(const RayT& r) {
 // reference would test no triangle under it. Deferred leaves are always tested.
 // Runs at most `steps` node visits or triangle tests; returns true when the
 // ray is finished (hit_face / r.tmax hold the result).
+// Deferred-node stack entries: (node, entry distance) for closest hits; the
+// node alone for any-hit rays, which never cull (their interval is fixed).
+template <bool ANY>
+struct StackEntry {
+  using type = int2;
+};
+template <>
+struct StackEntry<true> {
+  using type = int;
+};
+
 template <bool ANY>
 __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref, int& sp, int& hit_face, bool finite,
-                                           int2* stack, int steps, bool* overflow) {
+                                           typename StackEntry<ANY>::type* stack, int steps, bool* overflow) {
   const float4* __restrict__ nodes = S.nodes;
   const float4* __restrict__ tris = S.tris;
   for (int it = 0; it < steps; ++it) {
@@ -163,7 +140,10 @@ __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref,
           *overflow = true;
           return true;
         }
-        stack[sp++] = make_int2(rfirst ? left : right, __float_as_int(rfirst ? tl : trr));
+        if constexpr (ANY)
+          stack[sp++] = rfirst ? left : right;
+        else
+          stack[sp++] = make_int2(rfirst ? left : right, __float_as_int(rfirst ? tl : trr));
         ref = rfirst ? right : left;
         continue;
       }
@@ -179,12 +159,17 @@ __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref,
         r.tmax = t;
       }
     }
-    for (;;) {
+    if constexpr (ANY) {
       if (sp == 0) return true;
-      int2 e = stack[--sp];
-      if (ANY || !finite || e.x < 0 || __int_as_float(e.y) < r.tmax) {
-        ref = e.x;
-        break;
+      ref = stack[--sp];
+    } else {
+      for (;;) {
+        if (sp == 0) return true;
+        int2 e = stack[--sp];
+        if (!finite || e.x < 0 || __int_as_float(e.y) < r.tmax) {
+          ref = e.x;
+          break;
+        }
       }
     }
   }
@@ -199,7 +184,7 @@ template <bool ANY, int STEPS, class Src, class Dst>
 __device__ __forceinline__ void trace_persistent(const DevScene& S, int count, int* work, Src src, Dst dst,
                                                  bool* overflow) {
   const int lane = threadIdx.x & 31;
-  int2 stack[kStackDepth];
+  typename StackEntry<ANY>::type stack[kStackDepth];
   int i = -1;
   bool exhausted = false;
   RayT r;
@@ -235,57 +220,6 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, int count, i
   }
 }
 
-
-// Closest hit (ANY = false) or any hit (ANY = true). stack: this thread's
-// column of a [depth][threads] shared array. Returns the hit face id or -1; on
-// a closest hit r.tmax holds the hit distance. *overflow is set when the
-// deferred-node stack would exceed kStackDepth (the reference's bitstack limit).
-template <bool ANY, int TOP>
-__device__ __forceinline__ int traverse(const DevScene& S, const float4* smem_top, RayT& r, int* stack, int stride,
-                                        bool* overflow, TraceStats* st) {
-  int hit_face = -1;
-  int ref = S.root_ref;
-  int sp = 0;
-  const float4* __restrict__ nodes = S.nodes;
-  const float4* __restrict__ tris = S.tris;
-  for (;;) {
-    if (ref >= 0) {
-      NodeBoxes b = load_node<TOP>(nodes, smem_top, ref);
-      if (st) st->interior++;
-      float tl, trr;
-      bool hl = slab(r, b.lx0, b.lx1, b.ly0, b.ly1, b.lz0, b.lz1, &tl);
-      bool hr = slab(r, b.rx0, b.rx1, b.ry0, b.ry1, b.rz0, b.rz1, &trr);
-      if (hl && hr) {
-        int nearc = (trr < tl) ? b.right : b.left;
-        int farc = (trr < tl) ? b.left : b.right;
-        if (sp >= kStackDepth) {
-          *overflow = true;
-          return hit_face;
-        }
-        stack[sp * stride] = farc;
-        ++sp;
-        ref = nearc;
-        continue;
-      }
-      if (hl) { ref = b.left; continue; }
-      if (hr) { ref = b.right; continue; }
-    } else {
-      int slot = ~ref;
-      const float4* tp = tris + 3 * (size_t)slot;
-      float4 p1 = __ldg(tp + 0), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
-      if (st) st->tris++;
-      float t = tri_t(r, p1, e1, e2);
-      if ((r.tmin < t) && (t < r.tmax)) {
-        hit_face = __float_as_int(p1.w);
-        if (ANY) return hit_face;
-        r.tmax = t;
-      }
-    }
-    if (sp == 0) return hit_face;
-    --sp;
-    ref = stack[sp * stride];
-  }
-}
 
 }  // namespace tr
 }  // namespace mt
