@@ -35,6 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 W_DEFAULT, H_DEFAULT, DEPTH, RR = 1920, 1080, 8, 3
+ENV_ON = True  # the sky environment and its light grid (off for the box room)
 NTRI = 1_000_000
 ENV_W, ENV_H = 2048, 1024
 GRID = (1600, 1600, 16, 32)  # light grid: nu, nv, tiles per cell (reference defaults, CLightGrid.java)
@@ -46,6 +47,9 @@ WORKLOADS = {
     "soup": dict(name="soup1M_1920x1080_depth8_rr3_env2048x1024", spp=1,
                  scene="1,000,000-triangle soup, centroids U[-1,1]^3, edges N(0,0.005^2), GGX r U[0.05,0.8], "
                        "albedo U[0.2,0.9]"),
+    "room": dict(name="boxroom36_256x256_depth4", spp=1, width=256, height=256, depth=4, rr=0, env=False,
+                 scene="box room: 36 triangles (walls, two GGX boxes r 0.3, a 0.25 x 0.25 ceiling emitter of "
+                       "radiance 15), pinhole fov 40, no environment"),
     "stadium": dict(name="stadium3.3M_1920x1080_spp4_depth8_rr3_env2048x1024", spp=4,
                     scene="200x200 ground plane of 2,000,000 triangles + icosphere level 8 (1,310,720 triangles, "
                           "r 0.05) displaced by 3-octave value noise of amplitude 0.005; Lambert/GGX 50/50, "
@@ -56,6 +60,8 @@ WORKLOAD = WORKLOADS["soup"]["name"]
 
 def make_scene(kind, small, width, height):
     from mambatracer_gb300 import scenes
+    if kind == "room":
+        return scenes.box_room(width, height)
     if kind == "stadium":
         return scenes.stadium(quads=300 if small else 1000, level=6 if small else 8, width=width, height=height)
     return scenes.soup(200_000 if small else NTRI, seed=1, width=width, height=height)
@@ -70,9 +76,11 @@ def config_dict(kind, width, height, ntri, world, inflight=1, small=False):
     return {
         "workload": w["name"] if not small else f"{kind}{ntri}_{width}x{height}_depth{DEPTH}_rr{RR}_env{ENV_W}x{ENV_H}",
         "scene": w["scene"] if not small else f"{ntri}-triangle {kind} (reduced)",
-        "environment": f"{ENV_W}x{ENV_H} FP32 lat-long sky gradient + 0.5 deg Gaussian sun (peak 5e4); SAT built in FP64",
+        "environment": (f"{ENV_W}x{ENV_H} FP32 lat-long sky gradient + 0.5 deg Gaussian sun (peak 5e4); SAT built in FP64"
+                        if ENV_ON else "none (the ceiling emitter lights the room)"),
         "light_grid": (f"{GRID[0]}x{GRID[1]} grid of {GRID[2]}x{GRID[3]}-tile cells, FP64 per-cell SATs, updated from "
-                       f"environment hits after each of the first {GRID_UPDATES} warm-up frames, then fixed"),
+                       f"environment hits after each of the first {GRID_UPDATES} warm-up frames, then fixed"
+                       if ENV_ON else "none"),
         "resolution": f"{width}x{height}", "spp_per_step": w["spp"], "max_depth": DEPTH, "rr_from_bounce": RR,
         "rng": "per-pixel seed pixel ^ 0x9E3779B9 into the reference WangHash chain",
         "film": "FP32 Kahan-compensated", "launch": "CUDA graph per frame" + (f", {inflight} frames in flight on separate streams" if inflight > 1 else ""),
@@ -165,8 +173,8 @@ def cpu_render_rate(orc, sc, nodes, bounds, env, lum, sat, width, height, second
             orc.lib.or_render_frame_grid(ptr(cam), width, height, DEPTH, 1, RR, None, float(1 + tid + 1000 * f),
                                          ptr(sc.points), ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces), sc.ntri,
                                          ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(env), ptr(lum), ptr(sat),
-                                         ENV_W, ENV_H, 1, 0, ptr(acc), ptr(c), ptr(rc), ptr(gfunc), ptr(gsat), None,
-                                         *GRID, ptr(pos), 1, 0)
+                                         ENV_W, ENV_H, int(ENV_ON), 0, ptr(acc), ptr(c), ptr(rc), ptr(gfunc), ptr(gsat),
+                                         None, *GRID, ptr(pos), int(ENV_ON), 0)
             with lock:
                 total["rays"] += int(rc.sum())
                 total["frames"] += 1
@@ -230,7 +238,7 @@ def run_gpu(args):
     from mambatracer_gb300 import api, build, scenes
     build.build()
 
-    width, height = (640, 360) if args.small else (W_DEFAULT, H_DEFAULT)
+    width, height = (640, 360) if args.small and args.workload != "room" else (W_DEFAULT, H_DEFAULT)
     spp = WORKLOADS[args.workload]["spp"]
     sc = make_scene(args.workload, args.small, width, height)
     ntri = sc.ntri
@@ -238,8 +246,9 @@ def run_gpu(args):
     ctx = api.Context(local)
     S = api.Scene(ctx, sc)
     nodes, bounds = S.build_bvh()
-    S.set_env(env, ENV_W, ENV_H)
-    S.grid_config(*GRID, enable=2)  # grid-guided environment sampling, FP64 per-cell SATs
+    if ENV_ON:
+        S.set_env(env, ENV_W, ENV_H)
+        S.grid_config(*GRID, enable=2)  # grid-guided environment sampling, FP64 per-cell SATs
     job = api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, use_graph=1,
                   inflight=args.inflight, grid_updates=min(GRID_UPDATES, args.warmup), spp=spp)
     cam = sc.camera.copy()
@@ -638,6 +647,10 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="served: seconds of arrivals")
     args = ap.parse_args()
+    w = WORKLOADS.get(args.workload)
+    if w is not None and "depth" in w:  # a workload with its own frame, depth and lighting
+        global W_DEFAULT, H_DEFAULT, DEPTH, RR, ENV_ON
+        W_DEFAULT, H_DEFAULT, DEPTH, RR, ENV_ON = w["width"], w["height"], w["depth"], w["rr"], w["env"]
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
