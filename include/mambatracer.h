@@ -112,6 +112,15 @@ int mt_bvh_build(mt_scene* scene, int32_t* nodes_out, float* bounds_out, int* de
  * CNormalBVH fills its CMemory<CNode>/CMemory<CBound> (CNormalBVH.java:59-79). */
 int mt_bvh_build_host(const float* points, int npoints, const int32_t* faces, int nfaces, int32_t* nodes_out,
                       float* bounds_out, int* depth_out);
+/* The same tree (CNormalBVH.build's splits, node numbering and bounds) built on
+ * the GPU, level by level, straight into the traversal layout; nodes_out /
+ * bounds_out (may be NULL) receive the reference-layout arrays, equal to
+ * mt_bvh_build's. */
+int mt_bvh_build_device(mt_scene* scene, int32_t* nodes_out, float* bounds_out, int* depth_out);
+/* Copy of the scene's traversal layout: interior records (nrec x 64 B: the two
+ * child boxes and child refs) and triangle slots (N x 48 B), either pointer may
+ * be NULL; nrec_out / root_ref_out receive the record count and the root ref. */
+int mt_scene_layout_read(mt_scene* scene, void* records_out, void* tris_out, int* nrec_out, int* root_ref_out);
 /* Use a BVH built elsewhere (the Java builder's nodes/bounds buffers). */
 int mt_bvh_import(mt_scene* scene, const int32_t* nodes, const float* bounds, int nnodes);
 /* Traversal precision: 0 = FP32 child boxes (default), 1 = 8-bit child boxes

@@ -73,6 +73,7 @@ SIGNATURES = {
     "mt_scene_set_bvh_precision": (I, [P, I]),
     "mt_scene_set_materials": (I, [P, P, I]),
     "mt_scene_light_count": (I, [P]),
+    "mt_scene_layout_read": (I, [P, P, P, PI, PI]),
     "mt_scene_destroy": (I, [P]),
     "mt_env_set": (I, [P, P, I, I]),
     "mt_env_set_with_sat": (I, [P, P, P, P, I, I]),
@@ -89,6 +90,7 @@ SIGNATURES = {
     "mt_job_grid_read": (I, [P, P, P, P]),
     "mt_image_argb": (I, [P, P, F, F, P]),
     "mt_preview_frame": (I, [P, P, I, I, P, P]),
+    "mt_bvh_build_device": (I, [P, P, P, PI]),
     "mt_server_create": (I, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
     "mt_server_destroy": (I, [P]),
     "mt_job_submit": (I, [P, P, P, I, I, I, F, P, C.POINTER(C.c_int64)]),

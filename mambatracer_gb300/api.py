@@ -77,6 +77,26 @@ class Scene:
         self.depth = depth.value
         return nodes, bounds
 
+    def build_bvh_device(self, want_arrays: bool = True):
+        """The same tree built on the GPU (returns nodes, bounds in the reference layout)."""
+        n = self.src.ntri
+        nodes = np.zeros((2 * n - 1, 7), np.int32) if want_arrays else None
+        bounds = np.zeros((2 * n - 1, 8), np.float32) if want_arrays else None
+        depth = C.c_int()
+        check(lib().mt_bvh_build_device(self.h, _p(nodes), _p(bounds), C.byref(depth)))
+        self.depth = depth.value
+        return nodes, bounds
+
+    def layout(self):
+        """The traversal layout on the device: (records (nrec, 16) float32,
+        tris (N, 12) float32, root ref)."""
+        nrec, root = C.c_int(), C.c_int()
+        check(lib().mt_scene_layout_read(self.h, None, None, C.byref(nrec), C.byref(root)))
+        recs = np.zeros((max(nrec.value, 0), 16), np.float32)
+        tris = np.zeros((self.src.ntri, 12), np.float32)
+        check(lib().mt_scene_layout_read(self.h, _p(recs) if nrec.value else None, _p(tris), None, None))
+        return recs, tris, root.value
+
     def import_bvh(self, nodes: np.ndarray, bounds: np.ndarray):
         nodes = np.ascontiguousarray(nodes, np.int32)
         bounds = np.ascontiguousarray(bounds, np.float32)

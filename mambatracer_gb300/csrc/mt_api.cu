@@ -590,6 +590,20 @@ extern "C" int mt_bvh_build_host(const float* points, int npoints, const int32_t
   return MT_OK;
 }
 
+extern "C" int mt_scene_layout_read(mt_scene* s, void* records_out, void* tris_out, int* nrec_out,
+                                    int* root_ref_out) {
+  if (!s) return fail(MT_ERR_INVALID, "NULL scene");
+  if (!s->has_bvh) return fail(MT_ERR_INVALID, "scene has no BVH");
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  CU(cudaStreamSynchronize(s->ctx->stream));
+  if (records_out && s->nrec) CU(cudaMemcpy(records_out, s->d_nodes, 64 * (size_t)s->nrec, cudaMemcpyDeviceToHost));
+  if (tris_out) CU(cudaMemcpy(tris_out, s->d_tris, 48 * (size_t)s->ntri, cudaMemcpyDeviceToHost));
+  if (nrec_out) *nrec_out = s->nrec;
+  if (root_ref_out) *root_ref_out = s->root_ref;
+  return MT_OK;
+}
+
 extern "C" int mt_bvh_import(mt_scene* s, const int32_t* nodes, const float* bounds, int nnodes) {
   if (!s || !nodes || !bounds) return fail(MT_ERR_INVALID, "NULL argument");
   std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
