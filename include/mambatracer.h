@@ -129,6 +129,13 @@ int mt_scene_set_bvh_precision(mt_scene* scene, int precision);
 /* Replace the material table (TracerAPI material edits, src/cl/ui/fx/main/TracerAPI.java:371). */
 int mt_scene_set_materials(mt_scene* scene, const void* materials, int nmaterials);
 int mt_scene_light_count(const mt_scene* scene);
+/* Bind a material's texture image (the images CTextureApplyPass.process reads
+ * on the host, src/cl/algorithms/CTextureApplyPass.java:37-92): kind 0 diffuse,
+ * 1 glossy, 2 roughness, 3 mirror (kept, never applied, as in the reference);
+ * argb: width*height ints in JavaFX PixelReader.getArgb order (row-major,
+ * 0xAARRGGBB); NULL removes the image. Materials flag their textures
+ * (isDiffuseTexture, ...); renders sample them on the device at the hit's uv. */
+int mt_scene_set_texture(mt_scene* scene, int material, int kind, const int32_t* argb, int width, int height);
 int mt_scene_destroy(mt_scene* scene);
 
 /* ------------------------------------------------ environment light */

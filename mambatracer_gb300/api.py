@@ -66,6 +66,17 @@ class Scene:
         self.h = h
         self.depth = None
         self.grid = (1600, 1600, 16, 32, 0)
+        for m, kind, img in getattr(sc, "textures", ()):
+            self.set_texture(m, kind, img)
+
+    def set_texture(self, material: int, kind: int, argb: np.ndarray | None):
+        """Bind a material's texture image (kind 0 diffuse, 1 glossy, 2 roughness,
+        3 mirror; ARGB int32 [H, W]); None removes it."""
+        if argb is None:
+            check(lib().mt_scene_set_texture(self.h, material, kind, None, 0, 0))
+            return
+        a = np.ascontiguousarray(argb).view(np.int32)
+        check(lib().mt_scene_set_texture(self.h, material, kind, _p(a), a.shape[1], a.shape[0]))
 
     def build_bvh(self):
         """CNormalBVH.build on the host (returns nodes, bounds in the reference layout)."""

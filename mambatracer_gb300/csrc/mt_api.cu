@@ -259,6 +259,34 @@ void free_scene(mt_scene* s) {
   dfree(s->d_env_lum);
   dfree(s->d_env_sat);
   dfree(s->d_env_sat64);
+  dfree(s->d_texels);
+  dfree(s->d_tex_ref);
+}
+
+// Texel pool (all images back to back) and the per-material table of
+// (first texel, width, height, 0) for diffuse, glossy, roughness and mirror.
+int upload_textures(mt_scene* s) {
+  s->h_tex.resize(4 * (size_t)s->nmat);
+  size_t total = 0;
+  for (const auto& t : s->h_tex) total += t.argb.size();
+  if (total > 0x7FFFFFFFu) return fail(MT_ERR_INVALID, "textures hold %zu texels (at most 2^31 - 1)", total);
+  dfree(s->d_texels);
+  dfree(s->d_tex_ref);
+  s->tex_on = 0;
+  if (total == 0) return MT_OK;
+  std::vector<int32_t> pool;
+  pool.reserve(total);
+  std::vector<int4> ref(s->h_tex.size());
+  for (size_t i = 0; i < s->h_tex.size(); ++i) {
+    const auto& t = s->h_tex[i];
+    ref[i] = make_int4(t.argb.empty() ? 0 : (int)pool.size(), t.argb.empty() ? 0 : t.w, t.argb.empty() ? 0 : t.h, 0);
+    pool.insert(pool.end(), t.argb.begin(), t.argb.end());
+  }
+  int r = upload(&s->d_texels, pool.data(), pool.size());
+  if (!r) r = upload(&s->d_tex_ref, ref.data(), ref.size());
+  if (r) return r;
+  s->tex_on = 1;
+  return MT_OK;
 }
 
 }  // namespace
@@ -324,7 +352,32 @@ extern "C" int mt_scene_set_materials(mt_scene* s, const void* materials, int nm
   s->nmat = nmaterials;
   int r = upload(&s->d_materials, materials, (size_t)nmaterials);
   if (!r) r = upload_lights(s);
+  if (!r) r = upload_textures(s);
   return r;
+}
+
+extern "C" int mt_scene_set_texture(mt_scene* s, int material, int kind, const int32_t* argb, int width,
+                                    int height) {
+  if (!s) return fail(MT_ERR_INVALID, "NULL scene");
+  if (material < 0 || material >= s->nmat) return fail(MT_ERR_INVALID, "material %d of %d", material, s->nmat);
+  if (kind < 0 || kind > 3) return fail(MT_ERR_INVALID, "texture kind %d (0 diffuse, 1 glossy, 2 roughness, 3 mirror)", kind);
+  if (argb && (width <= 0 || height <= 0 || (long long)width * height > 0x7FFFFFFFll))
+    return fail(MT_ERR_INVALID, "texture of %d x %d", width, height);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  int q = quiesce(s->ctx);
+  if (q) return q;
+  ++s->version;
+  s->h_tex.resize(4 * (size_t)s->nmat);
+  auto& t = s->h_tex[4 * (size_t)material + kind];
+  if (argb) {
+    t.argb.assign(argb, argb + (size_t)width * height);
+    t.w = width;
+    t.h = height;
+  } else {
+    t = mt_scene::HostTex{};
+  }
+  return upload_textures(s);
 }
 
 extern "C" int mt_scene_light_count(const mt_scene* s) { return s ? s->nlights : -1; }

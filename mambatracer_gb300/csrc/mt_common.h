@@ -59,6 +59,11 @@ struct DevScene {
   const Material* materials;
   const int* light_faces;
   int nlights;
+  // textures: ARGB texel pool and, per material, 4 entries (diffuse, glossy,
+  // roughness, mirror) of (first texel, width, height, 0); width 0 = no image
+  const int* texels;
+  const int4* tex_ref;
+  int tex_on;
 };
 
 struct DevEnv {

@@ -229,6 +229,59 @@ __device__ __forceinline__ Bsdf setup_bsdf(const DevScene& S, V d, V n, int mat)
   }
   return b;
 }
+// ------------------------------------------------------------- textures
+// Java's float -> int cast: NaN -> 0, saturating at the int range.
+__device__ __forceinline__ int java_f2i(float x) {
+  if (x != x) return 0;
+  if (x >= 2147483648.f) return 0x7FFFFFFF;
+  if (x <= -2147483648.f) return (int)0x80000000;
+  return (int)x;
+}
+// TextureInfoCache.getDomainValue (TextureInfoCache.java:131-136)
+__device__ __forceinline__ float tex_domain(float x) {
+  return x < 0.f ? (x - (float)java_f2i(x)) + 1.f : x - (float)java_f2i(x);
+}
+// CTextureApplyPass.process (CTextureApplyPass.java:37-92): the texel at
+// ((int)(u' (W - 1)), (int)(v' (H - 1))) of a W x H ARGB image; the index is
+// clamped to the image (Java's PixelReader throws beyond it, which only
+// infinite or |uv| >= 2^31 coordinates reach).
+__device__ __forceinline__ int tex_fetch(const int* __restrict__ texels, int4 ref, float u, float v) {
+  const float dx = tex_domain(u) * ((float)ref.y - 1.f);
+  const float dy = tex_domain(v) * ((float)ref.z - 1.f);
+  const int x = min(max(java_f2i(dx), 0), ref.y - 1), y = min(max(java_f2i(dy), 0), ref.z - 1);
+  return __ldg(texels + ref.x + (long long)y * ref.y + x);
+}
+// getFloat4ARGB (Util.cl:482-493)
+__device__ __forceinline__ float4 argb_float4(int c) {
+  return make_float4(((c >> 16) & 0xFF) / 255.0f, ((c >> 8) & 0xFF) / 255.0f, (c & 0xFF) / 255.0f,
+                     ((c >> 24) & 0xFF) / 255.0f);
+}
+__device__ __forceinline__ bool has_textures(const Material& M) {
+  return M.isDiffuseTexture || M.isGlossyTexture || M.isRoughnessTexture;
+}
+// texturePassGI + CTextureApplyPass.process + updateToTextureColorGI
+// (Render.cl:127-231): a path's copy of its material takes the texel colours at
+// the hit's uv (diffuse and glossy colour; roughness from red and green). A
+// flagged texture without an image reads ARGB 0. The component probabilities
+// stay those of the untextured material, as SetupBSDFPath computed them first.
+__device__ __forceinline__ void apply_textures(const DevScene& S, int mat, float u, float v, Material& m) {
+  const int4* r = S.tex_ref + 4 * (size_t)mat;
+  if (m.isDiffuseTexture) {
+    const int4 t = __ldg(r + 0);
+    m.diffuse_color = argb_float4(t.y > 0 ? tex_fetch(S.texels, t, u, v) : 0);
+  }
+  if (m.isGlossyTexture) {
+    const int4 t = __ldg(r + 1);
+    m.glossy_color = argb_float4(t.y > 0 ? tex_fetch(S.texels, t, u, v) : 0);
+  }
+  if (m.isRoughnessTexture) {
+    const int4 t = __ldg(r + 2);
+    const float4 c = argb_float4(t.y > 0 ? tex_fetch(S.texels, t, u, v) : 0);
+    m.glossy_param.y = fmaxf(0.001f, c.x);
+    m.glossy_param.z = fmaxf(0.001f, c.y);
+  }
+}
+
 // Bsdf.cl:162-166
 __device__ __forceinline__ bool is_emitter(const Material& M) {
   V c = muls(M.emission_color, M.emission_param.x);

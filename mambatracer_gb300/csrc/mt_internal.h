@@ -98,6 +98,15 @@ struct mt_scene {
   double* d_env_sat64 = nullptr;
   int env_w = 0, env_h = 0, env_present = 0;
   int grid_nu = 1600, grid_nv = 1600, grid_rx = 16, grid_ry = 32, grid_on = 0;  // grid_on: 0, 1 FP32, 2 FP64 SAT
+  // textures: host images per (material, kind), the device pool and table
+  struct HostTex {
+    std::vector<int32_t> argb;
+    int w = 0, h = 0;
+  };
+  std::vector<HostTex> h_tex;  // 4 per material: diffuse, glossy, roughness, mirror
+  int* d_texels = nullptr;
+  int4* d_tex_ref = nullptr;
+  int tex_on = 0;
   unsigned version = 0;  // bumped when device arrays or the grid configuration change
   std::atomic<int> refs{0};  // served requests queued or running on this scene
 
@@ -117,6 +126,9 @@ struct mt_scene {
     s.materials = d_materials;
     s.light_faces = d_light_faces;
     s.nlights = nlights;
+    s.texels = d_texels;
+    s.tex_ref = d_tex_ref;
+    s.tex_on = tex_on;
     return s;
   }
   DevEnv env_view() const {

@@ -167,7 +167,8 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_shadow(DevScene S
 // mode 1 (benchmark semantics): samples are keyed on the pixel, Russian
 // roulette runs after the BSDF sample, and the survivors and shadow rays are
 // compacted together afterwards.
-template <int MODE, int MINB>
+// TEX: the scene has textures (a separate instance keeps the untextured one lean).
+template <int MODE, int MINB, bool TEX = false>
 __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEnv E, const PassParams* __restrict__ pp,
                                                          Ctrl* ctrl, int b, FrameBufs fb,
                                                          unsigned long long* status) {
@@ -260,6 +261,12 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEn
   V sho = zero4(), shd = zero4(), shc = zero4();
   V ndir = zero4();
   if (alive) {
+    Material tm;  // the path's textured copy of its material
+    if (TEX && has_textures(*B.pm)) {
+      tm = *B.pm;
+      apply_textures(S, B.mat, H.u, H.v, tm);
+      B.pm = &tm;
+    }
     int32_t lx, ly, bx, by;
     int gid;
     if (MODE == 0) {
@@ -467,7 +474,11 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
     if (ev) cudaEventRecord(ev[e++], st);
     unsigned long long* stb = status + (size_t)(b - 1) * status_stride;
     const int sm = shade_minb();
-    if (mode == 0)
+    if (S.tex_on && mode == 0)
+      k_shade<0, 3, true><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+    else if (S.tex_on)
+      k_shade<1, 4, true><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+    else if (mode == 0)
       k_shade<0, 3><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
     else if (sm == 4)
       k_shade<1, 4><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);

@@ -502,10 +502,34 @@ __global__ void k_texture_pass(const RPath* paths, int npaths, const RIsect* ise
   }
 }
 
-// getFloat4ARGB (Util.cl:482-493)
-__device__ __forceinline__ float4 argb_f4(int c) {
-  return make_float4(((c >> 16) & 0xFF) / 255.0f, ((c >> 8) & 0xFF) / 255.0f, (c & 0xFF) / 255.0f,
-                     ((c >> 24) & 0xFF) / 255.0f);
+// CTextureApplyPass.process (CTextureApplyPass.java:37-92) on the device, in
+// place of the reference's per-bounce copy of TextureData to the host and back:
+// below the count, each flagged texture (w > 0) of the slot's material
+// (parameters.x) with an image gets its ARGB texel in z; without an image z is
+// left as it was, as the host pass leaves it. tex_ref: 4 int4 per material
+// (first texel, width, height, 0) for diffuse, glossy, roughness, mirror.
+__global__ void k_texture_apply(RTex* tex, const int* count, const int* __restrict__ texels, long long ntexels,
+                                const int4* __restrict__ tex_ref, int nref, int cap, int* err) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= min(*count, cap)) return;
+  RTex& t = tex[id];
+  const int mat = t.parameters.x;
+  int4* kinds[3] = {&t.diffuse, &t.glossy, &t.roughness};
+  for (int k = 0; k < 3; ++k) {
+    int4& e = *kinds[k];
+    if (e.w <= 0) continue;
+    if (mat < 0 || 4 * (long long)mat + k >= nref) {
+      latch(err, kErrIndex);
+      return;
+    }
+    const int4 r = tex_ref[4 * mat + k];
+    if (r.y <= 0 || r.z <= 0) continue;
+    if (r.x < 0 || (long long)r.x + (long long)r.y * r.z > ntexels) {
+      latch(err, kErrIndex);
+      return;
+    }
+    e.z = tex_fetch(texels, r, __int_as_float(e.x), __int_as_float(e.y));
+  }
 }
 
 // updateToTextureColorGI (Render.cl:189-231)
@@ -520,10 +544,10 @@ __global__ void k_texture_color(RPath* paths, int npaths, const RTex* tex, const
   }
   Material& P = paths[pix].bsdf.param;
   const RTex& t = tex[id];
-  if (t.diffuse.w) P.diffuse_color = argb_f4(t.diffuse.z);
-  if (t.glossy.w) P.glossy_color = argb_f4(t.glossy.z);
+  if (t.diffuse.w) P.diffuse_color = argb_float4(t.diffuse.z);
+  if (t.glossy.w) P.glossy_color = argb_float4(t.glossy.z);
   if (t.roughness.w) {
-    const float4 c = argb_f4(t.roughness.z);
+    const float4 c = argb_float4(t.roughness.z);
     P.glossy_param.y = fmaxf(0.001f, c.x);
     P.glossy_param.z = fmaxf(0.001f, c.y);
   }
@@ -912,10 +936,10 @@ __global__ void k_rt_texture_color(RBsdf* bsdfs, const RTex* tex, int cap) {
   if (id >= cap) return;
   Material& P = bsdfs[id].param;
   const RTex& t = tex[id];
-  if (t.diffuse.w) P.diffuse_color = argb_f4(t.diffuse.z);
-  if (t.glossy.w) P.glossy_color = argb_f4(t.glossy.z);
+  if (t.diffuse.w) P.diffuse_color = argb_float4(t.diffuse.z);
+  if (t.glossy.w) P.glossy_color = argb_float4(t.glossy.z);
   if (t.roughness.w) {
-    const float4 c = argb_f4(t.roughness.z);
+    const float4 c = argb_float4(t.roughness.z);
     P.glossy_param.y = c.x;
     P.glossy_param.z = c.y;
   }
@@ -1001,6 +1025,7 @@ enum KernelId {
   kIdentifyLights, kPrepareLights,
   kGridRowScan, kGridColScan, kGridInit, kGridInitFuncSat, kGridCalcFunc,
   kRtCameraRays, kRtSetupBsdf, kRtTexturePass, kRtTextureColor, kRtFastShade, kRtBackground, kRtGroup, kFindBound,
+  kTextureApply,
   kNumKernels
 };
 
@@ -1023,6 +1048,7 @@ const Spec kSpecs[kNumKernels] = {
     {"calculateFunc", 1},
     {"InitCameraRayData", 2}, {"SetupBSDFRaytrace", 4}, {"textureInitPassRT", 3}, {"updateToTextureColorRT", 2},
     {"fastShade", 3}, {"backgroundShade", 6}, {"updateGroupbufferShadeImage", 3}, {"findBound", 7},
+    {"textureApplyPass", 4},
 };
 
 std::string names_list() {
@@ -1229,6 +1255,13 @@ extern "C" int mt_launch_1d(mt_kernel* k, size_t global, size_t local) {
       const int cap = std::min({capn(1, sizeof(RIsect)), capn(2, sizeof(RTex)), capn(3, 4)});
       k_texture_pass<<<B, T, 0, st>>>(ptr<RPath>(k, 0), count_of<RPath>(k, 0), ptr<RIsect>(k, 1), ptr<RTex>(k, 2),
                                       ptr<int>(k, 3), ptr<int>(k, 4), cap, err);
+      break;
+    }
+    case kTextureApply: {
+      if (k->args[1]->bytes < 4) return fail(MT_ERR_INVALID, "count buffer too small");
+      long long ntexels = (long long)(k->args[2]->bytes / 4);
+      k_texture_apply<<<B, T, 0, st>>>(ptr<RTex>(k, 0), ptr<int>(k, 1), ptr<int>(k, 2), ntexels, ptr<int4>(k, 3),
+                                       count_of<int4>(k, 3), capn(0, sizeof(RTex)), err);
       break;
     }
     case kTextureColor: {

@@ -5,7 +5,9 @@ mt_launch_1d) the way its Java host classes do: the buffers of CDeviceGI.createB
 (src/cl/device/CDeviceGI.java:130-164), the frame loop of CDeviceGI.loop (:214-271),
 CCompact.execute (src/cl/algorithms/CCompact.java:79-89), the light list of
 CLightConfiguration.initLights (src/cl/algorithms/CLightConfiguration.java:43-87) with
-PrefixSumInteger (src/cl/algorithms/PrefixSumInteger.java), and CImage.processImage
+PrefixSumInteger (src/cl/algorithms/PrefixSumInteger.java), the texture pass with
+CTextureApplyPass.process's texel lookup as a device kernel (textureApplyPass) in place
+of its copy to the host and back, and CImage.processImage
 (src/cl/image/CImage.java:124-136) with PrefixSumFloat. Every buffer has the
 reference's layout; every launch is one reference kernel. It is the plain wavefront
 that a host keeping its own loop gets from the library, and the comparison point for
@@ -18,6 +20,7 @@ import ctypes as C
 import numpy as np
 
 from ._lib import check, lib
+from .scenes import texture_tables
 
 LOCAL = 100          # CDeviceGI.localWorkSize
 SCAN_LOCAL = 128     # PrefixSumInteger / PrefixSumFloat LOCALSIZE
@@ -176,6 +179,11 @@ class PlainDeviceGI:
         self.paths = Buf(ctx, 304 * N)
         self.isects = Buf(ctx, 96 * N)
         self.tex = Buf(ctx, 80 * N)
+        # the material images CTextureApplyPass.process reads on the host, as a
+        # texel pool and a per-material table for the device lookup
+        texels, table = texture_tables(sc)
+        self.texels = Buf(ctx, host=texels)
+        self.tex_ref = Buf(ctx, host=table)
         # CImage
         self.frame_count = float_buf(ctx, 1.0)
         self.accum = Buf(ctx, 16 * N)
@@ -216,6 +224,7 @@ class PlainDeviceGI:
                           self.accum, self.pixels, self.count, self.state, self.materials, *mesh, self.nodes,
                           self.bounds, *envb)
         self.k_texpass = k("texturePassGI", self.paths, self.isects, self.tex, self.pixels, self.count)
+        self.k_texapply = k("textureApplyPass", self.tex, self.count, self.texels, self.tex_ref)
         self.k_texcolor = k("updateToTextureColorGI", self.paths, self.tex, self.pixels, self.count)
         # CImage.createKernels
         self.k_init_accum = k("InitFloat4DataXYZ", self.accum, self.frame_size)
@@ -281,6 +290,7 @@ class PlainDeviceGI:
             if record_counts:
                 counts.append(self.count.int())
             self.k_texpass.run(G, LOCAL)
+            self.k_texapply.run(G, LOCAL)  # CTextureApplyPass.process, on the device
             self.k_texcolor.run(G, LOCAL)
             self._state(*next(s), frame_count)
             self.k_direct.run(G, LOCAL)

@@ -6,6 +6,7 @@ points float4 (w = 0), uvs float2, normals float4, faces 10 x int32 with
 generators are seeded so every run sees the same scene.
 
   box_room      the box room (36 triangles, 256 x 256, depth 4)
+  textured_room the box room with texture images on the floor, a wall and the boxes
   soup          uniform triangle soup (1M triangles) in [-1, 1]^3
   stadium       ground plane of 2M triangles plus a displaced icosphere
   sky_env       zenith-to-horizon gradient plus a Gaussian sun, lat-long FP32 RGB
@@ -35,6 +36,9 @@ class Scene:
     normals: np.ndarray = field(default_factory=lambda: np.zeros((1, 4), np.float32))
     camera: np.ndarray | None = None
     name: str = ""
+    # texture images: (material, kind 0 diffuse / 1 glossy / 2 roughness / 3 mirror,
+    # ARGB int32 [H, W] in PixelReader.getArgb order)
+    textures: list = field(default_factory=list)
 
     @property
     def ntri(self) -> int:
@@ -134,6 +138,73 @@ def box_room(width=256, height=256) -> Scene:
     cam = make_camera((0.5, 0.5, 2.35), (0.5, 0.5, 0.0), (0.0, 1.0, 0.0), 40.0, width, height)
     return Scene(points=_points(pts), faces=_faces(idx, np.array(mats)), materials=materials,
                  camera=cam, name="box_room")
+
+
+def _argb(r, g, b, a=None) -> np.ndarray:
+    """float channels in [0, 1] -> 0xAARRGGBB int32 (8 bits each, rounded)."""
+    q = lambda c: np.clip(np.rint(np.asarray(c, np.float64) * 255.0), 0, 255).astype(np.uint32)
+    a = np.ones_like(np.asarray(r, np.float64)) if a is None else a
+    return ((q(a) << 24) | (q(r) << 16) | (q(g) << 8) | q(b)).astype(np.uint32).view(np.int32)
+
+
+def textured_room(width=128, height=96, seed=3) -> Scene:
+    """The box room with texture images (CTextureApplyPass's inputs): the floor
+    (material 5) a 64 x 64 diffuse checkerboard tiled three times (uvs 0..3); the
+    red left wall a 40 x 24 diffuse stripe image read at negative uvs (-1.3..0.7,
+    wrapped by the reference's domain rule); the boxes (no uvs: the hit's
+    barycentric coordinates index the images) a 32 x 16 glossy colour ramp and a
+    16 x 16 roughness noise image (red = ax, green = ay)."""
+    sc = box_room(width, height)
+    faces = sc.faces.copy()
+    n = faces.shape[0]
+    uvs = np.zeros((3 * n, 2), np.float32)
+    # floor: triangles 0, 1 (points (0,0,0),(0,0,1),(1,0,1) and (0,0,0),(1,0,1),(1,0,0)); uv = 3 * (x, z)
+    # left wall: triangles 6, 7 (x = 0); uv = 2 * (z, y) - (1.3, 1.3)
+    for t in range(n):
+        p = sc.points[[faces["vx"][t], faces["vy"][t], faces["vz"][t]], :3]
+        if t in (0, 1):
+            uvs[3 * t:3 * t + 3] = 3.0 * p[:, [0, 2]]
+        elif t in (6, 7):
+            uvs[3 * t:3 * t + 3] = 2.0 * p[:, [2, 1]] - 1.3
+        else:
+            continue
+        faces["uvx"][t], faces["uvy"][t], faces["uvz"][t] = 3 * t, 3 * t + 1, 3 * t + 2
+    mats = faces["mat"].copy()
+    mats[0:2] = 5
+    faces["mat"] = mats
+    materials = np.concatenate([sc.materials, sc.materials[:1].copy()])
+    materials[5]["isDiffuseTexture"] = 1
+    materials[1]["isDiffuseTexture"] = 1
+    materials[3]["isGlossyTexture"] = 1
+    materials[3]["isRoughnessTexture"] = 1
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:64, 0:64]
+    chk = ((xx // 8 + yy // 8) % 2).astype(np.float64)
+    floor = _argb(0.15 + 0.7 * chk, 0.15 + 0.6 * chk, 0.2 + 0.5 * (1 - chk))
+    yy, xx = np.mgrid[0:24, 0:40]
+    stripe = ((xx // 5) % 2).astype(np.float64)
+    wall = _argb(0.8 * stripe + 0.1, 0.1 + 0.2 * yy / 23.0, 0.1 + 0.1 * stripe)
+    yy, xx = np.mgrid[0:16, 0:32]
+    ramp = _argb(0.02 + 0.5 * xx / 31.0, 0.04 + 0.3 * yy / 15.0, np.full(xx.shape, 0.3))
+    rough = _argb(rng.uniform(0.02, 0.9, (16, 16)), rng.uniform(0.02, 0.9, (16, 16)), np.zeros((16, 16)))
+    return Scene(points=sc.points, faces=faces, materials=materials, uvs=uvs, camera=sc.camera,
+                 name="textured_room", textures=[(5, 0, floor), (1, 0, wall), (3, 1, ramp), (3, 2, rough)])
+
+
+def texture_tables(sc: Scene) -> tuple[np.ndarray, np.ndarray]:
+    """The scene's images as one ARGB texel pool and the per-material table of
+    (first texel, width, height, 0) for kinds 0..3 (width 0: no image), int32
+    [M * 4, 4] -- the layout of the textureApplyPass kernel's arguments."""
+    nmat = sc.materials.shape[0]
+    table = np.zeros((nmat * 4, 4), np.int32)
+    pool, off = [], 0
+    for m, kind, img in sc.textures:
+        img = np.ascontiguousarray(img, np.int32)
+        table[4 * m + kind] = (off, img.shape[1], img.shape[0], 0)
+        pool.append(img.reshape(-1))
+        off += img.size
+    texels = np.concatenate(pool) if pool else np.zeros(1, np.int32)
+    return texels, table
 
 
 def _palette_materials(levels=64, glossy_fraction=1.0):

@@ -910,12 +910,72 @@ inline void stage_seed(int bounce, int stage, int32_t* sx, int32_t* sy) {
 }
 inline int32_t pixel_gid(int pixel) { return (int32_t)((uint32_t)pixel ^ 0x9E3779B9u); }
 
+// ------------------------------------------------------------ textures
+// Textures bound for the next frames (test infrastructure state): an ARGB texel
+// pool and, per material, 4 entries (first texel, width, height, 0) for
+// diffuse, glossy, roughness, mirror; width 0 = no image.
+struct Textures {
+  const int* texels = nullptr;
+  const int* ref = nullptr;
+  int nref = 0;  // entries (4 ints each)
+};
+Textures g_tex;
+
+// Java's (int) cast of a float (JLS 5.1.3): NaN -> 0, saturating.
+inline int java_f2i(float x) {
+  if (x != x) return 0;
+  if (x >= 2147483648.0f) return 2147483647;
+  if (x <= -2147483648.0f) return -2147483647 - 1;
+  return (int)x;
+}
+// TextureInfoCache.getDomainValue (TextureInfoCache.java:131-136)
+inline float domain_value(float x) { return x < 0 ? (x - (float)java_f2i(x)) + 1.0f : x - (float)java_f2i(x); }
+// CTextureApplyPass.process (CTextureApplyPass.java:47-87): the ARGB texel at
+// ((int)(u' (W - 1)), (int)(v' (H - 1))), the index clamped to the image.
+inline int texel_at(const Textures& T, int entry, float u, float v) {
+  const int* r = T.ref + 4 * (size_t)entry;
+  float dx = domain_value(u) * ((float)r[1] - 1.0f);
+  float dy = domain_value(v) * ((float)r[2] - 1.0f);
+  int x = std::min(std::max(java_f2i(dx), 0), r[1] - 1);
+  int y = std::min(std::max(java_f2i(dy), 0), r[2] - 1);
+  return T.texels[r[0] + (size_t)y * r[1] + x];
+}
+// getFloat4ARGB (Util.cl:482-493)
+inline void argb_to_float4(int c, float* out) {
+  out[3] = ((c >> 24) & 0xFF) / 255.0f;
+  out[0] = ((c >> 16) & 0xFF) / 255.0f;
+  out[1] = ((c >> 8) & 0xFF) / 255.0f;
+  out[2] = (c & 0xFF) / 255.0f;
+}
+// texturePassGI, CTextureApplyPass.process and updateToTextureColorGI
+// (Render.cl:127-231): the flagged textures of material `mat` at uv replace the
+// diffuse colour, the glossy colour, and the roughness (glossy_param.y/z from red
+// and green, at least 0.001). A flagged texture without an image reads ARGB 0.
+inline void apply_textures(const Textures& T, int mat, float u, float v, SurfaceParameter& p) {
+  auto argb = [&](int kind) {
+    int e = 4 * mat + kind;
+    return (e < T.nref && T.ref[4 * (size_t)e + 1] > 0) ? texel_at(T, e, u, v) : 0;
+  };
+  if (p.isDiffuseTexture) argb_to_float4(argb(0), p.diffuse_color);
+  if (p.isGlossyTexture) argb_to_float4(argb(1), p.glossy_color);
+  if (p.isRoughnessTexture) {
+    float c[4];
+    argb_to_float4(argb(2), c);
+    p.glossy_param[1] = std::fmax(0.001f, c[0]);
+    p.glossy_param[2] = std::fmax(0.001f, c[1]);
+  }
+}
+inline bool has_textures(const SurfaceParameter& p) {
+  return p.isDiffuseTexture || p.isGlossyTexture || p.isRoughnessTexture;
+}
+
 template <class R>
 struct Path {
   V4<R> throughput, hitpoint;
   int lastSpecular;
   R lastPdfW;
   Bsdf<R> bsdf;
+  SurfaceParameter textured;  // the path's textured copy of its material
 };
 
 struct Scene {
@@ -1036,6 +1096,17 @@ void render_frame(const Scene& S, const Env<R>& E, const CameraF& cam_in, const 
     for (int j = kept; j < N; ++j) { init_isect(isects[j]); pixels[j] = 0; }
     count = kept;
     if (counts_out) counts_out[b - 1] = count;
+
+    // texture pass (CDeviceGI.java:241-244) over the live queue
+    if (g_tex.nref > 0) {
+      for (int j = 0; j < count; ++j) {
+        Path<R>& pa = paths[pixels[j]];
+        if (!pa.bsdf.param || !has_textures(*pa.bsdf.param)) continue;
+        pa.textured = *pa.bsdf.param;
+        apply_textures(g_tex, pa.bsdf.materialID, (float)isects[j].uv[0], (float)isects[j].uv[1], pa.textured);
+        pa.bsdf.param = &pa.textured;
+      }
+    }
 
     // DirectLight (Render.cl:377-466)
     int32_t lx = 0, ly = 0, bx = 0, by = 0;
@@ -1571,6 +1642,23 @@ int or_render_frame_grid(const void* camera, int width, int height, int max_dept
   }
   if (ray_counts) { ray_counts[0] = rc.primary; ray_counts[1] = rc.extension; ray_counts[2] = rc.shadow; }
   return S.nlights;
+}
+
+// Textures for the frames that follow (NULL / 0 entries: none).
+void or_set_textures(const int* texels, const int* tex_ref, int nentries) {
+  g_tex.texels = texels;
+  g_tex.ref = tex_ref;
+  g_tex.nref = texels && tex_ref ? nentries : 0;
+}
+
+// The texture pass on one material at one uv (material: 144 B in, out).
+void or_texture_apply(const float* material, int mat, float u, float v, const int* texels, const int* tex_ref,
+                      int nentries, float* material_out) {
+  SurfaceParameter p;
+  std::memcpy(&p, material, sizeof(p));
+  Textures T{texels, tex_ref, nentries};
+  apply_textures(T, mat, u, v, p);
+  std::memcpy(material_out, &p, sizeof(p));
 }
 
 int or_render_frame(const void* camera, int width, int height, int max_depth, int mode, int rr_depth,

@@ -70,6 +70,8 @@ class Oracle:
         L.or_tonemap.argtypes = [P, I, F, F, F, P, P, P]
         L.or_tonemap_with_total.argtypes = [P, I, F, F, F, P, P, P, P]
         L.or_preview.argtypes = [P, I, I, P, P, P, P, I, P, P, P, P, I, I, I, P, P]
+        L.or_set_textures.argtypes = [P, P, I]
+        L.or_texture_apply.argtypes = [P, I, F, F, P, P, I, P]
 
 
 class RefOracle:
@@ -107,6 +109,8 @@ class RefOracle:
         L.ref_env_grid_radiance.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P]
         L.ref_average_accum.argtypes = [P, F, I, P, P, P]
         L.ref_preview.argtypes = [P, I, I, P, P, P, P, I, P, P, P, P, I, I, I, P, P]
+        L.ref_set_textures.argtypes = [P, P, I]
+        L.ref_texture_apply.argtypes = [P, I, F, F, P, P, I, P]
         L.ref_update_frame_image.argtypes = [P, P, F, I, I, F, F]
         L.ref_lightgrid_global_index.restype = I
         L.ref_lightgrid_global_index.argtypes = [I, I, I, I, I, I, I]

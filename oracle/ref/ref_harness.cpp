@@ -9,7 +9,9 @@
 // work-group's items as fibers that yield at every barrier.
 #include <ucontext.h>
 
+#include <algorithm>
 #include <cstdlib>
+#include <cstring>
 #include <functional>
 #include <type_traits>
 #include <vector>
@@ -116,6 +118,52 @@ LightGrid* new_light_grid() {
   g->subgridRangeX = 16;
   g->subgridRangeY = 32;
   return g;
+}
+
+// Texture images for ref_render_frame: an ARGB texel pool and 4 entries per
+// material (first texel, width, height, 0) for diffuse, glossy, roughness,
+// mirror; width 0 = no image.
+struct RefTextures {
+  const int* texels = nullptr;
+  const int* ref = nullptr;
+  int nref = 0;
+};
+RefTextures g_ref_tex;
+
+// Java's (int) cast of a float: NaN -> 0, saturating at the int range.
+int jcast(float x) {
+  if (x != x) return 0;
+  if (x >= 2147483648.0f) return 2147483647;
+  if (x <= -2147483648.0f) return -2147483647 - 1;
+  return (int)x;
+}
+
+// CTextureApplyPass.process (src/cl/algorithms/CTextureApplyPass.java:37-92),
+// the Java host pass between texturePassGI and updateToTextureColorGI, with
+// TextureInfoCache.getDomainValue (TextureInfoCache.java:131-136). The texel
+// index is clamped to the image where Java's PixelReader would throw.
+void texture_apply_process(TextureData* tex, int count, const RefTextures& T) {
+  auto dom = [](float x) { return x < 0 ? x - (float)jcast(x) + 1 : x - (float)jcast(x); };
+  for (int index = 0; index < count; ++index) {
+    TextureData& t = tex[index];
+    int4* kinds[3] = {&t.diffuseTexture, &t.glossyTexture, &t.roughnessTexture};
+    for (int k = 0; k < 3; ++k) {
+      if (!(kinds[k]->w > 0)) continue;
+      const int entry = 4 * t.parameters.x + k;
+      if (t.parameters.x < 0 || entry >= T.nref) continue;
+      const int* r = T.ref + 4 * (size_t)entry;
+      if (r[1] <= 0) continue;  // image == null
+      float x, y;
+      std::memcpy(&x, &kinds[k]->x, 4);
+      std::memcpy(&y, &kinds[k]->y, 4);
+      x = dom(x);
+      y = dom(y);
+      float dx = (float)x * ((float)r[1] - 1);
+      float dy = (float)y * ((float)r[2] - 1);
+      int ix = std::min(std::max(jcast(dx), 0), r[1] - 1), iy = std::min(std::max(jcast(dy), 0), r[2] - 1);
+      kinds[k]->z = T.texels[r[0] + (size_t)iy * r[1] + ix];
+    }
+  }
 }
 
 }  // namespace
@@ -539,10 +587,42 @@ int ref_bsdf_eval(const float* material, const float* n, const float* ng, const 
   return 1;
 }
 
-// One progressive GI frame, restating CDeviceGI.loop (CDeviceGI.java:214-271)
-// without the texture pass (untextured scenes): raygen and path/queue init, then
-// `max_depth` bounces of IntersectPrimitives, SetupBSDFPath, LightHitPass,
-// CCompact.execute (CCompact.java:79-89), DirectLight, SampleBSDFRayDirection.
+// Textures for ref_render_frame (NULL / 0 entries: none, and the texture pass
+// is skipped).
+void ref_set_textures(const int* texels, const int* tex_ref, int nentries) {
+  g_ref_tex.texels = texels;
+  g_ref_tex.ref = tex_ref;
+  g_ref_tex.nref = texels && tex_ref ? nentries : 0;
+}
+
+// The texture pass on one path: a Path whose Bsdf holds `material` (144 B) and
+// material id `mat`, an Intersection with uv (u, v), through texturePassGI,
+// CTextureApplyPass.process and updateToTextureColorGI; the Bsdf's parameters
+// after the pass go to material_out.
+void ref_texture_apply(const float* material, int mat, float u, float v, const int* texels, const int* tex_ref,
+                       int nentries, float* material_out) {
+  Path path;
+  Intersection isect;
+  TextureData tex;
+  std::memset(&path, 0, sizeof(path));
+  std::memset(&isect, 0, sizeof(isect));
+  std::memset(&tex, 0, sizeof(tex));
+  std::memcpy(&path.bsdf.param, material, sizeof(SurfaceParameter));
+  path.bsdf.materialID = mat;
+  isect.uv.x = u;
+  isect.uv.y = v;
+  int pixel = 0, count = 1;
+  RefTextures T{texels, tex_ref, nentries};
+  run_serial(1, [&] { texturePassGI(&path, &isect, &tex, &pixel, &count); });
+  texture_apply_process(&tex, count, T);
+  run_serial(1, [&] { updateToTextureColorGI(&path, &tex, &pixel, &count); });
+  std::memcpy(material_out, &path.bsdf.param, sizeof(SurfaceParameter));
+}
+
+// One progressive GI frame, restating CDeviceGI.loop (CDeviceGI.java:214-271):
+// raygen and path/queue init, then `max_depth` bounces of IntersectPrimitives,
+// SetupBSDFPath, LightHitPass, CCompact.execute (CCompact.java:79-89), the
+// texture pass (when textures are set), DirectLight, SampleBSDFRayDirection.
 // seeds: the State seed pair of each allocateState() call in launch order
 // (1 + 2*max_depth pairs). Film accumulates into accum (float4 per pixel).
 // counts_out[b] = live queue length after bounce b's compaction.
@@ -561,6 +641,8 @@ int ref_render_frame(const void* camera, int width, int height, int max_depth, c
   std::vector<Intersection> isects(N), tmp_isects(N);
   std::vector<Path> paths(N);
   std::vector<int> pixels(N), tmp_pixels(N);
+  std::vector<TextureData> texd(N);
+  std::memset(texd.data(), 0, sizeof(TextureData) * (size_t)N);
   int length = N, count = N, size = nfaces;
 
   // lights (CDeviceGI.initLight, CDeviceGI.java:293-306)
@@ -620,6 +702,12 @@ int ref_render_frame(const void* camera, int width, int height, int max_depth, c
     run_serial(N, [&] { TransferIntersection(isects.data(), tmp_isects.data(), &length); });
     run_serial(N, [&] { TransferPixels(pixels.data(), tmp_pixels.data(), &length); });
     if (counts_out) counts_out[pathLength - 1] = count;
+    // texture pass (CDeviceGI.java:241-244)
+    if (g_ref_tex.nref > 0) {
+      run_serial(N, [&] { texturePassGI(paths.data(), isects.data(), texd.data(), pixels.data(), &count); });
+      texture_apply_process(texd.data(), count, g_ref_tex);
+      run_serial(N, [&] { updateToTextureColorGI(paths.data(), texd.data(), pixels.data(), &count); });
+    }
     // directLightEvaluation (CDeviceGI.java:273-277)
     allocate_state();
     run_serial(N, [&] {

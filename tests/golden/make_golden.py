@@ -52,7 +52,28 @@ def golden_inputs():
     film = (rng.exponential(1.0, size=(64 * 48, 4)) * rng.choice([0.0, 0.3, 3.0, 40.0], size=(64 * 48, 1)))
     film[:, 3] = 7.0
     g["tone_film"] = film.astype(np.float32)
+    # texture pass: the textured room's images, materials with random texture
+    # flags, uvs in and beyond [0, 1] plus the special values
+    g["tex_room"] = scenes.textured_room(40, 32)
+    n = 600
+    u = rng.uniform(-3, 3, n).astype(np.float32)
+    v = rng.uniform(-3, 3, n).astype(np.float32)
+    special = np.array([0, 1, -1, 2, -2, 0.5, -0.5, 1e-9, -1e-9, 0.99999994, -0.99999994, 3e9, -3e9,
+                        np.nan, np.inf, -np.inf], np.float32)
+    u[:special.size] = special
+    v[:special.size] = special[::-1]
+    g["tex_u"], g["tex_v"] = u, v
+    g["tex_mat"] = rng.integers(0, g["tex_room"].materials.shape[0], n).astype(np.int32)
+    g["tex_flags"] = rng.integers(0, 2, (n, 3)).astype(np.int32)
+    g["tex_seeds"] = rng.integers(2 ** 29, 2 ** 30, size=2 * (1 + 2 * 6)).astype(np.int32)
     return g
+
+
+def texture_material(g, i):
+    """Golden texture case i: its material (one MATERIAL record) with the case's flags."""
+    m = g["tex_room"].materials[g["tex_mat"][i]:g["tex_mat"][i] + 1].copy()
+    m["isDiffuseTexture"], m["isGlossyTexture"], m["isRoughnessTexture"] = g["tex_flags"][i]
+    return m
 
 
 GRID_CAM = np.array([0.1, 0.2, 2.5, 0.0], np.float32)
@@ -215,6 +236,25 @@ def main():
     ref.lib.ref_preview(ptr(cam), 64, 48, ptr(room.points), ptr(room.uvs), ptr(room.normals), ptr(room.faces),
                         room.ntri, ptr(room.materials), ptr(rn), ptr(rb), ptr(z), 1, 1, 0, ptr(pa), ptr(pg))
     out["preview_argb"], out["preview_group"] = pa, pg
+    # the texture pass (texturePassGI, CTextureApplyPass.process, updateToTextureColorGI)
+    tr = g["tex_room"]
+    texels, table = scenes.texture_tables(tr)
+    mo = np.zeros((len(g["tex_u"]), 36), np.float32)
+    for i in range(len(g["tex_u"])):
+        m = texture_material(g, i)
+        ref.lib.ref_texture_apply(ptr(m), int(g["tex_mat"][i]), float(g["tex_u"][i]), float(g["tex_v"][i]),
+                                  ptr(texels), ptr(table), table.shape[0], ptr(mo[i]))
+    out["tex_material_out"] = mo
+    # a textured room frame, depth 6
+    tn, tb, _, _ = bvh_build(orc, tr)
+    tacc = np.zeros((40 * 32, 4), np.float32)
+    tc = np.zeros(6, np.int32)
+    ref.lib.ref_set_textures(ptr(texels), ptr(table), table.shape[0])
+    ref.lib.ref_render_frame(ptr(tr.camera), 40, 32, 6, ptr(g["tex_seeds"]), 1.0, ptr(tr.points), ptr(tr.uvs),
+                             ptr(tr.normals), ptr(tr.faces), tr.ntri, ptr(tr.materials), ptr(tn), ptr(tb), ptr(z),
+                             ptr(z), ptr(z), 1, 1, 0, ptr(tacc), ptr(tc))
+    ref.lib.ref_set_textures(None, None, 0)
+    out["tex_frame_accum"], out["tex_frame_counts"] = tacc, tc
     np.savez_compressed(OUT, **out)
     print(OUT, os.path.getsize(OUT), "bytes")
 

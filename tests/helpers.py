@@ -60,13 +60,29 @@ def oracle_frames(orc, sc, nodes, bounds, W, H, depth, mode, rr, seeds_list, env
         acc = np.zeros((W * H, 4), np.float64 if fp64 else np.float32)
     cam = sc.camera.copy()
     counts, rays = [], np.zeros(3, np.int64)
+    textures = getattr(sc, "textures", None)
+    if textures:
+        from mambatracer_gb300 import scenes
+        texels, table = scenes.texture_tables(sc)
+        orc.lib.or_set_textures(ptr(texels), ptr(table), table.shape[0])
+    try:
+        _frames(orc, sc, nodes, bounds, W, H, depth, mode, rr, seeds_list, env is not None, fp64, acc, first_frame,
+                grid, cam, envmap, lum, sat, ew, eh, counts, rays)
+    finally:
+        if textures:
+            orc.lib.or_set_textures(None, None, 0)
+    return acc, np.stack(counts), rays
+
+
+def _frames(orc, sc, nodes, bounds, W, H, depth, mode, rr, seeds_list, has_env, fp64, acc, first_frame, grid, cam,
+            envmap, lum, sat, ew, eh, counts, rays):
     for f, seeds in enumerate(seeds_list):
         c = np.zeros(depth, np.int32)
         rc = np.zeros(3, np.int64)
         s = None if seeds is None else np.ascontiguousarray(seeds, np.int32)
         args = [ptr(cam), W, H, depth, mode, rr, ptr(s), float(first_frame + f), ptr(sc.points), ptr(sc.uvs),
                 ptr(sc.normals), ptr(sc.faces), sc.ntri, ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(envmap),
-                ptr(lum), ptr(sat), ew, eh, int(env is not None), int(fp64), ptr(acc), ptr(c), ptr(rc)]
+                ptr(lum), ptr(sat), ew, eh, int(has_env), int(fp64), ptr(acc), ptr(c), ptr(rc)]
         if grid is None:
             orc.lib.or_render_frame(*args)
         else:
@@ -76,7 +92,6 @@ def oracle_frames(orc, sc, nodes, bounds, W, H, depth, mode, rr, seeds_list, env
                                          grid["nv"], grid["rx"], grid["ry"], ptr(pos), 1, int(gacc is not None))
         counts.append(c)
         rays += rc
-    return acc, np.stack(counts), rays
 
 
 def rel_rmse(a, b):

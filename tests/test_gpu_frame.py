@@ -41,10 +41,12 @@ def seeds_for(depth, frames, seed=5):
     return [rng.integers(2 ** 29, 2 ** 30, size=2 * (1 + 2 * depth)).astype(np.int32) for _ in range(frames)]
 
 
-@pytest.mark.parametrize("which", ["room", "soup_env", "stadium_env"])
+@pytest.mark.parametrize("which", ["room", "tex_room", "soup_env", "stadium_env"])
 def test_reference_mode(ctx, orc, which):
     if which == "room":
         sc, W, H, depth, env = scenes.box_room(128, 96), 128, 96, 4, None
+    elif which == "tex_room":  # texture images sampled on the device (CTextureApplyPass's lookup)
+        sc, W, H, depth, env = scenes.textured_room(128, 96), 128, 96, 6, None
     elif which == "stadium_env":
         sc = scenes.stadium(quads=60, level=4, width=96, height=64)
         W, H, depth, env = 96, 64, 6, (scenes.sky_env(512, 256), 512, 256)
@@ -87,6 +89,35 @@ def test_benchmark_mode(ctx, orc):
         rays, counts = J.stats()
         assert np.abs(rays - orays).max() <= 0.005 * orays.max()
     assert rel_rmse(J.film(), acc) < 1e-4
+    J.close()
+    S.close()
+
+
+def test_textured_benchmark_mode(ctx, orc):
+    sc = scenes.textured_room(96, 64)
+    S, nodes, bounds = setup(ctx, orc, sc)
+    W, H, depth = 96, 64, 8
+    J = api.Job(ctx, S, W, H, max_depth=depth, mode=1, rr_depth=3, film_kahan=0)
+    J.set_camera(sc.camera)
+    acc = None
+    for f in range(2):
+        J.render(None, float(f + 1))
+        acc, oc, orays = oracle_frames(orc, sc, nodes, bounds, W, H, depth, 1, 3, [None], acc=acc,
+                                       first_frame=f + 1)
+        rays, counts = J.stats()
+        assert np.abs(rays - orays).max() <= 0.005 * orays.max()
+    assert rel_rmse(J.film(), acc) < 1e-4
+    # without the images the film differs (the textures are applied)
+    S2 = api.Scene(ctx, scenes.Scene(points=sc.points, faces=sc.faces, materials=sc.materials, uvs=sc.uvs,
+                                     camera=sc.camera))
+    S2.import_bvh(nodes, bounds)
+    J2 = api.Job(ctx, S2, W, H, max_depth=depth, mode=1, rr_depth=3, film_kahan=0)
+    J2.set_camera(sc.camera)
+    J2.render(None, 1.0)
+    J2.render(None, 2.0)
+    assert rel_rmse(J2.film(), acc) > 1e-2
+    J2.close()
+    S2.close()
     J.close()
     S.close()
 

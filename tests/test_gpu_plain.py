@@ -24,10 +24,12 @@ def seeds_for(depth, frames, seed=9):
     return [rng.integers(2 ** 29, 2 ** 30, size=2 * (1 + 2 * depth)).astype(np.int32) for _ in range(frames)]
 
 
-@pytest.mark.parametrize("which", ["room", "soup_env"])
+@pytest.mark.parametrize("which", ["room", "tex_room", "soup_env"])
 def test_plain_loop_matches_oracle_and_fused_path(ctx, orc, which):
     if which == "room":
         sc, W, H, depth, env = scenes.box_room(64, 48), 64, 48, 4, None
+    elif which == "tex_room":  # texturePassGI, textureApplyPass (the device lookup), updateToTextureColorGI
+        sc, W, H, depth, env = scenes.textured_room(64, 48), 64, 48, 6, None
     else:
         sc = scenes.soup(30000, seed=5, extent=0.8, edge_sigma=0.015)
         W, H, depth, env = 48, 40, 5, (scenes.sky_env(256, 128), 256, 128)
@@ -59,13 +61,13 @@ def test_plain_loop_matches_oracle_and_fused_path(ctx, orc, which):
         J.render(s, float(f + 1))
         _, jc = J.stats()
         assert counts == jc.tolist(), (counts, jc)
-        if which == "room":
+        if which != "soup_env":
             assert counts == oc[0].tolist(), (counts, oc[0])
         else:
             assert np.abs(np.array(counts) - oc[0]).max() <= max(1, 0.01 * oc[0].max()), (counts, oc[0])
     ctx.finish()
     film = dev.film()
-    assert rel_rmse(film, acc) < (1e-5 if which == "room" else 1e-3)
+    assert rel_rmse(film, acc) < (1e-3 if which == "soup_env" else 1e-5)
     assert film[:, :3].tobytes() == J.film()[:, :3].tobytes()
     # CImage.processImage through averageAccum, the reference's scans and updateFrameImage
     argb = dev.process_image(2.0)

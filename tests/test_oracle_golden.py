@@ -7,7 +7,7 @@ the restatement must reproduce them bit for bit.
 import numpy as np
 import pytest
 
-from mambatracer_gb300 import layout
+from mambatracer_gb300 import layout, scenes
 from tests.golden.make_golden import bsdf_material, unit
 from tests.helpers import bvh_build, ptr
 
@@ -222,3 +222,39 @@ def test_preview_frame(orc, ginputs, golden):
     orc.lib.or_preview(ptr(room.camera), 64, 48, ptr(room.points), ptr(room.uvs), ptr(room.normals), ptr(room.faces),
                        room.ntri, ptr(room.materials), ptr(rn), ptr(rb), ptr(z), 1, 1, 0, ptr(argb), ptr(group))
     assert beq(argb, golden["preview_argb"]) and beq(group, golden["preview_group"])
+
+
+def test_texture_pass(orc, ginputs, golden):
+    """texturePassGI + CTextureApplyPass.process + updateToTextureColorGI
+    (Render.cl:127-231) on 600 flagged materials and uvs (tiled, negative, NaN,
+    infinite): the material after the pass."""
+    from tests.golden.make_golden import texture_material
+    tr = ginputs["tex_room"]
+    texels, table = scenes.texture_tables(tr)
+    out = np.zeros_like(golden["tex_material_out"])
+    for i in range(out.shape[0]):
+        m = texture_material(ginputs, i)
+        orc.lib.or_texture_apply(ptr(m), int(ginputs["tex_mat"][i]), float(ginputs["tex_u"][i]),
+                                 float(ginputs["tex_v"][i]), ptr(texels), ptr(table), table.shape[0], ptr(out[i]))
+    assert beq(out, golden["tex_material_out"])
+
+
+def test_textured_frame(orc, ginputs, golden):
+    """A depth-6 frame of the textured room (CDeviceGI.loop with its texture pass):
+    film and queue lengths."""
+    from oracle.oracle import bvh_build
+    tr = ginputs["tex_room"]
+    texels, table = scenes.texture_tables(tr)
+    tn, tb, _, _ = bvh_build(orc, tr)
+    z = np.zeros(4, np.float32)
+    acc = np.zeros((40 * 32, 4), np.float32)
+    c = np.zeros(6, np.int32)
+    orc.lib.or_set_textures(ptr(texels), ptr(table), table.shape[0])
+    try:
+        orc.lib.or_render_frame(ptr(tr.camera), 40, 32, 6, 0, 0, ptr(ginputs["tex_seeds"]), 1.0, ptr(tr.points),
+                                ptr(tr.uvs), ptr(tr.normals), ptr(tr.faces), tr.ntri, ptr(tr.materials), ptr(tn),
+                                ptr(tb), ptr(z), ptr(z), ptr(z), 1, 1, 0, 0, ptr(acc), ptr(c), None)
+    finally:
+        orc.lib.or_set_textures(None, None, 0)
+    assert beq(c, golden["tex_frame_counts"])
+    assert beq(acc, golden["tex_frame_accum"])

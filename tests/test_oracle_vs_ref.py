@@ -238,3 +238,74 @@ def test_preview_frame(orc, ref, which):
     assert out["ref"][1].tobytes() == out["or"][1].tobytes()
     assert out["ref"][0].tobytes() == out["or"][0].tobytes()
     assert (out["or"][1] >= 0).sum() > W * H // 4 and np.unique(out["or"][0]).size > 20
+
+
+def _texture_cases(seed, n):
+    """Materials with random texture flags and uvs: in [0, 1], tiled, negative,
+    integers, tiny negatives, NaN and infinities."""
+    rng = np.random.default_rng(seed)
+    sc = scenes.textured_room()
+    texels, table = scenes.texture_tables(sc)
+    u = rng.uniform(-3, 3, n).astype(np.float32)
+    v = rng.uniform(-3, 3, n).astype(np.float32)
+    special = np.array([0, 1, -1, 2, -2, 0.5, -0.5, 1e-9, -1e-9, 0.99999994, -0.99999994, 3e9, -3e9,
+                        np.nan, np.inf, -np.inf], np.float32)
+    u[:special.size] = special
+    v[:special.size] = special[::-1]
+    mats = rng.integers(0, sc.materials.shape[0], n)
+    flags = rng.integers(0, 2, (n, 3))
+    return sc, texels, table, u, v, mats, flags
+
+
+@pytest.mark.parametrize("seed", [51, 52])
+def test_texture_pass(orc, ref, seed):
+    """texturePassGI + CTextureApplyPass.process + updateToTextureColorGI
+    (Render.cl:127-231) on one path: the oracle's material after the pass equals
+    the reference kernels' byte for byte."""
+    sc, texels, table, u, v, mats, flags = _texture_cases(seed, 4000)
+    for i in range(len(u)):
+        m = sc.materials[mats[i]:mats[i] + 1].copy()
+        m["isDiffuseTexture"], m["isGlossyTexture"], m["isRoughnessTexture"] = flags[i]
+        a = np.zeros(36, np.float32)
+        b = np.zeros(36, np.float32)
+        ref.lib.ref_texture_apply(ptr(m), int(mats[i]), float(u[i]), float(v[i]), ptr(texels), ptr(table),
+                                  table.shape[0], ptr(a))
+        orc.lib.or_texture_apply(ptr(m), int(mats[i]), float(u[i]), float(v[i]), ptr(texels), ptr(table),
+                                 table.shape[0], ptr(b))
+        assert a.tobytes() == b.tobytes(), (i, u[i], v[i], flags[i])
+
+
+@pytest.mark.parametrize("depth", [4, 8])
+def test_textured_frame(orc, ref, depth):
+    """CDeviceGI.loop with the texture pass on the textured box room: film and
+    queue lengths bit-identical."""
+    sc = scenes.textured_room(40, 32)
+    nodes, bounds, _, _ = bvh_build(orc, sc)
+    texels, table = scenes.texture_tables(sc)
+    rng = np.random.default_rng(depth + 7)
+    seeds = rng.integers(2 ** 29, 2 ** 30, size=2 * (1 + 2 * depth)).astype(np.int32)
+    cam = sc.camera.copy()
+    acc_a = np.zeros((40 * 32, 4), np.float32)
+    acc_b = acc_a.copy()
+    acc_c = acc_a.copy()
+    z = np.zeros(4, np.float32)
+    ca, cb = np.zeros(depth, np.int32), np.zeros(depth, np.int32)
+    ref.lib.ref_set_textures(ptr(texels), ptr(table), table.shape[0])
+    orc.lib.or_set_textures(ptr(texels), ptr(table), table.shape[0])
+    try:
+        ref.lib.ref_render_frame(ptr(cam), 40, 32, depth, ptr(seeds), 1.0, ptr(sc.points), ptr(sc.uvs),
+                                 ptr(sc.normals), ptr(sc.faces), sc.ntri, ptr(sc.materials), ptr(nodes), ptr(bounds),
+                                 ptr(z), ptr(z), ptr(z), 1, 1, 0, ptr(acc_a), ptr(ca))
+        orc.lib.or_render_frame(ptr(cam), 40, 32, depth, 0, 0, ptr(seeds), 1.0, ptr(sc.points), ptr(sc.uvs),
+                                ptr(sc.normals), ptr(sc.faces), sc.ntri, ptr(sc.materials), ptr(nodes), ptr(bounds),
+                                ptr(z), ptr(z), ptr(z), 1, 1, 0, 0, ptr(acc_b), ptr(cb), None)
+    finally:
+        ref.lib.ref_set_textures(None, None, 0)
+        orc.lib.or_set_textures(None, None, 0)
+    assert np.array_equal(ca, cb)
+    assert acc_a.tobytes() == acc_b.tobytes()
+    # the textures change the image
+    orc.lib.or_render_frame(ptr(cam), 40, 32, depth, 0, 0, ptr(seeds), 1.0, ptr(sc.points), ptr(sc.uvs),
+                            ptr(sc.normals), ptr(sc.faces), sc.ntri, ptr(sc.materials), ptr(nodes), ptr(bounds),
+                            ptr(z), ptr(z), ptr(z), 1, 1, 0, 0, ptr(acc_c), None, None)
+    assert (np.abs(acc_c - acc_b).max(axis=1) > 1e-3).sum() > 100
