@@ -204,11 +204,12 @@ def cpu_scene(orc, kind):
     return sc, nodes, bounds, env, lum, sat
 
 
-def algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_count, threads):
+def algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_count, threads, rec_bytes=64):
     """Per-launch algorithmic bytes of the primary-ray closest-hit launch:
-    sum over rays of 32 (ray in) + 16 (hit out) + 64 per interior visit + 48 per
-    triangle test, the visit counts taken from the FP32 oracle traversal of the
-    same rays (benchmark-semantics raygen of this frame)."""
+    sum over rays of 32 (ray in) + 16 (hit out) + rec_bytes per interior visit
+    (64 for FP32 records, 32 for FP16 ones) + 48 per triangle test, the visit
+    counts taken from the FP32 oracle traversal of the same rays
+    (benchmark-semantics raygen of this frame)."""
     from mambatracer_gb300 import layout
     from oracle.oracle import ptr
     n = width * height
@@ -231,7 +232,7 @@ def algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_count, t
     with cf.ThreadPoolExecutor(threads) as ex:
         list(ex.map(work, [c for c in chunks if len(c)]))
     v_int, tri = res[:, 0].sum(), res[:, 1].sum()
-    return int(n * 48 + 64 * v_int + 48 * tri), float(v_int) / n, float(tri) / n
+    return int(n * 48 + rec_bytes * v_int + 48 * tri), float(v_int) / n, float(tri) / n
 
 
 # ------------------------------------------------------------- GPU arm
@@ -254,6 +255,8 @@ def run_gpu(args):
     t_bvh = time.perf_counter()
     nodes, bounds = S.build_bvh_device()  # CNormalBVH.build's tree, built level by level on the GPU
     bvh_build_ms = (time.perf_counter() - t_bvh) * 1e3
+    if args.precision:
+        S.set_precision(1)  # FP16 child boxes rounded outward, 32-byte records
     if ENV_ON:
         S.set_env(env, ENV_W, ENV_H)
         S.grid_config(*GRID, enable=2)  # grid-guided environment sampling, FP64 per-cell SATs
@@ -357,7 +360,8 @@ def run_gpu(args):
         orc = Oracle()
         threads = os.cpu_count() or 1
         t_alg = time.perf_counter()
-        alg_bytes, v_int, tri = algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_no(1), threads)
+        alg_bytes, v_int, tri = algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_no(1), threads,
+                                                  rec_bytes=32 if args.precision else 64)
         t_alg = time.perf_counter() - t_alg
         peaks = {}
         try:
@@ -405,6 +409,7 @@ def run_gpu(args):
             "inflight_frames": args.inflight,
             "msamples_per_s": round(width * height * spp * args.steps * world / (ms * 1e-3) / 1e6, 2),
             "bvh_depth": S.depth, "bvh_build_ms": round(bvh_build_ms, 2), "bvh_build": "GPU, level-synchronous",
+            "bvh_records": "FP16 child boxes rounded outward, 32 B" if args.precision else "FP32 child boxes, 64 B",
             "alg_bytes_seconds": round(t_alg, 1),
         }
     job.close()
@@ -651,6 +656,8 @@ def main():
     ap.add_argument("--small", action="store_true", help="small case for profiler captures")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--inflight", type=int, default=4, help="frames kept in flight on separate streams (1..4)")
+    ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
+                    help="BVH records: 0 FP32 child boxes (64 B), 1 FP16 outward-rounded (32 B)")
     ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS) + ["batched", "served", "plain"])
     ap.add_argument("--lanes", type=int, default=16, help="batched/served: requests in flight")
     ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")

@@ -123,8 +123,12 @@ int mt_bvh_build_device(mt_scene* scene, int32_t* nodes_out, float* bounds_out, 
 int mt_scene_layout_read(mt_scene* scene, void* records_out, void* tris_out, int* nrec_out, int* root_ref_out);
 /* Use a BVH built elsewhere (the Java builder's nodes/bounds buffers). */
 int mt_bvh_import(mt_scene* scene, const int32_t* nodes, const float* bounds, int nnodes);
-/* Traversal precision: 0 = FP32 child boxes (default), 1 = 8-bit child boxes
- * quantised relative to the parent and rounded outward. */
+/* Traversal record format: 0 = FP32 child boxes (default, 64-byte records),
+ * 1 = FP16 child boxes rounded outward (32-byte records, kept beside the FP32
+ * ones and rebuilt with every BVH build or import). Outward rounding keeps every
+ * node the FP32 traversal enters, so closest hits are the same triangles at the
+ * same distances; only which of two triangles hit at exactly the same distance
+ * is reported can change with the visit order. */
 int mt_scene_set_bvh_precision(mt_scene* scene, int precision);
 /* Replace the material table (TracerAPI material edits, src/cl/ui/fx/main/TracerAPI.java:371). */
 int mt_scene_set_materials(mt_scene* scene, const void* materials, int nmaterials);

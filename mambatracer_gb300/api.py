@@ -108,6 +108,10 @@ class Scene:
         check(lib().mt_scene_layout_read(self.h, _p(recs) if nrec.value else None, _p(tris), None, None))
         return recs, tris, root.value
 
+    def set_precision(self, precision: int):
+        """Traversal record format: 0 FP32 child boxes, 1 FP16 rounded outward."""
+        check(lib().mt_scene_set_bvh_precision(self.h, precision))
+
     def import_bvh(self, nodes: np.ndarray, bounds: np.ndarray):
         nodes = np.ascontiguousarray(nodes, np.int32)
         bounds = np.ascontiguousarray(bounds, np.float32)

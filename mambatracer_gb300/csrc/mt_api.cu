@@ -255,6 +255,7 @@ void free_scene(mt_scene* s) {
   dfree(s->d_light_faces);
   dfree(s->d_nodes);
   dfree(s->d_tris);
+  dfree(s->d_qnodes);
   dfree(s->d_env_rgb);
   dfree(s->d_env_lum);
   dfree(s->d_env_sat);
@@ -618,7 +619,8 @@ extern "C" int mt_bvh_build(mt_scene* s, int32_t* nodes_out, float* bounds_out, 
   int q = quiesce(s->ctx);
   if (q) return q;
   ++s->version;
-  return import_bvh(s, nodes.data(), bounds.data(), 2 * n - 1);
+  int r = import_bvh(s, nodes.data(), bounds.data(), 2 * n - 1);
+  return r ? r : refresh_qnodes(s);
 }
 
 extern "C" int mt_bvh_build_host(const float* points, int npoints, const int32_t* faces, int nfaces,
@@ -664,14 +666,20 @@ extern "C" int mt_bvh_import(mt_scene* s, const int32_t* nodes, const float* bou
   int q = quiesce(s->ctx);
   if (q) return q;
   ++s->version;
-  return import_bvh(s, nodes, bounds, nnodes);
+  int r = import_bvh(s, nodes, bounds, nnodes);
+  return r ? r : refresh_qnodes(s);
 }
 
 extern "C" int mt_scene_set_bvh_precision(mt_scene* s, int precision) {
   if (!s) return fail(MT_ERR_INVALID, "NULL scene");
-  if (precision != 0) return fail(MT_ERR_INVALID, "BVH precision %d is not available in this build", precision);
+  if (precision != 0 && precision != 1) return fail(MT_ERR_INVALID, "BVH precision %d (0 FP32, 1 FP16)", precision);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  CU(cudaSetDevice(s->ctx->device));
+  int q = quiesce(s->ctx);
+  if (q) return q;
+  ++s->version;
   s->precision = precision;
-  return MT_OK;
+  return refresh_qnodes(s);
 }
 
 // -------------------------------------------------------------- environment

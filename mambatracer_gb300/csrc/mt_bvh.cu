@@ -25,6 +25,7 @@
 // interior records in breadth-first order (the order of a level's nodes by
 // their triangle range), leaf slots = the triangles' final positions (the
 // depth-first leaf order), each record holding its two children's boxes.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
@@ -354,6 +355,20 @@ __global__ void k_tris(int n, const int* __restrict__ obj, const float4* __restr
   tris[3 * (size_t)k + 2] = make_float4(p3.x - p1.x, p3.y - p1.y, p3.z - p1.z, 0.f);
 }
 
+// FP16 records from FP32 ones: lower planes rounded down, upper planes up.
+__global__ void k_quantize_fp16(const float4* __restrict__ recs, int nrec, uint4* q) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrec) return;
+  const float4* p = recs + 4 * (size_t)i;
+  const float4 n0 = p[0], n1 = p[1], n2 = p[2], n3 = p[3];
+  auto pair = [](float lo, float hi) {
+    __half2 h = __halves2half2(__float2half_rd(lo), __float2half_ru(hi));
+    return *reinterpret_cast<unsigned*>(&h);
+  };
+  q[2 * (size_t)i + 0] = make_uint4(pair(n0.x, n0.y), pair(n0.z, n0.w), pair(n1.x, n1.y), pair(n1.z, n1.w));
+  q[2 * (size_t)i + 1] = make_uint4(pair(n2.x, n2.y), pair(n2.z, n2.w), __float_as_uint(n3.x), __float_as_uint(n3.y));
+}
+
 __global__ void k_seed(Seg* segs, int n) {
   if (blockIdx.x == 0 && threadIdx.x == 0) segs[0] = Seg{0, 0, n, 1, 0, -1, 0};
 }
@@ -487,5 +502,19 @@ extern "C" int mt_bvh_build_device(mt_scene* s, int32_t* nodes_out, float* bound
   s->has_bvh = 1;
   ++s->version;
   if (depth_out) *depth_out = depth;
+  return refresh_qnodes(s);
+}
+
+int refresh_qnodes(mt_scene* s) {
+  dfree(s->d_qnodes);
+  if (s->precision != 1 || !s->has_bvh || s->nrec == 0) return MT_OK;
+  int r = dalloc(&s->d_qnodes, 2 * (size_t)s->nrec);
+  if (r) return r;
+  cudaStream_t st = s->ctx->stream;
+  k_quantize_fp16<<<blocks(s->nrec), kT, 0, st>>>(s->d_nodes, s->nrec, s->d_qnodes);
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+    dfree(s->d_qnodes);
+    return fail(MT_ERR_CUDA, "FP16 records: %s", cudaGetErrorString(cudaGetLastError()));
+  }
   return MT_OK;
 }

@@ -42,7 +42,8 @@ static_assert(sizeof(Material) == 144, "Material layout");
 //   a child ref >= 0 is a record index, < 0 is ~(triangle slot).
 //   tris: 3 float4 per triangle slot (leaf order): (p1.xyz, bits(face id)),
 //     (p2 - p1, 0), (p3 - p1, 0), the edges of the reference's Moller-Trumbore.
-//   qnodes: 8-bit child boxes (precision 1): 2 float4 + 1 uint4 per record.
+//   qnodes: FP16 child boxes rounded outward (precision 1), 2 x 16 B per record:
+//     (L.x, L.y, R.x, R.y) as (lo, hi) half2 pairs, then (L.z, R.z, left ref, right ref).
 struct DevScene {
   const float4* nodes;
   const float4* qnodes;

@@ -90,6 +90,7 @@ struct mt_scene {
   // traversal layout
   float4* d_nodes = nullptr;
   float4* d_tris = nullptr;
+  uint4* d_qnodes = nullptr;  // FP16 records (precision 1)
   int nrec = 0, root_ref = 0, depth = 0, has_bvh = 0, precision = 0;
   // environment
   float4* d_env_rgb = nullptr;
@@ -113,12 +114,12 @@ struct mt_scene {
   DevScene view() const {
     DevScene s{};
     s.nodes = d_nodes;
-    s.qnodes = nullptr;
+    s.qnodes = reinterpret_cast<const float4*>(d_qnodes);
     s.tris = d_tris;
     s.root_ref = root_ref;
     s.ntri = ntri;
     s.nrec = nrec;
-    s.precision = precision;
+    s.precision = (precision == 1 && d_qnodes) ? 1 : 0;
     s.points = d_points;
     s.uvs = d_uvs;
     s.normals = d_normals;
@@ -223,3 +224,5 @@ void join_jobs(mt_context* ctx);
 int quiesce(mt_context* ctx);
 // Waits for the requests running on the context's servers' lanes.
 void servers_sync(mt_context* ctx);
+// Rebuild (precision 1) or drop the scene's FP16 records from its FP32 records.
+int refresh_qnodes(mt_scene* s);

@@ -134,24 +134,27 @@ constexpr int kSteps = 64;
 // MINB: resident blocks per SM the register allocation is bounded for (the
 // traversal is latency-bound: more resident warps hide more load latency, at
 // the price of registers).
-template <int MINB>
+// PREC: the BVH record format (0 FP32 child boxes, 1 FP16 outward-rounded).
+template <int MINB, int PREC>
 __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_closest(DevScene S, Ctrl* ctrl, int b, FrameBufs fb) {
   const int count = ctrl->count[b];
   bool overflow = false;
-  tr::trace_persistent<false, kSteps>(S, count, &ctrl->work[2 * b], QueueRays{fb.q_o[(b + 1) & 1], fb.q_d[(b + 1) & 1]},
-                                     HitOut{fb.hit_t, fb.hit_prim}, &overflow);
+  tr::trace_persistent<false, kSteps, QueueRays, HitOut, PREC>(
+      S, count, &ctrl->work[2 * b], QueueRays{fb.q_o[(b + 1) & 1], fb.q_d[(b + 1) & 1]}, HitOut{fb.hit_t, fb.hit_prim},
+      &overflow);
   if (overflow) atomicExch(&ctrl->error, kDevErrStack);
 }
 
-template <int MINB>
+template <int MINB, int PREC>
 __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_shadow(DevScene S, Ctrl* ctrl, int b, int mode,
                                                                       FrameBufs fb, int kahan) {
   // mode 0: shadow slots are the compacted survivor slots (flagged by pixel >= 0)
   const int count = mode == 0 ? ctrl->count[b + 1] : ctrl->shadow[b];
   bool overflow = false;
   unsigned traced = 0;
-  tr::trace_persistent<true, kSteps>(S, count, &ctrl->work[2 * b + 1], ShadowRays{fb.s_o, fb.s_d},
-                                    ShadowResolve{fb.s_o, fb.s_c, fb.film, fb.film_c, kahan, &traced}, &overflow);
+  tr::trace_persistent<true, kSteps, ShadowRays, ShadowResolve, PREC>(
+      S, count, &ctrl->work[2 * b + 1], ShadowRays{fb.s_o, fb.s_d},
+      ShadowResolve{fb.s_o, fb.s_c, fb.film, fb.film_c, kahan, &traced}, &overflow);
   unsigned long long tot = traced;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
@@ -435,16 +438,23 @@ int shade_minb() {
 template <int MINB>
 int trace_blocks_per_sm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest<MINB>, kTraceThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest<MINB, 0>, kTraceThreads, 0);
   return n > 0 ? n : 1;
 }
 template <int MINB>
 void launch_traces(cudaStream_t st, int grid, const DevScene& S, Ctrl* ctrl, int b, int mode, FrameBufs fb, int kahan,
                    bool closest) {
-  if (closest)
-    k_trace_closest<MINB><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb);
-  else
-    k_trace_shadow<MINB><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan);
+  if (closest) {
+    if (S.precision == 1)
+      k_trace_closest<MINB, 1><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb);
+    else
+      k_trace_closest<MINB, 0><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb);
+  } else {
+    if (S.precision == 1)
+      k_trace_shadow<MINB, 1><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan);
+    else
+      k_trace_shadow<MINB, 0><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan);
+  }
 }
 }  // namespace
 
@@ -519,23 +529,29 @@ struct QueryOut {
 };
 }  // namespace
 
+template <int PREC>
 __global__ void __launch_bounds__(kTraceThreads, 8) k_query(DevScene S, const float4* __restrict__ rays, int n, int any,
                                                             float* __restrict__ t_out, int* __restrict__ prim_out,
                                                             int* work, int* err) {
   bool overflow = false;
   if (any)
-    tr::trace_persistent<true, kSteps>(S, n, work, RefRays{rays}, QueryOut{1, t_out, prim_out}, &overflow);
+    tr::trace_persistent<true, kSteps, RefRays, QueryOut, PREC>(S, n, work, RefRays{rays}, QueryOut{1, t_out, prim_out},
+                                                                &overflow);
   else
-    tr::trace_persistent<false, kSteps>(S, n, work, RefRays{rays}, QueryOut{0, t_out, prim_out}, &overflow);
+    tr::trace_persistent<false, kSteps, RefRays, QueryOut, PREC>(S, n, work, RefRays{rays},
+                                                                 QueryOut{0, t_out, prim_out}, &overflow);
   if (overflow) atomicExch(err, kDevErrStack);
 }
 
 int launch_query(cudaStream_t st, const DevScene& S, const float4* rays, int n, int any, float* t_out, int* prim_out,
                  int* work, int* err, int num_sms) {
   int bps = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_query, kTraceThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_query<0>, kTraceThreads, 0);
   if (bps < 1) bps = 1;
-  k_query<<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
+  if (S.precision == 1)
+    k_query<1><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
+  else
+    k_query<0><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -9,7 +9,18 @@
 // per-thread stack of deferred children (local memory) visits the same nodes in
 // the same order without re-reading parents. Identical order and identical
 // arithmetic give identical hit ids, including ties.
+//
+// Two record formats (DevScene::precision): 0 = FP32 child boxes, 64 bytes per
+// record; 1 = FP16 child boxes rounded outward (lower bounds down, upper bounds
+// up), 32 bytes per record: the half-size record halves the bytes a visit
+// moves through L1/L2. An outward-rounded box contains the FP32 box, and the
+// slab arithmetic is monotonic in the planes, so every node the FP32 traversal
+// enters is entered too and the closest hit is the same triangle at the same
+// distance; only a different visit order can pick another of two triangles hit
+// at exactly the same distance.
 #pragma once
+#include <cuda_fp16.h>
+
 #include "mt_device.cuh"
 
 namespace mt {
@@ -113,15 +124,42 @@ struct StackEntry<true> {
   using type = int;
 };
 
-template <bool ANY>
+// A record's two child boxes as n0 = (L.lo.x, L.hi.x, L.lo.y, L.hi.y),
+// n1 = the same for R, n2 = (L.lo.z, L.hi.z, R.lo.z, R.hi.z), and its child refs.
+// FP16 records: q0 = half2 pairs (L x, L y, R x, R y), q1 = (L z, R z, left, right).
+template <int PREC>
+__device__ __forceinline__ void load_record(const DevScene& S, int ref, float4& n0, float4& n1, float4& n2, int& left,
+                                            int& right) {
+  if constexpr (PREC == 0) {
+    const float4* p = S.nodes + 4 * (size_t)ref;
+    n0 = __ldg(p + 0);
+    n1 = __ldg(p + 1);
+    n2 = __ldg(p + 2);
+    const float4 n3 = __ldg(p + 3);
+    left = __float_as_int(n3.x);
+    right = __float_as_int(n3.y);
+  } else {
+    const uint4* p = reinterpret_cast<const uint4*>(S.qnodes) + 2 * (size_t)ref;
+    const uint4 q0 = __ldg(p + 0), q1 = __ldg(p + 1);
+    auto h2 = [](unsigned u) { return __half22float2(*reinterpret_cast<const __half2*>(&u)); };
+    const float2 lx = h2(q0.x), ly = h2(q0.y), rx = h2(q0.z), ry = h2(q0.w), lz = h2(q1.x), rz = h2(q1.y);
+    n0 = make_float4(lx.x, lx.y, ly.x, ly.y);
+    n1 = make_float4(rx.x, rx.y, ry.x, ry.y);
+    n2 = make_float4(lz.x, lz.y, rz.x, rz.y);
+    left = (int)q1.z;
+    right = (int)q1.w;
+  }
+}
+
+template <bool ANY, int PREC = 0>
 __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref, int& sp, int& hit_face, bool finite,
                                            typename StackEntry<ANY>::type* stack, int steps, bool* overflow) {
-  const float4* __restrict__ nodes = S.nodes;
   const float4* __restrict__ tris = S.tris;
   for (int it = 0; it < steps; ++it) {
     if (ref >= 0) {
-      const float4* p = nodes + 4 * (size_t)ref;
-      float4 n0 = __ldg(p + 0), n1 = __ldg(p + 1), n2 = __ldg(p + 2), n3 = __ldg(p + 3);
+      float4 n0, n1, n2;
+      int left, right;
+      load_record<PREC>(S, ref, n0, n1, n2, left, right);
       float tl, trr;
       bool hl, hr;
       if (finite) {
@@ -133,7 +171,6 @@ __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref,
         hl = slab(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, &tl);
         hr = slab(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, &trr);
       }
-      const int left = __float_as_int(n3.x), right = __float_as_int(n3.y);
       if (hl && hr) {
         const bool rfirst = trr < tl;
         if (sp >= kStackDepth) {
@@ -180,7 +217,7 @@ __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref,
 // finished its ray takes the next one from the global counter, so warps stay
 // full while rays of very different lengths run side by side.
 // Src: RayT load(int i); Dst: void store(int i, const RayT&, int hit_face).
-template <bool ANY, int STEPS, class Src, class Dst>
+template <bool ANY, int STEPS, class Src, class Dst, int PREC = 0>
 __device__ __forceinline__ void trace_persistent(const DevScene& S, int count, int* work, Src src, Dst dst,
                                                  bool* overflow) {
   const int lane = threadIdx.x & 31;
@@ -213,7 +250,7 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, int count, i
     }
     const bool active = i >= 0;
     if (!__any_sync(0xffffffffu, active)) break;
-    if (active && trav_steps<ANY>(S, r, ref, sp, hit, finite, stack, STEPS, overflow)) {
+    if (active && trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, STEPS, overflow)) {
       dst(i, r, hit);
       i = -1;
     }

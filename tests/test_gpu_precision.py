@@ -1,0 +1,75 @@
+"""FP16 traversal records (mt_scene_set_bvh_precision(scene, 1)): child boxes
+rounded outward to half precision, 32 bytes per record. The traversal enters
+every node the FP32 records let it enter, so closest hits are the same
+triangles at the same distances (bit for bit) and any-hit answers are the same;
+the only freedom is which of two triangles hit at exactly the same distance is
+kept, when the changed visit order meets them the other way round. Frames in
+benchmark semantics are compared with the FP32 records' frames."""
+import numpy as np
+import pytest
+
+from mambatracer_gb300 import api, layout, scenes
+from mambatracer_gb300._lib import MTError
+from tests.helpers import rel_rmse
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "room": lambda: scenes.box_room(64, 48),
+    "soup": lambda: scenes.soup(200000, seed=8, extent=0.8, edge_sigma=0.01),
+    "stadium": lambda: scenes.stadium(quads=300, level=6, width=64, height=48),
+}
+
+
+@pytest.mark.parametrize("which", list(CASES))
+def test_fp16_records_trace_the_same_hits(ctx, which):
+    sc = CASES[which]()
+    S = api.Scene(ctx, sc)
+    S.build_bvh_device(want_arrays=False)
+    o, d = scenes.random_rays(sc, 200000, seed=19, inside=True)
+    rays = layout.make_rays(o, d)
+    srays = layout.make_rays(o, d, tmin=1e-4, tmax=0.25)
+    t0, p0 = S.trace_closest(rays)
+    a0 = S.trace_any(srays)
+    S.set_precision(1)
+    t1, p1 = S.trace_closest(rays)
+    a1 = S.trace_any(srays)
+    assert (p0 >= 0).sum() > 10000
+    assert t0.tobytes() == t1.tobytes()
+    differ = p0 != p1
+    assert differ.sum() <= 1e-4 * len(p0), differ.sum()   # exact-distance ties only
+    assert np.array_equal(a0, a1)
+    # a rebuild keeps the format; going back to FP32 gives the FP32 answers
+    S.build_bvh_device(want_arrays=False)
+    t2, p2 = S.trace_closest(rays)
+    assert t2.tobytes() == t1.tobytes() and np.array_equal(p2, p1)
+    S.set_precision(0)
+    t3, p3 = S.trace_closest(rays)
+    assert t3.tobytes() == t0.tobytes() and np.array_equal(p3, p0)
+    S.close()
+
+
+def test_fp16_records_render(ctx):
+    sc = scenes.soup(100000, seed=3, extent=0.8, edge_sigma=0.01)
+    env = scenes.sky_env(512, 256)
+    S = api.Scene(ctx, sc)
+    S.build_bvh_device(want_arrays=False)
+    S.set_env(env, 512, 256)
+    films = []
+    for prec in (0, 1):
+        S.set_precision(prec)
+        J = api.Job(ctx, S, 96, 64, max_depth=8, mode=1, rr_depth=3, film_kahan=1)
+        J.set_camera(sc.camera)
+        for f in range(4):
+            J.render(None, float(f + 1))
+        films.append(J.film())
+        J.close()
+    assert rel_rmse(films[1], films[0]) < 1e-4
+    S.close()
+
+
+def test_precision_argument_checked(ctx):
+    S = api.Scene(ctx, scenes.box_room(8, 8))
+    with pytest.raises(MTError):
+        S.set_precision(2)
+    S.close()
