@@ -163,18 +163,191 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_shadow(DevScene S
 }
 
 // ----------------------------------------------------------------- shade
-// mode 0 (reference semantics): survivors are compacted first, the light and
-// BSDF samples of a survivor are keyed on its compacted slot as DirectLight and
-// SampleBSDFRayDirection key them on get_global_id; the shadow ray of survivor
-// j' sits at shadow slot j'.
-// mode 1 (benchmark semantics): samples are keyed on the pixel, Russian
-// roulette runs after the BSDF sample, and the survivors and shadow rays are
-// compacted together afterwards.
+// The per-path work, in two phases around the reference's compaction:
+//   shade_hit       IntersectPrimitives' hit record, SetupBSDFPath and
+//                   LightHitPass (emitter or environment contribution);
+//   shade_continue  the texture pass, DirectLight (light sample, BSDF
+//                   evaluation, shadow ray) and SampleBSDFRayDirection, then
+//                   Russian roulette in benchmark semantics.
+struct PathState {
+  bool alive;
+  int pixel;
+  V thr, ps;
+  int spec;
+  Hit H;
+  Bsdf B;
+};
+struct ShadeOut {
+  bool has_shadow;
+  V sho, shd, shc, ndir;
+};
+
+template <int MODE>
+__device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, const PassParams* __restrict__ pp, int b,
+                                          const FrameBufs& fb, int j, int count, PathState& P) {
+  const int kahan = pp->kahan;
+  P.alive = false;
+  P.pixel = 0;
+  P.thr = zero4();
+  P.ps = zero4();
+  P.spec = 0;
+  P.B.mat = -1;
+  if (j >= count) return;
+  float4 qo = __ldg(fb.q_o[(b + 1) & 1] + j);
+  float4 qd = __ldg(fb.q_d[(b + 1) & 1] + j);
+  const int pixel = __float_as_int(qo.w);
+  P.pixel = pixel;
+  V o = mk(qo.x, qo.y, qo.z, 0.f), d = mk(qd.x, qd.y, qd.z, 0.f);
+  const float t = fb.hit_t[j];
+  const int prim = fb.hit_prim[j];
+  P.thr = fb.thr[pixel];
+  P.ps = fb.ps[pixel];
+  P.spec = fb.flag[pixel];
+  if (prim >= 0) {
+    hit_record(S, o, d, t, prim, P.H);
+    P.B = setup_bsdf(S, d, P.H.n, P.H.mat);
+    if (P.B.mat >= 0) {
+      const Material& M = S.materials[P.B.mat];
+      if (is_emitter(M)) {  // LightHitPass emitter branch, Render.cl:76-104
+        float pick = 1.f / (float)S.nlights;
+        if (MODE == 1 && E.present && S.nlights > 0) pick = pick * 0.5f;
+        AreaLight L = get_area_light(S, M, prim);
+        float pdfA = 0.f;
+        V c = radiance_area(L, d, &pdfA);
+        if (zero3(c)) {
+          P.alive = true;  // Render.cl:88-89 returns with isect->hit still set
+        } else {
+          float w = 1.f;
+          if (!P.spec) {
+            float pdfW = pdf_a_to_w(pdfA, t, P.B.fix.z);
+            w = mis2(P.ps.w, pdfW * pick);
+          }
+          film_add(fb.film, fb.film_c, pixel, muls(mul(P.thr, c), w), kahan);
+        }
+      } else {
+        P.alive = true;
+      }
+    }
+  } else if (E.present) {  // LightHitPass environment branch, Render.cl:106-123
+    float pdfW = 0.f;
+    V c;
+    if (MODE == 1 && E.grid_on)
+      c = radiance_env_grid(E, pp->cam_pos, P.ps, d, &pdfW, pp->grid_accum && !P.spec);
+    else
+      c = radiance_env(E, d, &pdfW);
+    if (!zero3(c)) {
+      if (MODE == 1 && S.nlights > 0) pdfW = pdfW * 0.5f;
+      float w = 1.f;
+      if (!P.spec) w = mis2(P.ps.w, pdfW);
+      film_add(fb.film, fb.film_c, pixel, muls(mul(P.thr, c), w), kahan);
+    }
+  }
+}
+
+// gid: the work-item id the samples are keyed on (mode 0: the compacted slot,
+// mode 1: the pixel's id). Writes the path state back; P.alive turns false when
+// Russian roulette ends the path.
+template <int MODE, bool TEX>
+__device__ __forceinline__ void shade_continue(const DevScene& S, const DevEnv& E, const PassParams* __restrict__ pp,
+                                               int b, const FrameBufs& fb, int gid, PathState& P, ShadeOut& R) {
+  const float fc = pp->frame_count;
+  R.has_shadow = false;
+  R.ndir = zero4();
+  Bsdf B = P.B;
+  Material tm;  // the path's textured copy of its material
+  if (TEX && has_textures(*B.pm)) {
+    tm = *B.pm;
+    apply_textures(S, B.mat, P.H.u, P.H.v, tm);
+    B.pm = &tm;
+  }
+  int32_t lx, ly, bx, by;
+  if (MODE == 0) {
+    lx = pp->seeds[2 * (2 * b)];
+    ly = pp->seeds[2 * (2 * b) + 1];
+    bx = lx;
+    by = ly;
+  } else {
+    stage_seed(b, 1, &lx, &ly);
+    stage_seed(b, 2, &bx, &by);
+  }
+  Seed s = gen_seed(lx, ly, fc, gid);
+  V dir = zero4();
+  float dist = 0.f, pdfW = 0.f, pick = 1.f;
+  V smp;
+  smp.x = rnd(s);
+  smp.y = rnd(s);
+  smp.z = rnd(s);
+  smp.w = rnd(s);
+  V rad = zero4();
+  bool smesh = false, senv = false;
+  if (E.present && S.nlights > 0) {
+    float r = rnd(s);
+    pick = pick * 0.5f;
+    if (r < 0.5f) smesh = true; else senv = true;
+  } else if (E.present) {
+    senv = true;
+  } else if (S.nlights > 0) {
+    smesh = true;
+  }
+  if (smesh) {
+    int li = (int)(rnd(s) * (float)S.nlights);
+    li = li < S.nlights ? li : S.nlights - 1;  // rounding of rnd * n for n > 2^22
+    int tri = S.light_faces[MODE == 0 ? 0 : li];  // Render.cl:305 reads light 0
+    pick = pick * (1.f / (float)S.nlights);
+    const Material& Ml = S.materials[__ldg(reinterpret_cast<const int*>(S.faces + tri) + 9) & 0xFFFF];
+    AreaLight L = get_area_light(S, Ml, tri);
+    rad = illuminate_area(L, P.H.p, smp.x, smp.y, &dir, &dist, &pdfW);
+  } else if (senv) {
+    if (MODE == 1 && E.grid_on)
+      rad = illuminate_env_grid(E, pp->cam_pos, P.H.p, smp, &dir, &dist, &pdfW);
+    else
+      rad = illuminate_env(E, smp, &dir, &dist, &pdfW);
+  }
+  if (!zero3(rad)) {
+    float bpdf = 0.f, cosO = 0.f;
+    V f = eval_bsdf(S, B, dir, &bpdf, &cosO);
+    if (!zero3(f)) {
+      float w = mis2(pdfW, bpdf);
+      float sc = (w * cosO / (pick * pdfW));
+      R.shc = mk(sc * (rad.x * f.x) * P.thr.x, sc * (rad.y * f.y) * P.thr.y, sc * (rad.z * f.z) * P.thr.z, 1.f);
+      R.sho = mk(P.H.p.x, P.H.p.y, P.H.p.z, __int_as_float(P.pixel));
+      R.shd = mk(dir.x, dir.y, dir.z, dist - 2.f * 1e-3f);
+      R.has_shadow = true;
+    }
+  }
+  // BSDF sample
+  Seed s2 = gen_seed(bx, by, fc, gid);
+  float s0 = rnd(s2), s1 = rnd(s2), sz = rnd(s2);
+  float pdf = 0.f, cosO = 0.f;
+  V f = sample_bsdf(S, B, s0, s1, sz, &R.ndir, &pdf, &cosO);
+  float q = cosO / pdf;
+  V thr = mul(P.thr, muls(f, q));
+  V ps = mk(P.H.p.x, P.H.p.y, P.H.p.z, pdf);
+  if (MODE == 1 && pp->rr_depth > 0 && b >= pp->rr_depth) {
+    int32_t rx, ry;
+    stage_seed(b, 3, &rx, &ry);
+    Seed rs = gen_seed(rx, ry, fc, gid);
+    float u = rnd(rs);
+    float mx = maxf_(thr.x, maxf_(thr.y, thr.z));
+    float cont = minf_(0.95f, mx);
+    if (!(u < cont)) P.alive = false;
+    else thr = divs(thr, cont);
+  }
+  fb.thr[P.pixel] = thr;
+  fb.ps[P.pixel] = ps;
+  fb.flag[P.pixel] = 0;
+}
+
+// Reference semantics (mode 0), one 256-path tile per block: survivors are
+// compacted in order (block scan + decoupled look-back) between the two phases,
+// and the light and BSDF samples of a survivor are keyed on its compacted slot
+// as DirectLight and SampleBSDFRayDirection key them on get_global_id; the
+// shadow ray of survivor j' sits at shadow slot j' (pixel -1: none).
 // TEX: the scene has textures (a separate instance keeps the untextured one lean).
-template <int MODE, int MINB, bool TEX = false>
-__global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEnv E, const PassParams* __restrict__ pp,
-                                                         Ctrl* ctrl, int b, FrameBufs fb,
-                                                         unsigned long long* status) {
+template <int MINB, bool TEX = false>
+__global__ void __launch_bounds__(kShadeThreads, MINB) k_shade_ref(DevScene S, DevEnv E, const PassParams* __restrict__ pp,
+                                                             Ctrl* ctrl, int b, FrameBufs fb,
+                                                             unsigned long long* status) {
   __shared__ unsigned long long sh[kShadeThreads / 32 + 1];
   __shared__ int s_tile;
   __shared__ unsigned long long s_base;
@@ -185,210 +358,74 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEn
   const int tile = s_tile;
   if (tile >= ntiles) return;
   const int j = tile * kShadeThreads + threadIdx.x;
-  const float fc = pp->frame_count;
-  const int kahan = pp->kahan;
-
-  bool alive = false;
-  int pixel = 0;
-  V thr = zero4(), ps = zero4();
-  int spec = 0;
-  Hit H;
-  Bsdf B;
-  B.mat = -1;
-  if (j < count) {
-    float4 qo = __ldg(fb.q_o[(b + 1) & 1] + j);
-    float4 qd = __ldg(fb.q_d[(b + 1) & 1] + j);
-    pixel = __float_as_int(qo.w);
-    V o = mk(qo.x, qo.y, qo.z, 0.f), d = mk(qd.x, qd.y, qd.z, 0.f);
-    const float t = fb.hit_t[j];
-    const int prim = fb.hit_prim[j];
-    thr = fb.thr[pixel];
-    ps = fb.ps[pixel];
-    spec = fb.flag[pixel];
-    if (prim >= 0) {
-      hit_record(S, o, d, t, prim, H);
-      B = setup_bsdf(S, d, H.n, H.mat);
-      if (B.mat >= 0) {
-        const Material& M = S.materials[B.mat];
-        if (is_emitter(M)) {  // LightHitPass emitter branch, Render.cl:76-104
-          float pick = 1.f / (float)S.nlights;
-          if (MODE == 1 && E.present && S.nlights > 0) pick = pick * 0.5f;
-          AreaLight L = get_area_light(S, M, prim);
-          float pdfA = 0.f;
-          V c = radiance_area(L, d, &pdfA);
-          if (zero3(c)) {
-            alive = true;  // Render.cl:88-89 returns with isect->hit still set
-          } else {
-            float w = 1.f;
-            if (!spec) {
-              float pdfW = pdf_a_to_w(pdfA, t, B.fix.z);
-              w = mis2(ps.w, pdfW * pick);
-            }
-            film_add(fb.film, fb.film_c, pixel, muls(mul(thr, c), w), kahan);
-          }
-        } else {
-          alive = true;
-        }
-      }
-    } else if (E.present) {  // LightHitPass environment branch, Render.cl:106-123
-      float pdfW = 0.f;
-      V c;
-      if (MODE == 1 && E.grid_on)
-        c = radiance_env_grid(E, pp->cam_pos, ps, d, &pdfW, pp->grid_accum && !spec);
-      else
-        c = radiance_env(E, d, &pdfW);
-      if (!zero3(c)) {
-        if (MODE == 1 && S.nlights > 0) pdfW = pdfW * 0.5f;
-        float w = 1.f;
-        if (!spec) w = mis2(ps.w, pdfW);
-        film_add(fb.film, fb.film_c, pixel, muls(mul(thr, c), w), kahan);
-      }
-    }
-  }
-
+  PathState P;
+  shade_hit<0>(S, E, pp, b, fb, j, count, P);
   unsigned long long tot = 0;
-  int slot = -1, sslot = -1;
-  if (MODE == 0) {
-    unsigned long long excl = block_rank2<kShadeThreads>(alive, false, &tot, sh);
-    if (threadIdx.x == 0) s_base = lookback(status, tile, tot, &ctrl->error);
-    __syncthreads();
-    slot = (int)(s_base + excl);
-    if (tile == ntiles - 1 && threadIdx.x == 0) {
-      ctrl->count[b + 1] = (int)(s_base + tot);
-      ctrl->shadow[b] = (int)(s_base + tot);
-    }
+  unsigned long long excl = block_rank2<kShadeThreads>(P.alive, false, &tot, sh);
+  if (threadIdx.x == 0) s_base = lookback(status, tile, tot, &ctrl->error);
+  __syncthreads();
+  const int slot = (int)(s_base + excl);
+  if (tile == ntiles - 1 && threadIdx.x == 0) {
+    ctrl->count[b + 1] = (int)(s_base + tot);
+    ctrl->shadow[b] = (int)(s_base + tot);
   }
-
-  // DirectLight (Render.cl:377-466) and SampleBSDFRayDirection (Render.cl:233-285)
-  bool has_shadow = false;
-  V sho = zero4(), shd = zero4(), shc = zero4();
-  V ndir = zero4();
-  if (alive) {
-    Material tm;  // the path's textured copy of its material
-    if (TEX && has_textures(*B.pm)) {
-      tm = *B.pm;
-      apply_textures(S, B.mat, H.u, H.v, tm);
-      B.pm = &tm;
-    }
-    int32_t lx, ly, bx, by;
-    int gid;
-    if (MODE == 0) {
-      lx = pp->seeds[2 * (2 * b)];
-      ly = pp->seeds[2 * (2 * b) + 1];
-      bx = lx;
-      by = ly;
-      gid = slot;
-    } else {
-      stage_seed(b, 1, &lx, &ly);
-      stage_seed(b, 2, &bx, &by);
-      gid = pixel_gid(pixel);
-    }
-    Seed s = gen_seed(lx, ly, fc, gid);
-    V dir = zero4();
-    float dist = 0.f, pdfW = 0.f, pick = 1.f;
-    V smp;
-    smp.x = rnd(s);
-    smp.y = rnd(s);
-    smp.z = rnd(s);
-    smp.w = rnd(s);
-    V rad = zero4();
-    bool smesh = false, senv = false;
-    if (E.present && S.nlights > 0) {
-      float r = rnd(s);
-      pick = pick * 0.5f;
-      if (r < 0.5f) smesh = true; else senv = true;
-    } else if (E.present) {
-      senv = true;
-    } else if (S.nlights > 0) {
-      smesh = true;
-    }
-    if (smesh) {
-      int li = (int)(rnd(s) * (float)S.nlights);
-      li = li < S.nlights ? li : S.nlights - 1;  // rounding of rnd * n for n > 2^22
-      int tri = S.light_faces[MODE == 0 ? 0 : li];  // Render.cl:305 reads light 0
-      pick = pick * (1.f / (float)S.nlights);
-      const Material& Ml = S.materials[__ldg(reinterpret_cast<const int*>(S.faces + tri) + 9) & 0xFFFF];
-      AreaLight L = get_area_light(S, Ml, tri);
-      rad = illuminate_area(L, H.p, smp.x, smp.y, &dir, &dist, &pdfW);
-    } else if (senv) {
-      if (MODE == 1 && E.grid_on)
-        rad = illuminate_env_grid(E, pp->cam_pos, H.p, smp, &dir, &dist, &pdfW);
-      else
-        rad = illuminate_env(E, smp, &dir, &dist, &pdfW);
-    }
-    if (!zero3(rad)) {
-      float bpdf = 0.f, cosO = 0.f;
-      V f = eval_bsdf(S, B, dir, &bpdf, &cosO);
-      if (!zero3(f)) {
-        float w = mis2(pdfW, bpdf);
-        float sc = (w * cosO / (pick * pdfW));
-        shc = mk(sc * (rad.x * f.x) * thr.x, sc * (rad.y * f.y) * thr.y, sc * (rad.z * f.z) * thr.z, 1.f);
-        sho = mk(H.p.x, H.p.y, H.p.z, __int_as_float(pixel));
-        shd = mk(dir.x, dir.y, dir.z, dist - 2.f * 1e-3f);
-        has_shadow = true;
-      }
-    }
-    // BSDF sample
-    Seed s2 = gen_seed(bx, by, fc, gid);
-    float s0 = rnd(s2), s1 = rnd(s2), sz = rnd(s2);
-    float pdf = 0.f, cosO = 0.f;
-    V f = sample_bsdf(S, B, s0, s1, sz, &ndir, &pdf, &cosO);
-    float q = cosO / pdf;
-    thr = mul(thr, muls(f, q));
-    spec = 0;
-    ps = mk(H.p.x, H.p.y, H.p.z, pdf);
-    if (MODE == 1 && pp->rr_depth > 0 && b >= pp->rr_depth) {
-      int32_t rx, ry;
-      stage_seed(b, 3, &rx, &ry);
-      Seed rs = gen_seed(rx, ry, fc, gid);
-      float u = rnd(rs);
-      float mx = maxf_(thr.x, maxf_(thr.y, thr.z));
-      float cont = minf_(0.95f, mx);
-      if (!(u < cont)) alive = false;
-      else thr = divs(thr, cont);
-    }
-    fb.thr[pixel] = thr;
-    fb.ps[pixel] = ps;
-    fb.flag[pixel] = 0;
-  }
-
-  if (MODE == 1) {
-    unsigned long long excl = block_rank2<kShadeThreads>(alive, has_shadow, &tot, sh);
-    if (threadIdx.x == 0) s_base = lookback(status, tile, tot, &ctrl->error);
-    __syncthreads();
-    unsigned long long pos = s_base + excl;
-    slot = (int)(pos & kLowMask);
-    sslot = (int)(pos >> 31);
-    if (tile == ntiles - 1 && threadIdx.x == 0) {
-      unsigned long long all = s_base + tot;
-      ctrl->count[b + 1] = (int)(all & kLowMask);
-      ctrl->shadow[b] = (int)(all >> 31);
-    }
-  } else {
-    sslot = slot;
-  }
+  if (!P.alive) return;
+  ShadeOut R;
+  shade_continue<0, TEX>(S, E, pp, b, fb, slot, P, R);
   const int nq = b & 1;  // queue written for bounce b + 1
-  if (MODE == 0) {
-    if (alive) {
-      fb.q_o[nq][slot] = mk(H.p.x, H.p.y, H.p.z, __int_as_float(pixel));
-      fb.q_d[nq][slot] = mk(ndir.x, ndir.y, ndir.z, 0.f);
-      if (has_shadow) {
-        fb.s_o[sslot] = sho;
-        fb.s_d[sslot] = shd;
-        fb.s_c[sslot] = shc;
-      } else {
-        fb.s_o[sslot] = mk(0.f, 0.f, 0.f, __int_as_float(-1));
-      }
-    }
+  fb.q_o[nq][slot] = mk(P.H.p.x, P.H.p.y, P.H.p.z, __int_as_float(P.pixel));
+  fb.q_d[nq][slot] = mk(R.ndir.x, R.ndir.y, R.ndir.z, 0.f);
+  if (R.has_shadow) {
+    fb.s_o[slot] = R.sho;
+    fb.s_d[slot] = R.shd;
+    fb.s_c[slot] = R.shc;
   } else {
-    if (alive) {
-      fb.q_o[nq][slot] = mk(H.p.x, H.p.y, H.p.z, __int_as_float(pixel));
-      fb.q_d[nq][slot] = mk(ndir.x, ndir.y, ndir.z, 0.f);
+    fb.s_o[slot] = mk(0.f, 0.f, 0.f, __int_as_float(-1));
+  }
+}
+
+// Benchmark semantics (mode 1): samples are keyed on the pixel, so the order of
+// the queues carries no meaning and no block ever waits for another. Warps run
+// persistently over 32-path chunks (a chunk counter per bounce); each warp
+// appends its survivors and its shadow rays to the next queues with one atomic
+// per queue per chunk (ballot ranks inside the warp). Russian roulette runs after
+// the BSDF sample.
+template <int MINB, bool TEX = false>
+__global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEnv E, const PassParams* __restrict__ pp,
+                                                         Ctrl* ctrl, int b, FrameBufs fb) {
+  const int count = ctrl->count[b];
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int nq = b & 1;  // queue written for bounce b + 1
+  for (;;) {
+    int chunk = 0;
+    if (lane == 0) chunk = atomicAdd(&ctrl->tiles[b], 1);
+    chunk = __shfl_sync(0xffffffffu, chunk, 0);
+    if (chunk * 32 >= count) break;
+    const int j = chunk * 32 + lane;
+    PathState P;
+    shade_hit<1>(S, E, pp, b, fb, j, count, P);
+    ShadeOut R;
+    R.has_shadow = false;
+    if (P.alive) shade_continue<1, TEX>(S, E, pp, b, fb, pixel_gid(P.pixel), P, R);
+    const unsigned am = __ballot_sync(0xffffffffu, P.alive), sm = __ballot_sync(0xffffffffu, R.has_shadow);
+    int qa = 0, qs = 0;
+    if (lane == 0) {
+      if (am) qa = atomicAdd(&ctrl->count[b + 1], __popc(am));
+      if (sm) qs = atomicAdd(&ctrl->shadow[b], __popc(sm));
     }
-    if (has_shadow) {
-      fb.s_o[sslot] = sho;
-      fb.s_d[sslot] = shd;
-      fb.s_c[sslot] = shc;
+    qa = __shfl_sync(0xffffffffu, qa, 0);
+    qs = __shfl_sync(0xffffffffu, qs, 0);
+    if (P.alive) {
+      const int slot = qa + __popc(am & lt);
+      fb.q_o[nq][slot] = mk(P.H.p.x, P.H.p.y, P.H.p.z, __int_as_float(P.pixel));
+      fb.q_d[nq][slot] = mk(R.ndir.x, R.ndir.y, R.ndir.z, 0.f);
+    }
+    if (R.has_shadow) {
+      const int sslot = qs + __popc(sm & lt);
+      fb.s_o[sslot] = R.sho;
+      fb.s_d[sslot] = R.shd;
+      fb.s_c[sslot] = R.shc;
     }
   }
 }
@@ -435,6 +472,15 @@ int shade_minb() {
   }();
   return v;
 }
+// Resident blocks per SM of the benchmark-semantics shading kernel (its grid is
+// one resident wave of persistent warps).
+int shade_blocks_per_sm(int minb) {
+  int n = 0;
+  if (minb == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shade<4>, kShadeThreads, 0);
+  else if (minb == 5) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shade<5>, kShadeThreads, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shade<3>, kShadeThreads, 0);
+  return n > 0 ? n : 1;
+}
 template <int MINB>
 int trace_blocks_per_sm() {
   int n = 0;
@@ -463,6 +509,7 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
                 size_t status_stride, int num_sms, cudaEvent_t* ev, unsigned long long* totals) {
   const int N = width * height;
   static int bps[17] = {};
+  static int shade_bps[6] = {};
   auto trace = [&](bool closest, int b) {
     const int minb = closest ? trace_minb() : shadow_minb();
     if (bps[minb] == 0)
@@ -483,19 +530,24 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
     trace(true, b);
     if (ev) cudaEventRecord(ev[e++], st);
     unsigned long long* stb = status + (size_t)(b - 1) * status_stride;
-    const int sm = shade_minb();
-    if (S.tex_on && mode == 0)
-      k_shade<0, 3, true><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
-    else if (S.tex_on)
-      k_shade<1, 4, true><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
-    else if (mode == 0)
-      k_shade<0, 3><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
-    else if (sm == 4)
-      k_shade<1, 4><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
-    else if (sm == 5)
-      k_shade<1, 5><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
-    else
-      k_shade<1, 3><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+    if (mode == 0) {
+      if (S.tex_on)
+        k_shade_ref<3, true><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+      else
+        k_shade_ref<3><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+    } else {
+      const int sm = shade_minb();
+      if (shade_bps[sm] == 0) shade_bps[sm] = shade_blocks_per_sm(sm);
+      const int sgrid = std::max(1, std::min(num_sms * shade_bps[sm], tiles));
+      if (S.tex_on)
+        k_shade<4, true><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
+      else if (sm == 4)
+        k_shade<4><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
+      else if (sm == 5)
+        k_shade<5><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
+      else
+        k_shade<3><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
+    }
     if (ev) cudaEventRecord(ev[e++], st);
     trace(false, b);
     if (ev) cudaEventRecord(ev[e++], st);
