@@ -181,8 +181,15 @@ struct ShadeOut {
   bool has_shadow;
   V sho, shd, shc, ndir;
 };
+// LEAN: an instance for scenes without mesh lights (hence without emitters) lit
+// by an environment map through the light grid, the benchmark scenes' case; it
+// leaves out the code of the other cases, which keeps the shading kernel's
+// instruction footprint small.
+template <int LEAN> __device__ __forceinline__ bool mesh_lights(const DevScene& S) { return !LEAN && S.nlights > 0; }
+template <int LEAN> __device__ __forceinline__ bool env_present(const DevEnv& E) { return LEAN || E.present; }
+template <int LEAN> __device__ __forceinline__ bool grid_on(const DevEnv& E) { return LEAN || E.grid_on; }
 
-template <int MODE>
+template <int MODE, int LEAN = 0>
 __device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, const PassParams* __restrict__ pp, int b,
                                           const FrameBufs& fb, int j, int count, PathState& P) {
   const int kahan = pp->kahan;
@@ -208,7 +215,7 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, co
     P.B = setup_bsdf(S, d, P.H.n, P.H.mat);
     if (P.B.mat >= 0) {
       const Material& M = S.materials[P.B.mat];
-      if (is_emitter(M)) {  // LightHitPass emitter branch, Render.cl:76-104
+      if (!LEAN && is_emitter(M)) {  // LightHitPass emitter branch, Render.cl:76-104
         float pick = 1.f / (float)S.nlights;
         if (MODE == 1 && E.present && S.nlights > 0) pick = pick * 0.5f;
         AreaLight L = get_area_light(S, M, prim);
@@ -228,15 +235,15 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, co
         P.alive = true;
       }
     }
-  } else if (E.present) {  // LightHitPass environment branch, Render.cl:106-123
+  } else if (env_present<LEAN>(E)) {  // LightHitPass environment branch, Render.cl:106-123
     float pdfW = 0.f;
     V c;
-    if (MODE == 1 && E.grid_on)
+    if (MODE == 1 && grid_on<LEAN>(E))
       c = radiance_env_grid(E, pp->cam_pos, P.ps, d, &pdfW, pp->grid_accum && !P.spec);
     else
       c = radiance_env(E, d, &pdfW);
     if (!zero3(c)) {
-      if (MODE == 1 && S.nlights > 0) pdfW = pdfW * 0.5f;
+      if (MODE == 1 && mesh_lights<LEAN>(S)) pdfW = pdfW * 0.5f;
       float w = 1.f;
       if (!P.spec) w = mis2(P.ps.w, pdfW);
       film_add(fb.film, fb.film_c, pixel, muls(mul(P.thr, c), w), kahan);
@@ -247,7 +254,7 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, co
 // gid: the work-item id the samples are keyed on (mode 0: the compacted slot,
 // mode 1: the pixel's id). Writes the path state back; P.alive turns false when
 // Russian roulette ends the path.
-template <int MODE, bool TEX>
+template <int MODE, bool TEX, int LEAN = 0>
 __device__ __forceinline__ void shade_continue(const DevScene& S, const DevEnv& E, const PassParams* __restrict__ pp,
                                                int b, const FrameBufs& fb, int gid, PathState& P, ShadeOut& R) {
   const float fc = pp->frame_count;
@@ -280,13 +287,13 @@ __device__ __forceinline__ void shade_continue(const DevScene& S, const DevEnv& 
   smp.w = rnd(s);
   V rad = zero4();
   bool smesh = false, senv = false;
-  if (E.present && S.nlights > 0) {
+  if (env_present<LEAN>(E) && mesh_lights<LEAN>(S)) {
     float r = rnd(s);
     pick = pick * 0.5f;
     if (r < 0.5f) smesh = true; else senv = true;
-  } else if (E.present) {
+  } else if (env_present<LEAN>(E)) {
     senv = true;
-  } else if (S.nlights > 0) {
+  } else if (mesh_lights<LEAN>(S)) {
     smesh = true;
   }
   if (smesh) {
@@ -298,7 +305,7 @@ __device__ __forceinline__ void shade_continue(const DevScene& S, const DevEnv& 
     AreaLight L = get_area_light(S, Ml, tri);
     rad = illuminate_area(L, P.H.p, smp.x, smp.y, &dir, &dist, &pdfW);
   } else if (senv) {
-    if (MODE == 1 && E.grid_on)
+    if (MODE == 1 && grid_on<LEAN>(E))
       rad = illuminate_env_grid(E, pp->cam_pos, P.H.p, smp, &dir, &dist, &pdfW);
     else
       rad = illuminate_env(E, smp, &dir, &dist, &pdfW);
@@ -390,7 +397,7 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade_ref(DevScene S, D
 // appends its survivors and its shadow rays to the next queues with one atomic
 // per queue per chunk (ballot ranks inside the warp). Russian roulette runs after
 // the BSDF sample.
-template <int MINB, bool TEX = false>
+template <int MINB, bool TEX = false, int LEAN = 0>
 __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEnv E, const PassParams* __restrict__ pp,
                                                          Ctrl* ctrl, int b, FrameBufs fb) {
   const int count = ctrl->count[b];
@@ -404,10 +411,10 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEn
     if (chunk * 32 >= count) break;
     const int j = chunk * 32 + lane;
     PathState P;
-    shade_hit<1>(S, E, pp, b, fb, j, count, P);
+    shade_hit<1, LEAN>(S, E, pp, b, fb, j, count, P);
     ShadeOut R;
     R.has_shadow = false;
-    if (P.alive) shade_continue<1, TEX>(S, E, pp, b, fb, pixel_gid(P.pixel), P, R);
+    if (P.alive) shade_continue<1, TEX, LEAN>(S, E, pp, b, fb, pixel_gid(P.pixel), P, R);
     const unsigned am = __ballot_sync(0xffffffffu, P.alive), sm = __ballot_sync(0xffffffffu, R.has_shadow);
     int qa = 0, qs = 0;
     if (lane == 0) {
@@ -539,8 +546,11 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
       const int sm = shade_minb();
       if (shade_bps[sm] == 0) shade_bps[sm] = shade_blocks_per_sm(sm);
       const int sgrid = std::max(1, std::min(num_sms * shade_bps[sm], tiles));
+      const bool lean = S.nlights == 0 && E.present && E.grid_on;
       if (S.tex_on)
         k_shade<4, true><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
+      else if (lean && sm == 4)
+        k_shade<4, false, 1><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
       else if (sm == 4)
         k_shade<4><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
       else if (sm == 5)
