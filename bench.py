@@ -374,7 +374,8 @@ def run_gpu(args):
         tp = os.path.join(ROOT, "profiles", "trace_closest_soup1M_1080p.json")
         if not args.small and args.workload == "soup" and os.path.exists(tp):
             tj = json.load(open(tp))
-            traffic, traffic_src = tj["dram_bytes_per_launch"], tj["source"]
+            key = "dram_bytes_per_launch_fp16_records" if args.precision else "dram_bytes_per_launch"
+            traffic, traffic_src = tj.get(key), tj["source"]
         achieved = alg_bytes / (t_b1 * 1e-3) / 1e9
         roofline = {"bound": "hbm", "kernel": "k_trace_closest (bounce 1, primary rays)",
                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
