@@ -656,7 +656,7 @@ def main():
     ap.add_argument("--impl", default="mambatracer", choices=["mambatracer", "reference"])
     ap.add_argument("--small", action="store_true", help="small case for profiler captures")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--inflight", type=int, default=4, help="frames kept in flight on separate streams (1..4)")
+    ap.add_argument("--inflight", type=int, default=6, help="frames kept in flight on separate streams (1..8)")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
                     help="BVH records: 0 FP32 child boxes (64 B), 1 FP16 outward-rounded (32 B)")
     ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS) + ["batched", "served", "plain"])

@@ -178,7 +178,7 @@ typedef struct mt_render_config {
   int spp;           /* passes per mt_render_frame call */
   int use_graph;     /* 1 = replay each frame's launches as a CUDA graph */
   int profile;       /* 1 = time every kernel launch with CUDA events (no graph) */
-  int inflight;      /* frames kept in flight on their own streams, 0 or 1 = one (1..4); each
+  int inflight;      /* frames kept in flight on their own streams, 0 or 1 = one (1..8); each
                         in-flight frame has its own path state and film, summed on read.
                         profile = 1 forces one. */
   int grid_updates;  /* mode 1 with the scene's light grid on: the first grid_updates frames add

@@ -154,7 +154,7 @@ int check_cfg(const mt_render_config* c) {
   if (c->max_depth < 1 || c->max_depth > kMaxDepth) return fail(MT_ERR_INVALID, "max_depth %d (1..%d)", c->max_depth, kMaxDepth);
   if (c->mode != 0 && c->mode != 1) return fail(MT_ERR_INVALID, "mode %d", c->mode);
   if (c->spp < 1 || c->spp > 4096) return fail(MT_ERR_INVALID, "spp %d", c->spp);
-  if (c->inflight < 0 || c->inflight > 4) return fail(MT_ERR_INVALID, "inflight %d (0..4)", c->inflight);
+  if (c->inflight < 0 || c->inflight > 8) return fail(MT_ERR_INVALID, "inflight %d (0..8)", c->inflight);
   if (c->grid_updates < 0) return fail(MT_ERR_INVALID, "grid_updates %d", c->grid_updates);
   return MT_OK;
 }

@@ -148,7 +148,7 @@ def test_graph_spp_and_kahan_are_consistent(ctx, orc):
     S.close()
 
 
-@pytest.mark.parametrize("inflight", [2, 4])
+@pytest.mark.parametrize("inflight", [2, 4, 8])
 def test_inflight_frames_match_one_stream(ctx, orc, inflight):
     """Frames kept in flight on separate streams trace the same rays as one stream
     (exact totals), and their summed films equal its film up to FP32 summation order."""
