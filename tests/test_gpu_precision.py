@@ -73,3 +73,33 @@ def test_precision_argument_checked(ctx):
     with pytest.raises(MTError):
         S.set_precision(2)
     S.close()
+
+
+def test_record_formats_against_fp64_oracle(ctx, orc):
+    """Both record formats' films (benchmark semantics, Kahan film) against the FP64
+    oracle at matched samples: relative RMSE within 1e-3 each, and the two films
+    within 1e-4 of each other (the same hits, up to exact-distance ties)."""
+    from tests.helpers import bvh_build, env_tables, oracle_frames
+    sc = scenes.soup(20000, seed=4, extent=0.8, edge_sigma=0.02, width=64, height=48)
+    env = scenes.sky_env(256, 128)
+    nodes, bounds, _, _ = bvh_build(orc, sc)
+    lum, sat = env_tables(orc, env, 256, 128)
+    S = api.Scene(ctx, sc)
+    S.import_bvh(nodes, bounds)
+    S.set_env_with_sat(env, lum, sat, 256, 128)
+    depth, spp = 6, 4
+    films = {}
+    for prec in (0, 1):
+        S.set_precision(prec)
+        J = api.Job(ctx, S, 64, 48, max_depth=depth, mode=1, rr_depth=3, film_kahan=1, spp=spp)
+        J.set_camera(sc.camera)
+        J.render(None, 1.0)
+        films[prec] = J.film()
+        J.close()
+    acc64, _, _ = oracle_frames(orc, sc, nodes, bounds, 64, 48, depth, 1, 3, [None] * spp,
+                                env=(env, 256, 128), fp64=True)
+    e32, e16 = rel_rmse(films[0], acc64), rel_rmse(films[1], acc64)
+    print(f"relative RMSE vs FP64 oracle: FP32 records {e32:.3e}, FP16 records {e16:.3e}")
+    assert e32 < 1e-3 and e16 < 1e-3
+    assert rel_rmse(films[1], films[0]) < 1e-4
+    S.close()
