@@ -491,7 +491,9 @@ def run_served(args):
     for key in keys:
         sc = scenes.box_room(64, 64) if key == "room" else make_scene(key, False, W_DEFAULT, H_DEFAULT)
         sc_h = api.Scene(ctx, sc)
-        sc_h.build_bvh()
+        sc_h.build_bvh_device(want_arrays=False)
+        if args.precision:
+            sc_h.set_precision(1)
         depth_of[key] = sc_h.depth
         if key != "room":
             sc_h.set_env(env, ENV_W, ENV_H)
@@ -527,6 +529,7 @@ def run_served(args):
             "camera": "uniform on a sphere of radius 3 around the origin, looking at it, fov 45",
             "max_depth": DEPTH, "rr_from_bounce": RR, "semantics": "benchmark (mode 1), full-map environment sampling",
             "admission_budget_bytes": budget, "bvh_depth": depth_of,
+            "bvh_records": "FP16 child boxes rounded outward, 32 B" if args.precision else "FP32 child boxes, 64 B",
             "latency": "submission to film in host memory (pinned staging), host clock",
             "equal_error": "the sequential run renders the same requests with the same spp",
         },
