@@ -352,7 +352,7 @@ int enqueue_frame(mt_job* j, JobSlot& s) {
     cudaEvent_t* ev = j->kev.empty() ? nullptr : j->kev.data() + per_pass_events * p;
     if (launch_pass(s.stream, S, E, s.d_pp + p, c.mode, c.max_depth, c.film_kahan, c.width, c.height, s.d_ctrl + p,
                     s.fb, s.d_status + j->status_stride * (size_t)c.max_depth * p, j->status_stride, ctx->num_sms,
-                    ev, j->d_totals))
+                    ev, j->d_totals, j->nslots > 1))
       return fail(MT_ERR_CUDA, "pass launch: %s", cudaGetErrorString(cudaGetLastError()));
   }
   return MT_OK;

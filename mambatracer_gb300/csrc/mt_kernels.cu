@@ -461,6 +461,25 @@ int env_minb(const char* name, int dflt) {
   int x = e ? std::atoi(e) : dflt;
   return (x == 8 || x == 12 || x == 16) ? x : dflt;
 }
+// Persistent traversal grids of a shared pass, in blocks per SM (MT_TRACE_GRID /
+// MT_SHADOW_GRID; 0: half of what fits). Frames in flight run their launches
+// side by side, so a launch that leaves room on each SM lets another frame's
+// kernels run there. Measured on the 1M soup with six frames in flight (blocks
+// per SM for closest / shadow rays): 12/8 (all that fits) 613-616 Mrays/s,
+// 8/8 637, 8/4 644, 6/4 633-651, 4/4 653, 3/3 651.
+int grid_bps(const char* name, int dflt) {
+  const char* e = std::getenv(name);
+  int x = e ? std::atoi(e) : dflt;
+  return x >= 0 && x <= 32 ? x : dflt;
+}
+int trace_grid_bps() {
+  static int v = grid_bps("MT_TRACE_GRID", 0);
+  return v;
+}
+int shadow_grid_bps() {
+  static int v = grid_bps("MT_SHADOW_GRID", 0);
+  return v;
+}
 int trace_minb() {
   static int v = env_minb("MT_TRACE_MINB", kTraceMinBlocksClosest);
   return v;
@@ -488,23 +507,8 @@ int shade_blocks_per_sm(int minb) {
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shade<3>, kShadeThreads, 0);
   return n > 0 ? n : 1;
 }
-// The traversal kernels use no shared memory and read nodes, triangles and their
-// stacks through L1: they ask for the largest L1 (shared-memory carveout 0 %;
-// MT_TRACE_CARVEOUT sets another percentage, -1 leaves the driver's choice).
-// Measured on the 1M soup with six frames in flight: 637-640 Mrays/s against
-// 613-616 with the driver's choice.
 template <int MINB>
 int trace_blocks_per_sm() {
-  static int carve = [] {
-    const char* e = std::getenv("MT_TRACE_CARVEOUT");
-    return e ? std::atoi(e) : 0;
-  }();
-  if (carve >= 0 && carve <= 100) {
-    cudaFuncSetAttribute(k_trace_closest<MINB, 0>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
-    cudaFuncSetAttribute(k_trace_closest<MINB, 1>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
-    cudaFuncSetAttribute(k_trace_shadow<MINB, 0>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
-    cudaFuncSetAttribute(k_trace_shadow<MINB, 1>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
-  }
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest<MINB, 0>, kTraceThreads, 0);
   return n > 0 ? n : 1;
@@ -528,7 +532,7 @@ void launch_traces(cudaStream_t st, int grid, const DevScene& S, Ctrl* ctrl, int
 
 int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassParams* d_pp, int mode, int max_depth,
                 int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb, unsigned long long* status,
-                size_t status_stride, int num_sms, cudaEvent_t* ev, unsigned long long* totals) {
+                size_t status_stride, int num_sms, cudaEvent_t* ev, unsigned long long* totals, bool shared) {
   const int N = width * height;
   static int bps[17] = {};
   static int shade_bps[6] = {};
@@ -536,7 +540,9 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
     const int minb = closest ? trace_minb() : shadow_minb();
     if (bps[minb] == 0)
       bps[minb] = minb == 16 ? trace_blocks_per_sm<16>() : minb == 12 ? trace_blocks_per_sm<12>() : trace_blocks_per_sm<8>();
-    const int grid = std::max(1, std::min(num_sms * bps[minb], (N + kTraceThreads - 1) / kTraceThreads));
+    const int want = closest ? trace_grid_bps() : shadow_grid_bps();
+    const int per_sm = !shared ? bps[minb] : want > 0 ? std::min(want, bps[minb]) : std::max(1, bps[minb] / 2);
+    const int grid = std::max(1, std::min(num_sms * per_sm, (N + kTraceThreads - 1) / kTraceThreads));
     if (minb == 16) launch_traces<16>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
     else if (minb == 12) launch_traces<12>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
     else launch_traces<8>(st, grid, S, ctrl, b, mode, fb, kahan, closest);

@@ -24,10 +24,13 @@ struct FrameBufs {
 
 // events: optional array of 2 + 3 * max_depth events recorded around each launch.
 // totals: optional running ray counts [primary, extension, shadow, error] of the job.
+// shared: other frames or requests run beside this pass on the GPU (frames in
+// flight, served lanes): each persistent traversal launch then takes half the
+// blocks an SM can hold, leaving room for their kernels.
 int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassParams* d_pp, int mode,
                 int max_depth, int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb,
                 unsigned long long* status, size_t status_stride, int num_sms, cudaEvent_t* events,
-                unsigned long long* totals);
+                unsigned long long* totals, bool shared = false);
 
 int launch_query(cudaStream_t st, const DevScene& S, const float4* rays, int n, int any, float* t_out,
                  int* prim_out, int* work, int* err, int num_sms);

@@ -182,7 +182,7 @@ int start_request(mt_server* s, Lane& L, Request* R) {
   for (int p = 0; p < R->spp; ++p)
     if (launch_pass(L.stream, S, E, L.d_pp + p, 1, c.max_depth, c.film_kahan, R->width, R->height, L.d_ctrl + p,
                     L.fb, L.d_status + stride * (size_t)c.max_depth * p, stride, s->ctx->num_sms, nullptr,
-                    s->d_totals))
+                    s->d_totals, s->lanes.size() > 1))
       return fail(MT_ERR_CUDA, "pass launch: %s", cudaGetErrorString(cudaGetLastError()));
   CU(cudaMemcpyAsync(L.h_stage, L.fb.film, N * 16, cudaMemcpyDeviceToHost, L.stream));
   CU(cudaLaunchHostFunc(L.stream, lane_done, &L));
