@@ -505,7 +505,9 @@ int import_bvh(mt_scene* s, const int32_t* nodes, const float* bounds, int nnode
   const int n = s->ntri;
   if (nnodes != 2 * n - 1) return fail(MT_ERR_INVALID, "%d nodes for %d triangles (want 2N-1)", nnodes, n);
   auto node = [&](int i) { return nodes + 7 * (size_t)i; };
-  // BFS over interior nodes for record numbering; DFS leaf order for triangle slots.
+  // A breadth-first pass checks the tree and its depth; a depth-first pass (left
+  // before right) numbers the interior records in preorder and the leaf slots
+  // in leaf order.
   std::vector<int> rec(nnodes, -1), slot(nnodes, -1), level(nnodes, 0);
   std::vector<int> order;
   order.reserve(n);
@@ -520,7 +522,6 @@ int import_bvh(mt_scene* s, const int32_t* nodes, const float* bounds, int nnode
     while (!q.empty()) {
       int i = q.front();
       q.pop_front();
-      rec[i] = k++;
       const int32_t* nd = node(i);
       for (int c : {nd[2], nd[3]}) {
         if (c <= 0 || c >= nnodes || seen[c]) return fail(MT_ERR_INVALID, "node %d: bad child %d", i, c);
@@ -533,7 +534,6 @@ int import_bvh(mt_scene* s, const int32_t* nodes, const float* bounds, int nnode
         else if (cn[6] < 0 || cn[6] >= n) return fail(MT_ERR_INVALID, "leaf %d: bad triangle %d", c, cn[6]);
       }
     }
-    // DFS (left before right) for leaf slots
     std::vector<int> st{0};
     while (!st.empty()) {
       int i = st.back();
@@ -544,6 +544,7 @@ int import_bvh(mt_scene* s, const int32_t* nodes, const float* bounds, int nnode
         order.push_back(nd[6]);
         continue;
       }
+      rec[i] = k++;
       st.push_back(nd[3]);
       st.push_back(nd[2]);
     }

@@ -22,9 +22,11 @@
 // node's index follows from its parent's counter and its left sibling's size.
 // The result equals the host build element for element (the test compares the
 // reference-layout arrays). The traversal layout is written in the same pass:
-// interior records in breadth-first order (the order of a level's nodes by
-// their triangle range), leaf slots = the triangles' final positions (the
-// depth-first leaf order), each record holding its two children's boxes.
+// interior records in depth-first preorder (an interior node with record R and
+// a left child of k triangles has its left child at R + 1 and its right child
+// at R + k, since the left subtree holds k - 1 interior nodes), leaf slots = the
+// triangles' final positions (the depth-first leaf order), each record holding
+// its two children's boxes.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
@@ -49,6 +51,7 @@ __device__ __forceinline__ float fval(int k) { return __int_as_float(k >= 0 ? k 
 
 struct Seg {
   int node, start, end, P, depth, prec, side;  // prec: parent's record (-1 for the root), side 0 left 1 right
+  int rec;                                     // its own record when interior (preorder rank)
 };
 struct Acc {
   int mn[3], mx[3], cmn[3], cmx[3];
@@ -270,15 +273,15 @@ __global__ void k_scan_add(int* out, int n, const int* __restrict__ bsum) {
 // Per node: its split position, the link from its parent's traversal record
 // (interior nodes numbered in level order), and its children in the next level.
 __global__ void k_link(int nseg, const Seg* __restrict__ segs, const Acc* __restrict__ acc, Dec* dec,
-                       const int* __restrict__ kint, int rec_base, float4* __restrict__ recs, int nrec_cap, Seg* next,
+                       const int* __restrict__ kint, float4* __restrict__ recs, int nrec_cap, Seg* next,
                        int next_cap, int* err) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
   const Seg g = segs[s];
   Dec d = dec[s];
   const int size = g.end - g.start;
-  const int rec = rec_base + kint[s];
-  if ((d.interior && (rec >= nrec_cap || 2 * kint[s] + 1 >= next_cap)) || g.prec >= nrec_cap) {
+  const int rec = g.rec;
+  if ((d.interior && (rec < 0 || rec >= nrec_cap || 2 * kint[s] + 1 >= next_cap)) || g.prec >= nrec_cap) {
     atomicExch(err, 1);
     d.interior = 0;
     dec[s] = d;
@@ -288,8 +291,9 @@ __global__ void k_link(int nseg, const Seg* __restrict__ segs, const Acc* __rest
     const int nl = acc[s].nl;
     d.mid = (nl != 0 && nl != size) ? g.start + nl : g.start + size / 2;
     dec[s] = d;
-    next[2 * kint[s]] = Seg{g.P, g.start, d.mid, g.P + 2, g.depth + 1, rec, 0};
-    next[2 * kint[s] + 1] = Seg{g.P + 1, d.mid, g.end, g.P + 2 * (d.mid - g.start), g.depth + 1, rec, 1};
+    next[2 * kint[s]] = Seg{g.P, g.start, d.mid, g.P + 2, g.depth + 1, rec, 0, rec + 1};
+    next[2 * kint[s] + 1] =
+        Seg{g.P + 1, d.mid, g.end, g.P + 2 * (d.mid - g.start), g.depth + 1, rec, 1, rec + (d.mid - g.start)};
   }
   if (g.prec >= 0) {
     const Acc a = acc[s];
@@ -370,7 +374,7 @@ __global__ void k_quantize_fp16(const float4* __restrict__ recs, int nrec, uint4
 }
 
 __global__ void k_seed(Seg* segs, int n) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) segs[0] = Seg{0, 0, n, 1, 0, -1, 0};
+  if (blockIdx.x == 0 && threadIdx.x == 0) segs[0] = Seg{0, 0, n, 1, 0, -1, 0, 0};
 }
 
 inline unsigned blocks(size_t n) { return (unsigned)((n + kT - 1) / kT); }
@@ -459,7 +463,7 @@ extern "C" int mt_bvh_build_device(mt_scene* s, int32_t* nodes_out, float* bound
     scan_ints(st, iflag, nseg, kint, bsum, words + 1);
     k_count<<<blocks(n), kT, 0, st>>>(n, seg, obj, cen, dec, acc, flag);
     scan_ints(st, flag, n, scan, bsum, words + 2);
-    k_link<<<blocks(nseg), kT, 0, st>>>(nseg, segs, acc, dec, kint, rec_base, recs, std::max(nrec, 1), next, n,
+    k_link<<<blocks(nseg), kT, 0, st>>>(nseg, segs, acc, dec, kint, recs, std::max(nrec, 1), next, n,
                                         words + 3);
     k_scatter<<<blocks(n), kT, 0, st>>>(n, seg, obj, flag, scan, segs, dec, acc, kint, obj2, seg2);
     int interior = 0;

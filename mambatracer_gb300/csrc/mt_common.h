@@ -34,7 +34,7 @@ struct Material {
 static_assert(sizeof(Material) == 144, "Material layout");
 
 // Scene as seen by kernels. Traversal data is the GPU layout:
-//   nodes: 4 float4 per interior record (BFS order):
+//   nodes: 4 float4 per interior record (depth-first preorder, root 0):
 //     n0 = (L.min.x, L.max.x, L.min.y, L.max.y)
 //     n1 = (R.min.x, R.max.x, R.min.y, R.max.y)
 //     n2 = (L.min.z, L.max.z, R.min.z, R.max.z)
