@@ -1,0 +1,70 @@
+"""Parity at the benchmark's full sizes, through properties that hold at any size.
+
+The 1M-triangle soup and the 3.3M-triangle stadium of the benchmark:
+  * the GPU BVH build equals the host build of CNormalBVH.build (nodes element
+    for element, bounds as values), and its traversal layout equals the one
+    imported from the host build;
+  * a sample of rays hits the same triangles at the same distances as the oracle;
+  * closest hits and any-hit queries agree on every ray: nothing is hit before
+    the closest hit, and the closest hit is found by an any-hit query that
+    reaches just past it (both traversals enter a node exactly when its box
+    passes the slab test for the ray's interval);
+  * FP16 records give the same distances as FP32 records.
+"""
+import numpy as np
+import pytest
+
+from mambatracer_gb300 import api, layout, scenes
+from tests.helpers import oracle_trace
+
+pytestmark = pytest.mark.gpu
+
+
+def _check_scene(ctx, orc, sc, nrays, nsample):
+    hn, hb, hd = api.bvh_build_host(sc)
+    S = api.Scene(ctx, sc)
+    dn, db = S.build_bvh_device()
+    assert S.depth == hd <= 64
+    assert np.array_equal(dn, hn) and np.array_equal(db, hb)
+    dev = S.layout()
+    S.import_bvh(hn, hb)
+    host = S.layout()
+    assert dev[2] == host[2] and dev[0].shape == host[0].shape
+    assert np.array_equal(dev[0][:, :12], host[0][:, :12]) and dev[0][:, 12:].tobytes() == host[0][:, 12:].tobytes()
+    assert dev[1].tobytes() == host[1].tobytes()
+
+    o, d = scenes.random_rays(sc, nrays, seed=71, inside=True)
+    rays = layout.make_rays(o, d)
+    t, p = S.trace_closest(rays)
+    hit = p >= 0
+    assert hit.sum() > nrays // 10
+
+    # a sample against the oracle, bit for bit
+    idx = np.random.default_rng(72).choice(nrays, nsample, replace=False)
+    sub = np.ascontiguousarray(layout.make_rays(o[idx], d[idx]))
+    to, po = oracle_trace(orc, sc, hn, hb, sub)
+    assert np.array_equal(p[idx], po)
+    assert t[idx].tobytes() == to.tobytes()
+
+    # any-hit before the closest hit: never occluded; just past it: occluded
+    before = layout.make_rays(o, d)
+    before["tMax"] = np.where(hit, t, np.float32(np.inf))
+    assert not S.trace_any(before).any()
+    past = layout.make_rays(o[hit], d[hit])
+    past["tMax"] = t[hit] * np.float32(1.001) + np.float32(1e-6)
+    assert S.trace_any(past).all()
+
+    # FP16 records: the same distances
+    S.set_precision(1)
+    t16, p16 = S.trace_closest(rays)
+    assert t16.tobytes() == t.tobytes()
+    assert (p16 != p).sum() <= max(2, nrays // 10000)
+    S.close()
+
+
+def test_soup_1m(ctx, orc):
+    _check_scene(ctx, orc, scenes.soup(1_000_000, seed=1), 1_000_000, 20000)
+
+
+def test_stadium_3m(ctx, orc):
+    _check_scene(ctx, orc, scenes.stadium(), 500_000, 10000)
