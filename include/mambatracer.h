@@ -103,6 +103,16 @@ int mt_kernel_destroy(mt_kernel* k);
 int mt_scene_create(mt_context* ctx, const float* points, int npoints, const float* uvs, int nuvs,
                     const float* normals, int nnormals, const int32_t* faces, int nfaces,
                     const void* materials, int nmaterials, mt_scene** out);
+/* OBJ text to the mesh arrays mt_scene_create takes: what TracerAPI.initMesh
+ * (src/cl/ui/fx/main/TracerAPI.java:393-438) gets from its OBJ parser into
+ * CMesh. v / vt / vn / f (v, v/vt, v//vn, v/vt/vn; negative indices count back;
+ * polygons split into triangle fans); each distinct `o` or `g` name is the next
+ * material (faces before any name: material 0). counts_out[5] receives the
+ * numbers of points, uvs, normals, faces and materials; with the array pointers
+ * NULL only the counts are returned, otherwise points (4 floats each), uvs (2),
+ * normals (4) and faces (10 ints) are filled. No device work, no context. */
+int mt_obj_parse(const char* text, size_t len, int32_t* counts_out, float* points_out, float* uvs_out,
+                 float* normals_out, int32_t* faces_out);
 /* CNormalBVH.build (src/cl/scene/CNormalBVH.java:45-148) on the host, same
  * node layout; optional copies of nodes (7*(2N-1) ints) and bounds (8*(2N-1)
  * floats) are returned. depth_out: the BVH depth. */

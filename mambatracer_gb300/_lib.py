@@ -73,6 +73,7 @@ SIGNATURES = {
     "mt_scene_set_bvh_precision": (I, [P, I]),
     "mt_scene_set_materials": (I, [P, P, I]),
     "mt_scene_light_count": (I, [P]),
+    "mt_obj_parse": (I, [P, C.c_size_t, P, P, P, P, P]),
     "mt_scene_set_texture": (I, [P, I, I, P, I, I]),
     "mt_scene_layout_read": (I, [P, P, P, PI, PI]),
     "mt_scene_destroy": (I, [P]),

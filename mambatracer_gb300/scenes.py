@@ -7,6 +7,7 @@ generators are seeded so every run sees the same scene.
 
   box_room      the box room (36 triangles, 256 x 256, depth 4)
   textured_room the box room with texture images on the floor, a wall and the boxes
+  from_obj      a scene from Wavefront OBJ text (the library's OBJ reader)
   soup          uniform triangle soup (1M triangles) in [-1, 1]^3
   stadium       ground plane of 2M triangles plus a displaced icosphere
   sky_env       zenith-to-horizon gradient plus a Gaussian sun, lat-long FP32 RGB
@@ -189,6 +190,29 @@ def textured_room(width=128, height=96, seed=3) -> Scene:
     rough = _argb(rng.uniform(0.02, 0.9, (16, 16)), rng.uniform(0.02, 0.9, (16, 16)), np.zeros((16, 16)))
     return Scene(points=sc.points, faces=faces, materials=materials, uvs=uvs, camera=sc.camera,
                  name="textured_room", textures=[(5, 0, floor), (1, 0, wall), (3, 1, ramp), (3, 2, rough)])
+
+
+def from_obj(text: str | bytes, materials: np.ndarray | None = None, camera: np.ndarray | None = None,
+             name: str = "obj") -> Scene:
+    """A scene from Wavefront OBJ text through the library's reader (mt_obj_parse,
+    the ingest path of TracerAPI.initMesh). Each `o`/`g` name is a material; with
+    `materials` None every one is the default grey diffuse (0.75)."""
+    import ctypes as C
+
+    from ._lib import check, lib
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    counts = np.zeros(5, np.int32)
+    p = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    check(lib().mt_obj_parse(data, len(data), p(counts), None, None, None, None))
+    npt, nuv, nnr, nf, nmat = (int(x) for x in counts)
+    pts = np.zeros((max(npt, 1), 4), np.float32)
+    uvs = np.zeros((max(nuv, 1), 2), np.float32)
+    nrm = np.zeros((max(nnr, 1), 4), np.float32)
+    faces = np.zeros(nf, dtype=FACE)
+    check(lib().mt_obj_parse(data, len(data), p(counts), p(pts), p(uvs), p(nrm), p(faces)))
+    if materials is None:
+        materials = np.stack([_material((0.75, 0.75, 0.75)) for _ in range(max(nmat, 1))])
+    return Scene(points=pts, faces=faces, materials=materials, uvs=uvs, normals=nrm, camera=camera, name=name)
 
 
 def texture_tables(sc: Scene) -> tuple[np.ndarray, np.ndarray]:
