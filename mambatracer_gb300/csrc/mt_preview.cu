@@ -55,7 +55,14 @@ struct PreviewOut {  // setupBsdf's cosine, fastShade, backgroundShade, group
       const Frame f = get_frame(H.n);
       const float coeff = local_coord(f, neg(d)).z;
       const Material& P = S.materials[H.mat];
-      const float4 ec = P.emission_color, dc = P.diffuse_color;
+      const float4 ec = P.emission_color;
+      float4 dc = P.diffuse_color;
+      // textureInitPassRT, CTextureApplyPass.process, updateToTextureColorRT
+      // (Raytrace.cl:52-145): the quick colour takes the diffuse texel at the hit's uv
+      if (S.tex_on && P.isDiffuseTexture && !is_emitter(P)) {
+        const int4 t = __ldg(S.tex_ref + 4 * (size_t)H.mat);
+        dc = argb_float4(t.y > 0 ? tex_fetch(S.texels, t, H.u, H.v) : 0);
+      }
       const V c = is_emitter(P) ? mk(ec.x, ec.y, ec.z, ec.w) : muls(mk(dc.x, dc.y, dc.z, dc.w), coeff);
       argb[id] = pack_argb(c.x, c.y, c.z, 1.f);
       if (group) group[id] = H.mat;

@@ -1704,7 +1704,12 @@ void or_preview(const void* camera, int width, int height, const float* points, 
       hit_record(r, child, m, is);
       Bsdf<float> b = setup_bsdf(r.d, is, mats);
       const float coeff = b.localDirFix.z;
-      const SurfaceParameter* p = mats + is.mat;
+      SurfaceParameter tp = mats[is.mat];
+      // textureInitPassRT, CTextureApplyPass.process, updateToTextureColorRT
+      // (Raytrace.cl:52-145, CDeviceRT.java:179-182): the texture pass of the
+      // frames that follow or_set_textures
+      if (g_tex.nref > 0 && !is_emitter(&tp)) apply_textures(g_tex, is.mat, is.uv[0], is.uv[1], tp);
+      const SurfaceParameter* p = &tp;
       V4<float> c;
       if (is_emitter(p)) c = col<float>(p->emission_color);
       else c = col<float>(p->diffuse_color) * coeff;

@@ -490,6 +490,13 @@ void ref_preview(const void* camera, int width, int height, const float* points,
                         (Face*)faces, &size, (BVHNode*)nodes, (BoundingBox*)bounds);
   });
   run_serial(n, [&] { SetupBSDFRaytrace(isects.data(), rays.data(), bsdfs.data(), (Material*)materials); });
+  if (g_ref_tex.nref > 0) {  // the texture pass of CDeviceRT.loop (CDeviceRT.java:179-182)
+    std::vector<TextureData> texd(n);
+    std::memset(texd.data(), 0, sizeof(TextureData) * (size_t)n);
+    run_serial(n, [&] { textureInitPassRT(bsdfs.data(), isects.data(), texd.data()); });
+    texture_apply_process(texd.data(), n, g_ref_tex);
+    run_serial(n, [&] { updateToTextureColorRT(bsdfs.data(), texd.data()); });
+  }
   run_serial(n, [&] { backgroundShade(isects.data(), &cam, argb, rays.data(), (float4*)envmap, lg); });
   run_serial(n, [&] { fastShade(isects.data(), bsdfs.data(), argb); });
   run_serial(n, [&] { updateGroupbufferShadeImage(isects.data(), &cam, group); });

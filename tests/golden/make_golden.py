@@ -255,6 +255,14 @@ def main():
                              ptr(z), ptr(z), 1, 1, 0, ptr(tacc), ptr(tc))
     ref.lib.ref_set_textures(None, None, 0)
     out["tex_frame_accum"], out["tex_frame_counts"] = tacc, tc
+    # the preview frame of the textured room, with the preview's texture pass
+    pa = np.zeros(40 * 32, np.int32)
+    pg = np.zeros(40 * 32, np.int32)
+    ref.lib.ref_set_textures(ptr(texels), ptr(table), table.shape[0])
+    ref.lib.ref_preview(ptr(tr.camera), 40, 32, ptr(tr.points), ptr(tr.uvs), ptr(tr.normals), ptr(tr.faces),
+                        tr.ntri, ptr(tr.materials), ptr(tn), ptr(tb), ptr(z), 1, 1, 0, ptr(pa), ptr(pg))
+    ref.lib.ref_set_textures(None, None, 0)
+    out["tex_preview_argb"], out["tex_preview_group"] = pa, pg
     np.savez_compressed(OUT, **out)
     print(OUT, os.path.getsize(OUT), "bytes")
 

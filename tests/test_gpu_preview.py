@@ -12,10 +12,12 @@ from tests.helpers import bvh_build, ptr
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("which", ["room", "soup_env", "stadium_env"])
+@pytest.mark.parametrize("which", ["room", "tex_room", "soup_env", "stadium_env"])
 def test_preview_frame(ctx, orc, which):
     if which == "room":
         sc, W, H, env = scenes.box_room(96, 64), 96, 64, None
+    elif which == "tex_room":  # the preview's texture pass (textureInitPassRT .. updateToTextureColorRT)
+        sc, W, H, env = scenes.textured_room(96, 64), 96, 64, None
     elif which == "soup_env":
         sc, W, H = scenes.soup(30000, seed=7, extent=0.8, edge_sigma=0.02), 96, 64
         env = scenes.sky_env(256, 128)
@@ -32,9 +34,14 @@ def test_preview_frame(ctx, orc, which):
     argb, group = S.preview(sc.camera, W, H)
     ra = np.zeros(W * H, np.int32)
     rg = np.zeros(W * H, np.int32)
-    orc.lib.or_preview(ptr(sc.camera), W, H, ptr(sc.points), ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces), sc.ntri,
-                       ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(envmap), ew, eh, int(env is not None),
-                       ptr(ra), ptr(rg))
+    texels, table = scenes.texture_tables(sc)
+    orc.lib.or_set_textures(ptr(texels), ptr(table), table.shape[0] if sc.textures else 0)
+    try:
+        orc.lib.or_preview(ptr(sc.camera), W, H, ptr(sc.points), ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces),
+                           sc.ntri, ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(envmap), ew, eh,
+                           int(env is not None), ptr(ra), ptr(rg))
+    finally:
+        orc.lib.or_set_textures(None, None, 0)
     assert group.tobytes() == rg.tobytes()
     a = argb.view(np.uint8).reshape(-1, 4).astype(np.int32)
     b = ra.view(np.uint8).reshape(-1, 4).astype(np.int32)
@@ -50,7 +57,9 @@ def test_preview_frame(ctx, orc, which):
             "normals": plain.Buf(ctx, host=sc.normals), "faces": plain.Buf(ctx, host=sc.faces),
             "size": plain.int_buf(ctx, sc.ntri), "materials": plain.Buf(ctx, host=sc.materials),
             "nodes": plain.Buf(ctx, host=nodes), "bounds": plain.Buf(ctx, host=bounds),
-            "env": plain.Buf(ctx, host=envmap), "grid": plain.Buf(ctx, plain.GRID_BYTES)}
+            "env": plain.Buf(ctx, host=envmap), "grid": plain.Buf(ctx, plain.GRID_BYTES),
+            "tex": plain.Buf(ctx, 80 * N), "texels": plain.Buf(ctx, host=texels), "texref": plain.Buf(ctx, host=table)}
+    bufs["tex"].write(np.zeros(80 * N, np.uint8))
     hdr = np.zeros(12, np.int32)
     hdr[0], hdr[2], hdr[3] = int(env is not None), ew, eh
     bufs["grid"].write(hdr.view(np.uint8))
@@ -60,6 +69,9 @@ def test_preview_frame(ctx, orc, which):
           plain.Kernel(ctx, "IntersectPrimitives", b_["rays"], b_["isects"], b_["count"], b_["points"], b_["uvs"],
                        b_["normals"], b_["faces"], b_["size"], b_["nodes"], b_["bounds"]),
           plain.Kernel(ctx, "SetupBSDFRaytrace", b_["isects"], b_["rays"], b_["bsdfs"], b_["materials"]),
+          plain.Kernel(ctx, "textureInitPassRT", b_["bsdfs"], b_["isects"], b_["tex"]),
+          plain.Kernel(ctx, "textureApplyPass", b_["tex"], b_["count"], b_["texels"], b_["texref"]),
+          plain.Kernel(ctx, "updateToTextureColorRT", b_["bsdfs"], b_["tex"]),
           plain.Kernel(ctx, "backgroundShade", b_["isects"], b_["camera"], b_["argb"], b_["rays"], b_["env"],
                        b_["grid"]),
           plain.Kernel(ctx, "fastShade", b_["isects"], b_["bsdfs"], b_["argb"]),

@@ -258,3 +258,22 @@ def test_textured_frame(orc, ginputs, golden):
         orc.lib.or_set_textures(None, None, 0)
     assert beq(c, golden["tex_frame_counts"])
     assert beq(acc, golden["tex_frame_accum"])
+
+
+def test_textured_preview_frame(orc, ginputs, golden):
+    """The preview frame of the textured room with the preview's texture pass
+    (textureInitPassRT, CTextureApplyPass.process, updateToTextureColorRT)."""
+    from oracle.oracle import bvh_build
+    tr = ginputs["tex_room"]
+    texels, table = scenes.texture_tables(tr)
+    tn, tb, _, _ = bvh_build(orc, tr)
+    z = np.zeros(4, np.float32)
+    argb = np.zeros(40 * 32, np.int32)
+    group = np.zeros(40 * 32, np.int32)
+    orc.lib.or_set_textures(ptr(texels), ptr(table), table.shape[0])
+    try:
+        orc.lib.or_preview(ptr(tr.camera), 40, 32, ptr(tr.points), ptr(tr.uvs), ptr(tr.normals), ptr(tr.faces),
+                           tr.ntri, ptr(tr.materials), ptr(tn), ptr(tb), ptr(z), 1, 1, 0, ptr(argb), ptr(group))
+    finally:
+        orc.lib.or_set_textures(None, None, 0)
+    assert beq(argb, golden["tex_preview_argb"]) and beq(group, golden["tex_preview_group"])

@@ -216,11 +216,14 @@ def test_tonemap_frame(orc, ref):
     assert argb.tobytes() == rargb.tobytes()
 
 
-@pytest.mark.parametrize("which", ["room", "soup_env"])
+@pytest.mark.parametrize("which", ["room", "tex_room", "soup_env"])
 def test_preview_frame(orc, ref, which):
-    """The preview device's frame (Raytrace.cl): ARGB and material group per pixel."""
+    """The preview device's frame (Raytrace.cl, with its texture pass on the
+    textured room): ARGB and material group per pixel."""
     if which == "room":
         sc, W, H, env = scenes.box_room(64, 48), 64, 48, None
+    elif which == "tex_room":
+        sc, W, H, env = scenes.textured_room(64, 48), 64, 48, None
     else:
         sc, W, H = scenes.soup(20000, seed=7, extent=0.8, edge_sigma=0.02), 64, 48
         env = scenes.sky_env(256, 128)
@@ -228,12 +231,19 @@ def test_preview_frame(orc, ref, which):
     envmap = env if env is not None else np.zeros((1, 4), np.float32)
     ew, eh = (256, 128) if env is not None else (1, 1)
     out = {}
-    for name, lib, fn in (("ref", ref.lib, "ref_preview"), ("or", orc.lib, "or_preview")):
+    texels, table = scenes.texture_tables(sc)
+    ntab = table.shape[0] if sc.textures else 0
+    for name, lib, fn, st in (("ref", ref.lib, "ref_preview", "ref_set_textures"),
+                              ("or", orc.lib, "or_preview", "or_set_textures")):
         argb = np.zeros(W * H, np.int32)
         group = np.zeros(W * H, np.int32)
-        getattr(lib, fn)(ptr(sc.camera), W, H, ptr(sc.points), ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces), sc.ntri,
-                         ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(envmap), ew, eh, int(env is not None),
-                         ptr(argb), ptr(group))
+        getattr(lib, st)(ptr(texels), ptr(table), ntab)
+        try:
+            getattr(lib, fn)(ptr(sc.camera), W, H, ptr(sc.points), ptr(sc.uvs), ptr(sc.normals), ptr(sc.faces),
+                             sc.ntri, ptr(sc.materials), ptr(nodes), ptr(bounds), ptr(envmap), ew, eh,
+                             int(env is not None), ptr(argb), ptr(group))
+        finally:
+            getattr(lib, st)(None, None, 0)
         out[name] = (argb, group)
     assert out["ref"][1].tobytes() == out["or"][1].tobytes()
     assert out["ref"][0].tobytes() == out["or"][0].tobytes()
