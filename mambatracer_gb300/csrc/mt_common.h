@@ -79,6 +79,12 @@ struct DevEnv {
   float* grid_accum;
   int grid_on;
   int nu, nv, rx, ry;
+  // tabulated CDFs (dv::RegionTab) of each cell's region of the grid and of each
+  // tile's region of the map; NULL: computed from the SATs
+  const float* cell_marg;
+  const float* cell_cond;
+  const float* tile_marg;
+  const float* tile_cond;
 };
 
 // Per-pass control block in device memory (zeroed at the start of each pass).

@@ -519,27 +519,38 @@ __device__ __forceinline__ float pdf_marg(const Region& r, int y, const float* s
   float last = sat_range(r, r.minX, r.minY, last_x(r), last_y(r), sat);
   return (fi * (float)(r.sx * r.sy)) / last;
 }
+// The values the searches of sample_cont compare: the marginal CDF at row y
+// (SAT.cl:190-197) and the conditional CDF at column x of row y (SAT.cl:183-188),
+// with the region total `last` and the row integral `fi`.
+__device__ __forceinline__ float marg_value(const Region& r, int y, const float* sat, float last) {
+  return sat_range(r, r.minX, r.minY, last_x(r), y - 1, sat) / last;
+}
+__device__ __forceinline__ float cond_value(const Region& r, int x, int y, const float* sat, float fi) {
+  return sat_range(r, r.minX, y, x - 1, y, sat) / fi;
+}
 // SAT.cl:244-259, :275-290, :313-323. The region total and the chosen row's
 // integral are read once instead of at every search step (same values, same
 // divisions, so the same result as the reference's per-step recomputation).
-__device__ __forceinline__ void sample_cont(const Region& r, float u0, float u1, float* uv, int* off, float* pdf,
-                                            const float* sat, const float* f) {
+// marg(y) / cond(x, y, fi) give the CDF values: computed from the SAT, or read
+// from tables that hold the same values (RegionTab).
+template <class M, class Cd>
+__device__ __forceinline__ void sample_cont_with(const Region& r, float u0, float u1, float* uv, int* off, float* pdf,
+                                                 const float* sat, const float* f, M marg, Cd cond) {
   float p1, p0;
   const float last = sat_range(r, r.minX, r.minY, last_x(r), last_y(r), sat);
-  auto marg = [&](int y) { return sat_range(r, r.minX, r.minY, last_x(r), y - 1, sat) / last; };
   {
     int b = r.minY, e = r.minY + r.sy;
     while (b != e) {
       int mid = b + (e - b) / 2;
-      float mv = marg(mid);
+      float mv = marg(mid, last);
       bool right = !(u1 < mv);
       b = right ? mid + 1 : b;
       e = right ? e : mid;
     }
     int o = b - 1 > 0 ? b - 1 : 0;
     off[1] = o;
-    float m0 = marg(o);
-    float du = (u1 - m0) / (marg(o + 1) - marg(o));
+    float m0 = marg(o, last);
+    float du = (u1 - m0) / (marg(o + 1, last) - marg(o, last));
     const float fi = sat_range(r, r.minX, o, last_x(r), o, sat);
     p1 = (fi * (float)(r.sx * r.sy)) / last;  // pdf_marg
     uv[1] = ((float)o + du) / (float)r.nv;
@@ -547,23 +558,44 @@ __device__ __forceinline__ void sample_cont(const Region& r, float u0, float u1,
   {
     int y = off[1];
     const float fi = sat_range(r, r.minX, y, last_x(r), y, sat);
-    auto cond = [&](int x) { return sat_range(r, r.minX, y, x - 1, y, sat) / fi; };
     int b = r.minX, e = r.minX + r.sx;
     while (b != e) {
       int mid = b + (e - b) / 2;
-      float mv = cond(mid);
+      float mv = cond(mid, y, fi);
       bool right = !(u0 < mv);
       b = right ? mid + 1 : b;
       e = right ? e : mid;
     }
     int o = b - 1 > 0 ? b - 1 : 0;
     off[0] = o;
-    float c0 = cond(o);
-    float du = (u0 - c0) / (cond(o + 1) - cond(o));
+    float c0 = cond(o, y, fi);
+    float du = (u0 - c0) / (cond(o + 1, y, fi) - cond(o, y, fi));
     p0 = func_at(r, o, y, f) / fi;  // pdf_cond
     uv[0] = ((float)o + du) / (float)r.nu;
   }
   pdf[0] = p0 * p1;
+}
+__device__ __forceinline__ void sample_cont(const Region& r, float u0, float u1, float* uv, int* off, float* pdf,
+                                            const float* sat, const float* f) {
+  sample_cont_with(r, u0, u1, uv, off, pdf, sat, f, [&](int y, float last) { return marg_value(r, y, sat, last); },
+                   [&](int x, int y, float fi) { return cond_value(r, x, y, sat, fi); });
+}
+// Tabulated CDFs of a region, the values marg_value / cond_value give, computed
+// once (k_region_tables): marg for rows y = minY-1 .. minY+sy (sy + 2 values),
+// cond for rows y = minY-1 .. minY+sy-1, each for columns x = minX-1 .. minX+sx
+// (sx + 2 values). The searches then read short contiguous arrays instead of
+// four scattered SAT entries per step. Rows and columns one before the region
+// serve the searches' edge case (the first row or column chosen, o = b - 1).
+struct RegionTab {
+  const float* marg;
+  const float* cond;
+};
+__device__ __forceinline__ void sample_cont_tab(const Region& r, float u0, float u1, float* uv, int* off, float* pdf,
+                                                const float* sat, const float* f, RegionTab t) {
+  const int cw = r.sx + 2;
+  sample_cont_with(
+      r, u0, u1, uv, off, pdf, sat, f, [&](int y, float) { return __ldg(t.marg + (y - r.minY + 1)); },
+      [&](int x, int y, float) { return __ldg(t.cond + (size_t)(y - r.minY + 1) * cw + (x - r.minX + 1)); });
 }
 
 // Util.cl:397-439
@@ -655,16 +687,28 @@ __device__ __forceinline__ Region env_tile_region(const DevEnv& E, int tx, int t
 }
 __device__ __forceinline__ V illuminate_env_grid(const DevEnv& E, const float* cam, V p, V s, V* dir, float* dist,
                                                  float* pdfW) {
-  const size_t base = grid_cell_base(E, grid_cell(E, cam, p));
+  const int cell = grid_cell(E, cam, p);
+  const size_t base = grid_cell_base(E, cell);
   const Region rc{E.nu, E.nv, 0, 0, E.rx, E.ry};
   float uvLL[2], pdfLL, uvSS[2], pdfSS;
   int offLL[2], offSS[2];
-  sample_cont(rc, s.x, s.y, uvLL, offLL, &pdfLL, E.grid_sat + base, E.grid_func + base);
+  if (E.cell_marg)  // tables of the cell's CDFs
+    sample_cont_tab(rc, s.x, s.y, uvLL, offLL, &pdfLL, E.grid_sat + base, E.grid_func + base,
+                    RegionTab{E.cell_marg + (size_t)cell * (E.ry + 2),
+                              E.cell_cond + (size_t)cell * (E.ry + 1) * (E.rx + 2)});
+  else
+    sample_cont(rc, s.x, s.y, uvLL, offLL, &pdfLL, E.grid_sat + base, E.grid_func + base);
   *dist = kFloatMax;
   *pdfW = 0.f;
   if (!(pdfLL > 0.f)) return zero4();  // empty cell: the BSDF sample covers it alone
   const Region rt = env_tile_region(E, offLL[0], offLL[1]);
-  sample_cont(rt, s.z, s.w, uvSS, offSS, &pdfSS, E.sat, E.lum);
+  if (E.tile_marg) {  // tables of the tile's CDFs (tiles divide the map: every tile is tw x th)
+    const int tw = E.w / E.rx, th = E.h / E.ry, tile = offLL[1] * E.rx + offLL[0];
+    sample_cont_tab(rt, s.z, s.w, uvSS, offSS, &pdfSS, E.sat, E.lum,
+                    RegionTab{E.tile_marg + (size_t)tile * (th + 2), E.tile_cond + (size_t)tile * (th + 1) * (tw + 2)});
+  } else {
+    sample_cont(rt, s.z, s.w, uvSS, offSS, &pdfSS, E.sat, E.lum);
+  }
   if (!(pdfSS > 0.f)) return zero4();
   V d = sph_dir(uvSS[0], uvSS[1]);
   *dir = d;

@@ -142,7 +142,88 @@ __global__ void k_grid_init_func(const double* __restrict__ sat64, const float* 
   func[i] = v;
 }
 
+// CDF tables (dv::RegionTab) of n regions of size sx x sy, one thread per value:
+// region k's values are marg for rows minY-1 .. minY+sy, then cond for rows
+// minY-1 .. minY+sy-1 and columns minX-1 .. minX+sx, computed by the functions
+// the sampler uses, so a table value equals the value it replaces.
+template <class RegionOf>
+__global__ void k_region_tables(int n, int sx, int sy, RegionOf region_of, float* marg, float* cond) {
+  const size_t per = (size_t)(sy + 2) + (size_t)(sy + 1) * (sx + 2);
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= per * (size_t)n) return;
+  const int k = (int)(i / per);
+  const size_t e = i % per;
+  const float* sat;
+  const dv::Region r = region_of(k, &sat);
+  const float last = dv::sat_range(r, r.minX, r.minY, dv::last_x(r), dv::last_y(r), sat);
+  if (e < (size_t)(sy + 2)) {
+    marg[(size_t)k * (sy + 2) + e] = dv::marg_value(r, r.minY - 1 + (int)e, sat, last);
+  } else {
+    const size_t e2 = e - (sy + 2);
+    const int row = (int)(e2 / (sx + 2)), col = (int)(e2 % (sx + 2));
+    const int y = r.minY - 1 + row, x = r.minX - 1 + col;
+    const float fi = dv::sat_range(r, r.minX, y, dv::last_x(r), y, sat);
+    cond[(size_t)k * (sy + 1) * (sx + 2) + e2] = dv::cond_value(r, x, y, sat, fi);
+  }
+}
+// the rx x ry tiles of the w x h map (tile ty * rx + tx), on the map's FP32 SAT
+struct TileRegions {
+  DevEnv E;
+  const float* sat;
+  __device__ dv::Region operator()(int k, const float** s) const {
+    *s = sat;
+    return dv::env_tile_region(E, k % E.rx, k / E.rx);
+  }
+};
+// the cells of the grid, each its own rx x ry SAT at its first tile
+struct CellRegions {
+  DevEnv E;
+  const float* sat;
+  __device__ dv::Region operator()(int k, const float** s) const {
+    *s = sat + dv::grid_cell_base(E, k);
+    return dv::Region{E.nu, E.nv, 0, 0, E.rx, E.ry};
+  }
+};
+
 }  // namespace
+
+size_t tile_table_floats(int w, int h, int rx, int ry, size_t* marg_floats) {
+  const int tw = w / rx, th = h / ry;
+  *marg_floats = (size_t)rx * ry * (th + 2);
+  return (size_t)rx * ry * (th + 1) * (tw + 2);
+}
+size_t cell_table_floats(int nu, int nv, int rx, int ry, size_t* marg_floats) {
+  const size_t cells = (size_t)(nu / rx) * (nv / ry);
+  *marg_floats = cells * (ry + 2);
+  return cells * (ry + 1) * (rx + 2);
+}
+
+int launch_tile_tables(cudaStream_t st, const float* sat, int w, int h, int rx, int ry, float* marg, float* cond) {
+  if (w % rx || h % ry) return -1;
+  DevEnv E{};
+  E.w = w;
+  E.h = h;
+  E.rx = rx;
+  E.ry = ry;
+  const int tw = w / rx, th = h / ry, n = rx * ry;
+  const size_t total = (size_t)n * ((th + 2) + (size_t)(th + 1) * (tw + 2));
+  k_region_tables<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(n, tw, th, TileRegions{E, sat}, marg, cond);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_cell_tables(cudaStream_t st, const float* grid_sat, int nu, int nv, int rx, int ry, float* marg,
+                       float* cond) {
+  if (nu % rx || nv % ry) return -1;
+  DevEnv E{};
+  E.nu = nu;
+  E.nv = nv;
+  E.rx = rx;
+  E.ry = ry;
+  const int n = (nu / rx) * (nv / ry);
+  const size_t total = (size_t)n * ((ry + 2) + (size_t)(ry + 1) * (rx + 2));
+  k_region_tables<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(n, rx, ry, CellRegions{E, grid_sat}, marg, cond);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
 
 int launch_grid_init(cudaStream_t st, const double* sat64, const float* sat32, int w, int h, int nu, int nv, int rx,
                      int ry, float* func) {

@@ -200,6 +200,10 @@ struct mt_job {
   float* d_grid_sat = nullptr;
   float* d_grid_accum = nullptr;
   double* d_grid_sat64 = nullptr;
+  // CDF tables of the grid-guided sampling: per cell (rebuilt with the cells'
+  // SATs) and per tile of the map
+  float *d_cell_marg = nullptr, *d_cell_cond = nullptr, *d_tile_marg = nullptr, *d_tile_cond = nullptr;
+  int grid_tables = 1;
   int grid_frames = 0;           // frames that have accumulated into the grid since it was set up
   cudaEvent_t grid_ev = nullptr;  // recorded after the last grid update
   // displayed image (mt_image_argb), allocated on first use

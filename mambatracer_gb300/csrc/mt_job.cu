@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 
@@ -126,6 +127,10 @@ void free_job(mt_job* j) {
   dfree(j->d_grid_sat);
   dfree(j->d_grid_accum);
   dfree(j->d_grid_sat64);
+  dfree(j->d_cell_marg);
+  dfree(j->d_cell_cond);
+  dfree(j->d_tile_marg);
+  dfree(j->d_tile_cond);
   dfree(j->d_argb);
   dfree(j->d_fb);
   dfree(j->d_tone_part);
@@ -203,9 +208,16 @@ int setup_grid(mt_job* j) {
     dfree(j->d_grid_sat);
     dfree(j->d_grid_accum);
     dfree(j->d_grid_sat64);
+    dfree(j->d_cell_marg);
+    dfree(j->d_cell_cond);
+    dfree(j->d_tile_marg);
+    dfree(j->d_tile_cond);
     j->grid_on = 0;
   }
   j->grid_frames = 0;
+  // MT_GRID_TABLES=0: sample from the SATs directly (the tables hold the same values)
+  const char* tv = std::getenv("MT_GRID_TABLES");
+  j->grid_tables = !(tv && std::atoi(tv) == 0);
   if (!want) return MT_OK;
   if (sc->env_w % sc->grid_rx || sc->env_h % sc->grid_ry)
     return fail(MT_ERR_INVALID, "light-grid tiles (%d x %d) must divide the %d x %d environment map", sc->grid_rx,
@@ -222,13 +234,23 @@ int setup_grid(mt_job* j) {
     if (!r) r = dalloc(&j->d_grid_sat, n);
     if (!r) r = dalloc(&j->d_grid_accum, n);
     if (!r && j->grid_fp64) r = dalloc(&j->d_grid_sat64, n);
+    size_t cm = 0, tm = 0;
+    const size_t cc = cell_table_floats(j->nu, j->nv, j->rx, j->ry, &cm);
+    const size_t tc = tile_table_floats(sc->env_w, sc->env_h, j->rx, j->ry, &tm);
+    if (!r) r = dalloc(&j->d_cell_marg, cm);
+    if (!r) r = dalloc(&j->d_cell_cond, cc);
+    if (!r) r = dalloc(&j->d_tile_marg, tm);
+    if (!r) r = dalloc(&j->d_tile_cond, tc);
     if (r) return r;
   }
   CU(cudaMemsetAsync(j->d_grid_accum, 0, n * 4, ctx->stream));
   if (launch_grid_init(ctx->stream, sc->d_env_sat64, sc->d_env_sat, sc->env_w, sc->env_h, j->nu, j->nv, j->rx, j->ry,
                        j->d_grid_func) ||
       launch_grid_sat(ctx->stream, j->d_grid_func, j->d_grid_sat, j->d_grid_sat64, j->nu, j->nv, j->rx, j->ry,
-                      j->grid_fp64))
+                      j->grid_fp64) ||
+      launch_cell_tables(ctx->stream, j->d_grid_sat, j->nu, j->nv, j->rx, j->ry, j->d_cell_marg, j->d_cell_cond) ||
+      launch_tile_tables(ctx->stream, sc->d_env_sat, sc->env_w, sc->env_h, j->rx, j->ry, j->d_tile_marg,
+                         j->d_tile_cond))
     return fail(MT_ERR_CUDA, "light-grid set-up launch: %s", cudaGetErrorString(cudaGetLastError()));
   j->grid_on = 1;
   return MT_OK;
@@ -337,6 +359,12 @@ int enqueue_frame(mt_job* j, JobSlot& s) {
     E.nv = j->nv;
     E.rx = j->rx;
     E.ry = j->ry;
+    if (j->grid_tables) {
+      E.cell_marg = j->d_cell_marg;
+      E.cell_cond = j->d_cell_cond;
+      E.tile_marg = j->d_tile_marg;
+      E.tile_cond = j->d_tile_cond;
+    }
   }
   const size_t per_pass_events = 2 + 3 * (size_t)c.max_depth;
   if (j->nslots > 1) {
@@ -430,7 +458,8 @@ extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_coun
     const size_t n = (size_t)j->nu * j->nv;
     CU(cudaMemcpyAsync(j->d_grid_func, j->d_grid_accum, n * 4, cudaMemcpyDeviceToDevice, s.stream));
     if (launch_grid_sat(s.stream, j->d_grid_func, j->d_grid_sat, j->d_grid_sat64, j->nu, j->nv, j->rx, j->ry,
-                        j->grid_fp64))
+                        j->grid_fp64) ||
+        launch_cell_tables(s.stream, j->d_grid_sat, j->nu, j->nv, j->rx, j->ry, j->d_cell_marg, j->d_cell_cond))
       return fail(MT_ERR_CUDA, "light-grid update launch: %s", cudaGetErrorString(cudaGetLastError()));
     CU(cudaEventRecord(j->grid_ev, s.stream));
     ++j->grid_frames;

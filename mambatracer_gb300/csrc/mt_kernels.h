@@ -47,5 +47,14 @@ int launch_grid_sat(cudaStream_t st, const float* func, float* sat32, double* sa
 // the tile (from sat64 when not NULL, else sat32).
 int launch_grid_init(cudaStream_t st, const double* sat64, const float* sat32, int w, int h, int nu, int nv, int rx,
                      int ry, float* func);
+// CDF tables of the grid-guided environment sampling (dv::RegionTab): for the
+// rx x ry tiles of the map (from its FP32 SAT) and for the grid's cells (from
+// the per-cell SATs). *_floats return the cond table's size and the marg table's
+// through *marg_floats.
+size_t tile_table_floats(int w, int h, int rx, int ry, size_t* marg_floats);
+size_t cell_table_floats(int nu, int nv, int rx, int ry, size_t* marg_floats);
+int launch_tile_tables(cudaStream_t st, const float* sat, int w, int h, int rx, int ry, float* marg, float* cond);
+int launch_cell_tables(cudaStream_t st, const float* grid_sat, int nu, int nv, int rx, int ry, float* marg,
+                       float* cond);
 
 }  // namespace mt

@@ -91,6 +91,27 @@ def test_accumulation_and_update(ctx, orc):
     S.close()
 
 
+@pytest.mark.parametrize("enable", [1, 2])
+def test_cdf_tables_give_the_same_samples(ctx, orc, monkeypatch, enable):
+    """The grid-guided sampler reads its searches' CDF values from tables built
+    once per cell and per tile; sampling straight from the SATs (MT_GRID_TABLES=0)
+    gives byte-identical films, so the tables hold exactly the values they
+    replace (frozen grid: no float-atomic accumulation between the two runs)."""
+    sc, S, nodes, bounds, env = setup(ctx, orc, enable=enable)
+    films = {}
+    for tables in ("0", "1"):
+        monkeypatch.setenv("MT_GRID_TABLES", tables)
+        J = api.Job(ctx, S, W, H, max_depth=DEPTH, mode=1, rr_depth=3, film_kahan=1, grid_updates=0)
+        J.set_camera(sc.camera)
+        for f in range(3):
+            J.render(None, float(f + 1))
+        films[tables] = (J.film(), J.stats()[0])
+        J.close()
+    assert films["0"][0].tobytes() == films["1"][0].tobytes()
+    assert np.array_equal(films["0"][1], films["1"][1])
+    S.close()
+
+
 def test_grid_and_full_map_estimate_the_same_image(ctx, orc):
     sc, S, nodes, bounds, env = setup(ctx, orc, ntri=5000)
     means = {}
