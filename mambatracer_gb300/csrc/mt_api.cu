@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -260,8 +261,28 @@ void free_scene(mt_scene* s) {
   dfree(s->d_env_lum);
   dfree(s->d_env_sat);
   dfree(s->d_env_sat64);
+  dfree(s->d_env_marg);
+  dfree(s->d_env_cond);
   dfree(s->d_texels);
   dfree(s->d_tex_ref);
+}
+
+// CDF tables of the whole map for full-map environment sampling, from its FP32 SAT.
+int build_env_tables(mt_scene* s) {
+  dfree(s->d_env_marg);
+  dfree(s->d_env_cond);
+  if (!cdf_tables_enabled()) return MT_OK;
+  size_t m = 0;
+  const size_t c = map_table_floats(s->env_w, s->env_h, &m);
+  int r = dalloc(&s->d_env_marg, m);
+  if (!r) r = dalloc(&s->d_env_cond, c);
+  if (!r && launch_map_tables(s->ctx->stream, s->d_env_sat, s->env_w, s->env_h, s->d_env_marg, s->d_env_cond))
+    r = fail(MT_ERR_CUDA, "environment tables: %s", cudaGetErrorString(cudaGetLastError()));
+  if (r) {
+    dfree(s->d_env_marg);
+    dfree(s->d_env_cond);
+  }
+  return r;
 }
 
 // Texel pool (all images back to back) and the per-material table of
@@ -379,6 +400,11 @@ extern "C" int mt_scene_set_texture(mt_scene* s, int material, int kind, const i
     t = mt_scene::HostTex{};
   }
   return upload_textures(s);
+}
+
+bool cdf_tables_enabled() {
+  const char* v = std::getenv("MT_CDF_TABLES");
+  return !(v && std::atoi(v) == 0);
 }
 
 extern "C" int mt_scene_light_count(const mt_scene* s) { return s ? s->nlights : -1; }
@@ -699,9 +725,10 @@ extern "C" int mt_env_set(mt_scene* s, const float* rgb, int w, int h) {
   if (r) return r;
   if (launch_env_build(s->ctx->stream, s->d_env_rgb, w, h, s->d_env_lum, s->d_env_sat64, s->d_env_sat))
     return fail(MT_ERR_CUDA, "environment build launch: %s", cudaGetErrorString(cudaGetLastError()));
-  CU(cudaStreamSynchronize(s->ctx->stream));
   s->env_w = w;
   s->env_h = h;
+  if ((r = build_env_tables(s))) return r;
+  CU(cudaStreamSynchronize(s->ctx->stream));
   s->env_present = 1;
   return MT_OK;
 }
@@ -721,6 +748,8 @@ extern "C" int mt_env_set_with_sat(mt_scene* s, const float* rgb, const float* l
   dfree(s->d_env_sat64);
   s->env_w = w;
   s->env_h = h;
+  if ((r = build_env_tables(s))) return r;
+  CU(cudaStreamSynchronize(s->ctx->stream));
   s->env_present = 1;
   return MT_OK;
 }

@@ -85,6 +85,9 @@ struct DevEnv {
   const float* cell_cond;
   const float* tile_marg;
   const float* tile_cond;
+  // the same for the whole map (full-map sampling); NULL: from the SAT
+  const float* env_marg;
+  const float* env_cond;
 };
 
 // Per-pass control block in device memory (zeroed at the start of each pass).

@@ -622,7 +622,10 @@ __device__ __forceinline__ V illuminate_env(const DevEnv& E, V s, V* dir, float*
   float uv[2];
   int off[2];
   float pdf;
-  sample_cont(r, s.x, s.y, uv, off, &pdf, E.sat, E.lum);
+  if (E.env_marg)  // tables of the map's CDFs
+    sample_cont_tab(r, s.x, s.y, uv, off, &pdf, E.sat, E.lum, RegionTab{E.env_marg, E.env_cond});
+  else
+    sample_cont(r, s.x, s.y, uv, off, &pdf, E.sat, E.lum);
   V d = sph_dir(uv[0], uv[1]);
   *dir = d;
   int x, y;

@@ -187,6 +187,22 @@ struct CellRegions {
 
 }  // namespace
 
+size_t map_table_floats(int w, int h, size_t* marg_floats) {
+  *marg_floats = (size_t)h + 2;
+  return (size_t)(h + 1) * (w + 2);
+}
+
+int launch_map_tables(cudaStream_t st, const float* sat, int w, int h, float* marg, float* cond) {
+  DevEnv E{};
+  E.w = w;
+  E.h = h;
+  E.rx = 1;
+  E.ry = 1;
+  const size_t total = (size_t)(h + 2) + (size_t)(h + 1) * (w + 2);
+  k_region_tables<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(1, w, h, TileRegions{E, sat}, marg, cond);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 size_t tile_table_floats(int w, int h, int rx, int ry, size_t* marg_floats) {
   const int tw = w / rx, th = h / ry;
   *marg_floats = (size_t)rx * ry * (th + 2);

@@ -97,6 +97,8 @@ struct mt_scene {
   float* d_env_lum = nullptr;
   float* d_env_sat = nullptr;
   double* d_env_sat64 = nullptr;
+  float* d_env_marg = nullptr;  // CDF tables of the whole map (dv::RegionTab)
+  float* d_env_cond = nullptr;
   int env_w = 0, env_h = 0, env_present = 0;
   int grid_nu = 1600, grid_nv = 1600, grid_rx = 16, grid_ry = 32, grid_on = 0;  // grid_on: 0, 1 FP32, 2 FP64 SAT
   // textures: host images per (material, kind), the device pool and table
@@ -141,6 +143,8 @@ struct mt_scene {
     e.h = env_h;
     e.present = env_present;
     e.grid_on = 0;
+    e.env_marg = d_env_marg;
+    e.env_cond = d_env_cond;
     return e;
   }
 };
@@ -230,3 +234,6 @@ int quiesce(mt_context* ctx);
 void servers_sync(mt_context* ctx);
 // Rebuild (precision 1) or drop the scene's FP16 records from its FP32 records.
 int refresh_qnodes(mt_scene* s);
+// MT_CDF_TABLES=0 turns the CDF tables of environment sampling off (the samplers
+// then search the SATs directly; the tables hold the same values).
+bool cdf_tables_enabled();

@@ -215,9 +215,7 @@ int setup_grid(mt_job* j) {
     j->grid_on = 0;
   }
   j->grid_frames = 0;
-  // MT_GRID_TABLES=0: sample from the SATs directly (the tables hold the same values)
-  const char* tv = std::getenv("MT_GRID_TABLES");
-  j->grid_tables = !(tv && std::atoi(tv) == 0);
+  j->grid_tables = cdf_tables_enabled();
   if (!want) return MT_OK;
   if (sc->env_w % sc->grid_rx || sc->env_h % sc->grid_ry)
     return fail(MT_ERR_INVALID, "light-grid tiles (%d x %d) must divide the %d x %d environment map", sc->grid_rx,

@@ -52,6 +52,8 @@ int launch_grid_init(cudaStream_t st, const double* sat64, const float* sat32, i
 // the per-cell SATs). *_floats return the cond table's size and the marg table's
 // through *marg_floats.
 size_t tile_table_floats(int w, int h, int rx, int ry, size_t* marg_floats);
+size_t map_table_floats(int w, int h, size_t* marg_floats);
+int launch_map_tables(cudaStream_t st, const float* sat, int w, int h, float* marg, float* cond);
 size_t cell_table_floats(int nu, int nv, int rx, int ry, size_t* marg_floats);
 int launch_tile_tables(cudaStream_t st, const float* sat, int w, int h, int rx, int ry, float* marg, float* cond);
 int launch_cell_tables(cudaStream_t st, const float* grid_sat, int nu, int nv, int rx, int ry, float* marg,

@@ -94,13 +94,13 @@ def test_accumulation_and_update(ctx, orc):
 @pytest.mark.parametrize("enable", [1, 2])
 def test_cdf_tables_give_the_same_samples(ctx, orc, monkeypatch, enable):
     """The grid-guided sampler reads its searches' CDF values from tables built
-    once per cell and per tile; sampling straight from the SATs (MT_GRID_TABLES=0)
+    once per cell and per tile; sampling straight from the SATs (MT_CDF_TABLES=0)
     gives byte-identical films, so the tables hold exactly the values they
     replace (frozen grid: no float-atomic accumulation between the two runs)."""
     sc, S, nodes, bounds, env = setup(ctx, orc, enable=enable)
     films = {}
     for tables in ("0", "1"):
-        monkeypatch.setenv("MT_GRID_TABLES", tables)
+        monkeypatch.setenv("MT_CDF_TABLES", tables)
         J = api.Job(ctx, S, W, H, max_depth=DEPTH, mode=1, rr_depth=3, film_kahan=1, grid_updates=0)
         J.set_camera(sc.camera)
         for f in range(3):
@@ -110,6 +110,29 @@ def test_cdf_tables_give_the_same_samples(ctx, orc, monkeypatch, enable):
     assert films["0"][0].tobytes() == films["1"][0].tobytes()
     assert np.array_equal(films["0"][1], films["1"][1])
     S.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_map_cdf_tables_give_the_same_samples(ctx, orc, monkeypatch, mode):
+    """Full-map environment sampling (grid off; reference semantics always sample
+    the full map) searches tables of the map's CDFs built when the environment
+    is set; without them (MT_CDF_TABLES=0 when the map is set) the films are
+    byte-identical."""
+    depth = 4
+    seeds = np.random.default_rng(11).integers(2 ** 29, 2 ** 30, size=2 * (1 + 2 * depth)).astype(np.int32)
+    films = {}
+    for tables in ("0", "1"):
+        monkeypatch.setenv("MT_CDF_TABLES", tables)
+        sc, S, nodes, bounds, env = setup(ctx, orc, enable=0)
+        J = api.Job(ctx, S, W, H, max_depth=depth, mode=mode, rr_depth=3, film_kahan=1)
+        J.set_camera(sc.camera)
+        for f in range(2):
+            J.render(seeds if mode == 0 else None, float(f + 1))
+        films[tables] = (J.film(), J.stats()[0])
+        J.close()
+        S.close()
+    assert films["0"][0].tobytes() == films["1"][0].tobytes()
+    assert np.array_equal(films["0"][1], films["1"][1])
 
 
 def test_grid_and_full_map_estimate_the_same_image(ctx, orc):
