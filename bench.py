@@ -663,7 +663,7 @@ def main():
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
                     help="BVH records: 0 FP32 child boxes (64 B), 1 FP16 outward-rounded (32 B)")
     ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS) + ["batched", "served", "plain"])
-    ap.add_argument("--lanes", type=int, default=16, help="batched/served: requests in flight")
+    ap.add_argument("--lanes", type=int, default=8, help="batched/served: requests in flight")
     ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="served: seconds of arrivals")
     args = ap.parse_args()
