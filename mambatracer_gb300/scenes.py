@@ -25,7 +25,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .layout import FACE, MATERIAL, default_material, make_camera
+from .layout import FACE, default_material, make_camera
 
 
 @dataclass
