@@ -326,6 +326,28 @@ typedef struct mt_served_stats {
   double span_ms;   /* first submission to last completion */
 } mt_served_stats;
 int mt_server_create(mt_context* ctx, const mt_server_config* cfg, mt_server** out);
+
+/* ------------------------------------------------------- merged batches */
+
+/* One frame of a merged batch: size, passes, the first pass's frame number
+ * (pass p renders frame frame_count + p, as mt_render_frame numbers a job's
+ * passes) and its CameraStruct (64 B, src/cl/kernel/Util.cl:78-85). */
+typedef struct {
+  int width, height, spp;
+  float frame_count;
+  unsigned char camera[64];
+} mt_batch_frame;
+/* Render n frames of uneven size of one scene through one set of wavefront
+ * queues (benchmark semantics, full-map environment sampling): each bounce is
+ * one launch per kernel for all frames still rendering. No reference
+ * counterpart (the reference renders one frame at a time); each frame's film
+ * equals the frame rendered alone by a job or a served request with the same
+ * camera, size, spp, frame number and path settings, bit for bit.
+ * films_out: the frames' float4 films back to back in frame order (sum over
+ * the frame's passes, not divided); rays_out (may be NULL): [primary,
+ * extension, shadow] rays traced. Synchronous; allocates its queues per call. */
+int mt_batch_render(mt_context* ctx, mt_scene* scene, const mt_batch_frame* frames, int nframes, int max_depth,
+                    int rr_depth, int film_kahan, float* films_out, int64_t* rays_out);
 /* Cancels queued requests, waits for running ones, frees the lanes. */
 int mt_server_destroy(mt_server* server);
 /* Queues a request; film_out (width * height float4, pinned or pageable host

@@ -29,6 +29,12 @@ class RenderConfig(C.Structure):
                 ("grid_updates", C.c_int)]
 
 
+class BatchFrame(C.Structure):
+    """mt_batch_frame"""
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("spp", C.c_int), ("frame_count", C.c_float),
+                ("camera", C.c_ubyte * 64)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("lanes", C.c_int), ("max_width", C.c_int), ("max_height", C.c_int), ("max_spp", C.c_int),
                 ("max_depth", C.c_int), ("rr_depth", C.c_int), ("film_kahan", C.c_int), ("pad_", C.c_int),
@@ -73,6 +79,7 @@ SIGNATURES = {
     "mt_scene_set_bvh_precision": (I, [P, I]),
     "mt_scene_set_materials": (I, [P, P, I]),
     "mt_scene_light_count": (I, [P]),
+    "mt_batch_render": (I, [P, P, P, I, I, I, I, P, P]),
     "mt_obj_parse": (I, [P, C.c_size_t, P, P, P, P, P]),
     "mt_scene_set_texture": (I, [P, I, I, P, I, I]),
     "mt_scene_layout_read": (I, [P, P, P, PI, PI]),

@@ -13,7 +13,7 @@ import threading
 import numpy as np
 
 from . import layout
-from ._lib import RenderConfig, ServedStats, ServerConfig, check, lib
+from ._lib import BatchFrame, RenderConfig, ServedStats, ServerConfig, check, lib
 
 
 def _p(a):
@@ -412,3 +412,24 @@ class Server:
             check(lib().mt_server_destroy(self.h))
             self.h = None
 
+
+
+def batch_render(ctx: Context, scene: Scene, frames, max_depth: int = 8, rr_depth: int = 3, film_kahan: int = 1):
+    """Frames of one scene through one set of wavefront queues (mt_batch_render).
+    frames: (camera, width, height, spp, frame_count) each. Returns the films
+    (float32 [w * h, 4] each, summed over the frame's passes) and the ray counts."""
+    arr = (BatchFrame * len(frames))()
+    for f, (cam, w, h, spp, fc) in zip(arr, frames):
+        c = np.array(cam, copy=True).reshape(-1)[:1]
+        f.width, f.height, f.spp, f.frame_count = int(w), int(h), int(spp), float(fc)
+        C.memmove(f.camera, np.frombuffer(c.tobytes(), np.uint8).ctypes.data, 64)
+    sizes = [int(w) * int(h) for _, w, h, _, _ in frames]
+    out = np.zeros((sum(sizes), 4), np.float32)
+    rays = np.zeros(3, np.int64)
+    check(lib().mt_batch_render(ctx.h, scene.h, C.cast(arr, C.c_void_p), len(frames), max_depth, rr_depth, film_kahan,
+                                _p(out), _p(rays)))
+    films, off = [], 0
+    for n in sizes:
+        films.append(out[off:off + n])
+        off += n
+    return films, rays

@@ -49,11 +49,8 @@ __device__ __forceinline__ void film_add(float4* __restrict__ acc, float4* __res
 // InitCameraRayDataJitter (src/cl/kernel/Initialize.cl:129-172) with the
 // per-frame camera constants precomputed on the host, plus the path and queue
 // resets of InitPathData / InitIntersection / InitIntDataToIndex.
-__global__ void k_raygen(const PassParams* __restrict__ pp, Ctrl* ctrl, FrameBufs fb) {
-  const int N = pp->width * pp->height;
-  const int id = blockIdx.x * blockDim.x + threadIdx.x;
-  if (id == 0) ctrl->count[1] = N;
-  if (id >= N) return;
+// The camera ray of pixel id (InitCameraRayDataJitter): origin, world direction.
+__device__ __forceinline__ void camera_ray(const PassParams* __restrict__ pp, int id, V* o_out, V* d_out) {
   int32_t sx, sy;
   if (pp->mode == 0) {
     sx = pp->seeds[0];
@@ -75,11 +72,25 @@ __global__ void k_raygen(const PassParams* __restrict__ pp, Ctrl* ctrl, FrameBuf
   V o = mk(dot3(m0, z) + m0.w, dot3(m1, z) + m1.w, dot3(m2, z) + m2.w, dot3(m3, z) + m3.w);
   if (!(o.w == 1.f)) o = mk(o.x / o.w, o.y / o.w, o.z / o.w, 0.f);
   V dw = mk(dot4(m0, d), dot4(m1, d), dot4(m2, d), 0.f);
-  fb.q_o[0][id] = mk(o.x, o.y, o.z, __int_as_float(id));
-  fb.q_d[0][id] = mk(dw.x, dw.y, dw.z, 0.f);
-  fb.thr[id] = mk(1.f, 1.f, 1.f, 1.f);
-  fb.ps[id] = mk(0.f, 0.f, 0.f, 1.f);  // hitpoint.xyz, lastPdfW
-  fb.flag[id] = 1;                     // lastSpecular
+  *o_out = o;
+  *d_out = dw;
+}
+// Queue slot and path state g of a new path (InitPathData).
+__device__ __forceinline__ void start_path(FrameBufs& fb, int g, V o, V dw) {
+  fb.q_o[0][g] = mk(o.x, o.y, o.z, __int_as_float(g));
+  fb.q_d[0][g] = mk(dw.x, dw.y, dw.z, 0.f);
+  fb.thr[g] = mk(1.f, 1.f, 1.f, 1.f);
+  fb.ps[g] = mk(0.f, 0.f, 0.f, 1.f);  // hitpoint.xyz, lastPdfW
+  fb.flag[g] = 1;                     // lastSpecular
+}
+__global__ void k_raygen(const PassParams* __restrict__ pp, Ctrl* ctrl, FrameBufs fb) {
+  const int N = pp->width * pp->height;
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id == 0) ctrl->count[1] = N;
+  if (id >= N) return;
+  V o, dw;
+  camera_ray(pp, id, &o, &dw);
+  start_path(fb, id, o, dw);
 }
 
 // ----------------------------------------------------------- traversal
@@ -171,7 +182,10 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_shadow(DevScene S
 //                   Russian roulette in benchmark semantics.
 struct PathState {
   bool alive;
-  int pixel;
+  int pixel;                // queue slot's path index (path state)
+  int fidx;                 // film index of its pixel
+  int local;                // its pixel within its frame (the samples' key)
+  const PassParams* pp;     // its frame's parameters
   V thr, ps;
   int spec;
   Hit H;
@@ -189,10 +203,40 @@ template <int LEAN> __device__ __forceinline__ bool mesh_lights(const DevScene& 
 template <int LEAN> __device__ __forceinline__ bool env_present(const DevEnv& E) { return LEAN || E.present; }
 template <int LEAN> __device__ __forceinline__ bool grid_on(const DevEnv& E) { return LEAN || E.grid_on; }
 
-template <int MODE, int LEAN = 0>
-__device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, const PassParams* __restrict__ pp, int b,
-                                          const FrameBufs& fb, int j, int count, PathState& P) {
-  const int kahan = pp->kahan;
+// Which frame a path belongs to: one frame (its parameters, film index = path
+// index), or a batch of frames sharing the queues (BatchFrames).
+struct OneFrame {
+  const PassParams* pp;
+  __device__ __forceinline__ void operator()(int g, PathState& P) const {
+    P.pp = pp;
+    P.fidx = g;
+    P.local = g;
+  }
+};
+// Frames of a merged batch pass: frame k holds the paths start[k] .. start[k+1]-1
+// (pixel g - start[k] of that frame), its film at film[k] .. and its parameters
+// at pp[k].
+struct BatchFrames {
+  const int* start;  // n + 1
+  const int* film;   // n
+  const PassParams* pp;
+  int n;
+  __device__ __forceinline__ void operator()(int g, PathState& P) const {
+    int lo = 0, hi = n - 1;  // the last frame with start <= g
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(start + mid) <= g) lo = mid;
+      else hi = mid - 1;
+    }
+    P.pp = pp + lo;
+    P.local = g - __ldg(start + lo);
+    P.fidx = __ldg(film + lo) + P.local;
+  }
+};
+
+template <int MODE, int LEAN = 0, class Res = OneFrame>
+__device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, Res res, int b, const FrameBufs& fb,
+                                          int j, int count, PathState& P) {
   P.alive = false;
   P.pixel = 0;
   P.thr = zero4();
@@ -204,6 +248,9 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, co
   float4 qd = __ldg(fb.q_d[(b + 1) & 1] + j);
   const int pixel = __float_as_int(qo.w);
   P.pixel = pixel;
+  res(pixel, P);
+  const PassParams* __restrict__ pp = P.pp;
+  const int kahan = pp->kahan;
   V o = mk(qo.x, qo.y, qo.z, 0.f), d = mk(qd.x, qd.y, qd.z, 0.f);
   const float t = fb.hit_t[j];
   const int prim = fb.hit_prim[j];
@@ -229,7 +276,7 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, co
             float pdfW = pdf_a_to_w(pdfA, t, P.B.fix.z);
             w = mis2(P.ps.w, pdfW * pick);
           }
-          film_add(fb.film, fb.film_c, pixel, muls(mul(P.thr, c), w), kahan);
+          film_add(fb.film, fb.film_c, P.fidx, muls(mul(P.thr, c), w), kahan);
         }
       } else {
         P.alive = true;
@@ -246,7 +293,7 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, co
       if (MODE == 1 && mesh_lights<LEAN>(S)) pdfW = pdfW * 0.5f;
       float w = 1.f;
       if (!P.spec) w = mis2(P.ps.w, pdfW);
-      film_add(fb.film, fb.film_c, pixel, muls(mul(P.thr, c), w), kahan);
+      film_add(fb.film, fb.film_c, P.fidx, muls(mul(P.thr, c), w), kahan);
     }
   }
 }
@@ -255,8 +302,9 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, co
 // mode 1: the pixel's id). Writes the path state back; P.alive turns false when
 // Russian roulette ends the path.
 template <int MODE, bool TEX, int LEAN = 0>
-__device__ __forceinline__ void shade_continue(const DevScene& S, const DevEnv& E, const PassParams* __restrict__ pp,
-                                               int b, const FrameBufs& fb, int gid, PathState& P, ShadeOut& R) {
+__device__ __forceinline__ void shade_continue(const DevScene& S, const DevEnv& E, int b, const FrameBufs& fb,
+                                               int gid, PathState& P, ShadeOut& R) {
+  const PassParams* __restrict__ pp = P.pp;
   const float fc = pp->frame_count;
   R.has_shadow = false;
   R.ndir = zero4();
@@ -317,7 +365,7 @@ __device__ __forceinline__ void shade_continue(const DevScene& S, const DevEnv& 
       float w = mis2(pdfW, bpdf);
       float sc = (w * cosO / (pick * pdfW));
       R.shc = mk(sc * (rad.x * f.x) * P.thr.x, sc * (rad.y * f.y) * P.thr.y, sc * (rad.z * f.z) * P.thr.z, 1.f);
-      R.sho = mk(P.H.p.x, P.H.p.y, P.H.p.z, __int_as_float(P.pixel));
+      R.sho = mk(P.H.p.x, P.H.p.y, P.H.p.z, __int_as_float(P.fidx));
       R.shd = mk(dir.x, dir.y, dir.z, dist - 2.f * 1e-3f);
       R.has_shadow = true;
     }
@@ -366,7 +414,7 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade_ref(DevScene S, D
   if (tile >= ntiles) return;
   const int j = tile * kShadeThreads + threadIdx.x;
   PathState P;
-  shade_hit<0>(S, E, pp, b, fb, j, count, P);
+  shade_hit<0>(S, E, OneFrame{pp}, b, fb, j, count, P);
   unsigned long long tot = 0;
   unsigned long long excl = block_rank2<kShadeThreads>(P.alive, false, &tot, sh);
   if (threadIdx.x == 0) s_base = lookback(status, tile, tot, &ctrl->error);
@@ -378,7 +426,7 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade_ref(DevScene S, D
   }
   if (!P.alive) return;
   ShadeOut R;
-  shade_continue<0, TEX>(S, E, pp, b, fb, slot, P, R);
+  shade_continue<0, TEX>(S, E, b, fb, slot, P, R);
   const int nq = b & 1;  // queue written for bounce b + 1
   fb.q_o[nq][slot] = mk(P.H.p.x, P.H.p.y, P.H.p.z, __int_as_float(P.pixel));
   fb.q_d[nq][slot] = mk(R.ndir.x, R.ndir.y, R.ndir.z, 0.f);
@@ -397,9 +445,10 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade_ref(DevScene S, D
 // appends its survivors and its shadow rays to the next queues with one atomic
 // per queue per chunk (ballot ranks inside the warp). Russian roulette runs after
 // the BSDF sample.
-template <int MINB, bool TEX = false, int LEAN = 0>
-__global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEnv E, const PassParams* __restrict__ pp,
-                                                         Ctrl* ctrl, int b, FrameBufs fb) {
+// Res: OneFrame (pp = the frame's parameters) or BatchFrames (a merged batch pass).
+template <int MINB, bool TEX = false, int LEAN = 0, class Res = OneFrame>
+__global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEnv E, Res res, Ctrl* ctrl, int b,
+                                                         FrameBufs fb) {
   const int count = ctrl->count[b];
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -411,10 +460,10 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEn
     if (chunk * 32 >= count) break;
     const int j = chunk * 32 + lane;
     PathState P;
-    shade_hit<1, LEAN>(S, E, pp, b, fb, j, count, P);
+    shade_hit<1, LEAN>(S, E, res, b, fb, j, count, P);
     ShadeOut R;
     R.has_shadow = false;
-    if (P.alive) shade_continue<1, TEX, LEAN>(S, E, pp, b, fb, pixel_gid(P.pixel), P, R);
+    if (P.alive) shade_continue<1, TEX, LEAN>(S, E, b, fb, pixel_gid(P.local), P, R);
     const unsigned am = __ballot_sync(0xffffffffu, P.alive), sm = __ballot_sync(0xffffffffu, R.has_shadow);
     int qa = 0, qs = 0;
     if (lane == 0) {
@@ -530,23 +579,27 @@ void launch_traces(cudaStream_t st, int grid, const DevScene& S, Ctrl* ctrl, int
 }
 }  // namespace
 
+// One persistent traversal launch over a queue of at most N rays.
+void launch_trace(cudaStream_t st, const DevScene& S, Ctrl* ctrl, int b, int mode, FrameBufs fb, int kahan, bool closest,
+                  int N, int num_sms, bool shared) {
+  static int bps[17] = {};
+  const int minb = closest ? trace_minb() : shadow_minb();
+  if (bps[minb] == 0)
+    bps[minb] = minb == 16 ? trace_blocks_per_sm<16>() : minb == 12 ? trace_blocks_per_sm<12>() : trace_blocks_per_sm<8>();
+  const int want = closest ? trace_grid_bps() : shadow_grid_bps();
+  const int per_sm = !shared ? bps[minb] : want > 0 ? std::min(want, bps[minb]) : std::max(1, bps[minb] / 2);
+  const int grid = std::max(1, std::min(num_sms * per_sm, (N + kTraceThreads - 1) / kTraceThreads));
+  if (minb == 16) launch_traces<16>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
+  else if (minb == 12) launch_traces<12>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
+  else launch_traces<8>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
+}
+
 int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassParams* d_pp, int mode, int max_depth,
                 int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb, unsigned long long* status,
                 size_t status_stride, int num_sms, cudaEvent_t* ev, unsigned long long* totals, bool shared) {
   const int N = width * height;
-  static int bps[17] = {};
   static int shade_bps[6] = {};
-  auto trace = [&](bool closest, int b) {
-    const int minb = closest ? trace_minb() : shadow_minb();
-    if (bps[minb] == 0)
-      bps[minb] = minb == 16 ? trace_blocks_per_sm<16>() : minb == 12 ? trace_blocks_per_sm<12>() : trace_blocks_per_sm<8>();
-    const int want = closest ? trace_grid_bps() : shadow_grid_bps();
-    const int per_sm = !shared ? bps[minb] : want > 0 ? std::min(want, bps[minb]) : std::max(1, bps[minb] / 2);
-    const int grid = std::max(1, std::min(num_sms * per_sm, (N + kTraceThreads - 1) / kTraceThreads));
-    if (minb == 16) launch_traces<16>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
-    else if (minb == 12) launch_traces<12>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
-    else launch_traces<8>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
-  };
+  auto trace = [&](bool closest, int b) { launch_trace(st, S, ctrl, b, mode, fb, kahan, closest, N, num_sms, shared); };
   // persistent traversal: one resident wave, or fewer blocks for a small frame
   // (a queue never exceeds the frame's pixels), leaving SMs to other streams
   const int tiles = (N + kShadeThreads - 1) / kShadeThreads;
@@ -569,21 +622,56 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
       const int sgrid = std::max(1, std::min(num_sms * shade_bps[sm], tiles));
       const bool lean = S.nlights == 0 && E.present && E.grid_on;
       if (S.tex_on)
-        k_shade<4, true><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
+        k_shade<4, true><<<sgrid, kShadeThreads, 0, st>>>(S, E, OneFrame{d_pp}, ctrl, b, fb);
       else if (lean && sm == 4)
-        k_shade<4, false, 1><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
+        k_shade<4, false, 1><<<sgrid, kShadeThreads, 0, st>>>(S, E, OneFrame{d_pp}, ctrl, b, fb);
       else if (sm == 4)
-        k_shade<4><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
+        k_shade<4><<<sgrid, kShadeThreads, 0, st>>>(S, E, OneFrame{d_pp}, ctrl, b, fb);
       else if (sm == 5)
-        k_shade<5><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
+        k_shade<5><<<sgrid, kShadeThreads, 0, st>>>(S, E, OneFrame{d_pp}, ctrl, b, fb);
       else
-        k_shade<3><<<sgrid, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb);
+        k_shade<3><<<sgrid, kShadeThreads, 0, st>>>(S, E, OneFrame{d_pp}, ctrl, b, fb);
     }
     if (ev) cudaEventRecord(ev[e++], st);
     trace(false, b);
     if (ev) cudaEventRecord(ev[e++], st);
   }
   if (totals) k_accumulate<<<1, 32, 0, st>>>(ctrl, max_depth, N, totals);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+namespace {
+// Camera rays of a merged batch pass: path g is pixel g - start[k] of frame k.
+__global__ void k_raygen_batch(BatchFrames B, int total, Ctrl* ctrl, FrameBufs fb) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g == 0) ctrl->count[1] = total;
+  if (g >= total) return;
+  PathState P;
+  B(g, P);
+  V o, dw;
+  camera_ray(P.pp, P.local, &o, &dw);
+  start_path(fb, g, o, dw);
+}
+}  // namespace
+
+int launch_batch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const int* d_start, const int* d_film,
+                      const PassParams* d_pp, int nframes, int total, int max_depth, int kahan, Ctrl* ctrl,
+                      FrameBufs fb, int num_sms, unsigned long long* totals) {
+  const BatchFrames B{d_start, d_film, d_pp, nframes};
+  static int shade_bps = 0;
+  if (shade_bps == 0) shade_bps = shade_blocks_per_sm(4);
+  const int tiles = (total + kShadeThreads - 1) / kShadeThreads;
+  const int sgrid = std::max(1, std::min(num_sms * shade_bps, tiles));
+  k_raygen_batch<<<(total + 255) / 256, 256, 0, st>>>(B, total, ctrl, fb);
+  for (int b = 1; b <= max_depth; ++b) {
+    launch_trace(st, S, ctrl, b, 1, fb, kahan, true, total, num_sms, false);
+    if (S.tex_on)
+      k_shade<4, true, 0, BatchFrames><<<sgrid, kShadeThreads, 0, st>>>(S, E, B, ctrl, b, fb);
+    else
+      k_shade<4, false, 0, BatchFrames><<<sgrid, kShadeThreads, 0, st>>>(S, E, B, ctrl, b, fb);
+    launch_trace(st, S, ctrl, b, 1, fb, kahan, false, total, num_sms, false);
+  }
+  if (totals) k_accumulate<<<1, 32, 0, st>>>(ctrl, max_depth, total, totals);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

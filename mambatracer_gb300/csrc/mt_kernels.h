@@ -27,6 +27,13 @@ struct FrameBufs {
 // shared: other frames or requests run beside this pass on the GPU (frames in
 // flight, served lanes): each persistent traversal launch then takes half the
 // blocks an SM can hold, leaving room for their kernels.
+// A merged batch pass (benchmark semantics, full-map environment sampling):
+// frames 0 .. nframes-1 share the queues; path g belongs to the frame k with
+// d_start[k] <= g < d_start[k+1] (pixel g - d_start[k]), its film slots start at
+// d_film[k], its parameters are d_pp[k]. total = d_start[nframes].
+int launch_batch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const int* d_start, const int* d_film,
+                      const PassParams* d_pp, int nframes, int total, int max_depth, int kahan, Ctrl* ctrl,
+                      FrameBufs fb, int num_sms, unsigned long long* totals);
 int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassParams* d_pp, int mode,
                 int max_depth, int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb,
                 unsigned long long* status, size_t status_stride, int num_sms, cudaEvent_t* events,
