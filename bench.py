@@ -512,14 +512,35 @@ def run_served(args):
                      "p99_ms": round(st["p99_ms"], 2), "max_ms": round(st["max_ms"], 2),
                      "span_s": round(st["span_ms"] * 1e-3, 3), "wall_s": round(wall, 3),
                      "completed": st["completed"], "max_queue": st["max_queue"], "rays": st["rays"]}
+    if args.workload == "batched":
+        # merged: each scene's requests as one batch through shared wavefront queues
+        t0 = time.perf_counter()
+        rays3 = np.zeros(3, np.int64)
+        lat = []
+        for key in keys:
+            frames = [(sphere_camera(cseed, w, h), w, h, spp, float(1 + 64 * k))
+                      for k, (t, kk, w, h, spp, cseed) in enumerate(reqs) if kk == key]
+            _, r = api.batch_render(ctx, S[key], frames, max_depth=DEPTH, rr_depth=RR, film_kahan=1)
+            rays3 += r
+            lat += [(time.perf_counter() - t0) * 1e3] * len(frames)
+        wall = time.perf_counter() - t0
+        lat = np.array(lat)
+        res["merged"] = {"mrays_per_s": round(int(rays3.sum()) / wall / 1e6, 2),
+                         "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                         "p95_ms": round(float(np.percentile(lat, 95)), 2),
+                         "p99_ms": round(float(np.percentile(lat, 99)), 2), "max_ms": round(float(lat.max()), 2),
+                         "wall_s": round(wall, 3), "batches": len(keys), "rays": rays3.tolist(),
+                         "how": "mt_batch_render per scene (its 32 requests through one set of queues), "
+                                "queues allocated and films copied to host inside the timed region"}
     pixels = sum(w * h * spp for _, _, w, h, spp, _ in reqs)
+    head = res.get("merged") or res["concurrent"]  # batched: the merged queues; served: the scheduler
     out = {
-        "metric": METRIC, "value": res["concurrent"]["mrays_per_s"], "unit": "Mrays/s", "n_gpus": 1,
+        "metric": METRIC, "value": head["mrays_per_s"], "unit": "Mrays/s", "n_gpus": 1,
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (procedural scenes and sky; no dataset)",
         "workload": args.workload, "requests": len(reqs), "samples": pixels,
-        "latency_ms": {k: res["concurrent"][k] for k in ("p50_ms", "p95_ms", "p99_ms", "max_ms")},
-        "concurrent": res["concurrent"], "sequential": res["sequential"],
-        "speedup_vs_sequential": round(res["concurrent"]["mrays_per_s"] / res["sequential"]["mrays_per_s"], 3),
+        "latency_ms": {k: head[k] for k in ("p50_ms", "p95_ms", "p99_ms", "max_ms")},
+        "concurrent": res["concurrent"], "sequential": res["sequential"], "merged": res.get("merged"),
+        "speedup_vs_sequential": round(head["mrays_per_s"] / res["sequential"]["mrays_per_s"], 3),
         "config": {
             "requests": ("64 jobs submitted at once, soup and stadium alternately, 4 spp" if args.workload == "batched"
                          else f"Poisson arrivals at {args.rate}/s for {args.duration} s, box room / soup / stadium "
