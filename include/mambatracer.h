@@ -307,7 +307,14 @@ int mt_trace_closest_dev(mt_scene* scene, mt_buffer* rays, int n, mt_buffer* t_o
  * served onto `lanes` preallocated lanes (stream + path state for the largest
  * frame) within a budget of path-state bytes (196 B per pixel; 0 = no limit);
  * no device memory is allocated while requests run. Scenes used by queued or
- * running requests cannot be destroyed (MT_ERR_BUSY). */
+ * running requests cannot be destroyed (MT_ERR_BUSY).
+ * merged = m (1..lanes): the running requests share wavefront queues (lanes x
+ * the largest frame paths, at most 2^30) instead of a lane each; the slots are
+ * split over m streams, and each stream issues rounds, a round being one merged
+ * pass per scene holding the next pass of every running request of its slots.
+ * A request joins at its stream's next round. A cancelled running request
+ * stops at the next round (state CANCELLED, no film). Films are the same, bit
+ * for bit, in both modes. */
 typedef struct mt_server mt_server;
 typedef struct mt_server_config {
   int lanes;                 /* requests in flight at once (1..64) */
@@ -316,7 +323,7 @@ typedef struct mt_server_config {
   int max_depth;             /* bounces per path */
   int rr_depth;              /* Russian roulette from this bounce on (0 = off) */
   int film_kahan;            /* compensated film sums */
-  int pad_;
+  int merged;                /* m >= 1: running requests share wavefront queues on m streams */
   uint64_t budget_bytes;     /* admission budget of path state + film, 0 = unlimited */
 } mt_server_config;
 typedef struct mt_served_stats {

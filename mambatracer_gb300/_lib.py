@@ -37,7 +37,7 @@ class BatchFrame(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("lanes", C.c_int), ("max_width", C.c_int), ("max_height", C.c_int), ("max_spp", C.c_int),
-                ("max_depth", C.c_int), ("rr_depth", C.c_int), ("film_kahan", C.c_int), ("pad_", C.c_int),
+                ("max_depth", C.c_int), ("rr_depth", C.c_int), ("film_kahan", C.c_int), ("merged", C.c_int),
                 ("budget_bytes", C.c_uint64)]
 
 

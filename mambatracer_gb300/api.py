@@ -359,15 +359,18 @@ class DeviceGI:
 class Server:
     """Served mode: concurrent render requests (mt_job_submit / poll / cancel / wait).
     A request renders `spp` benchmark-semantics passes of one camera; its film lands in
-    the float32 array given at submission (kept alive here until the request ends)."""
+    the float32 array given at submission (kept alive here until the request ends).
+    merged=m (m >= 1): the running requests share wavefront queues, their slots split
+    over m streams that each run rounds of one merged pass per scene; films are the same
+    bit for bit."""
 
     QUEUED, RUNNING, DONE, CANCELLED, FAILED = range(5)
 
     def __init__(self, ctx: Context, lanes: int = 8, max_width: int = 1920, max_height: int = 1080,
                  max_spp: int = 64, max_depth: int = 8, rr_depth: int = 3, film_kahan: int = 1,
-                 budget_bytes: int = 0):
-        self.cfg = ServerConfig(lanes, max_width, max_height, max_spp, max_depth, rr_depth, film_kahan, 0,
-                                budget_bytes)
+                 budget_bytes: int = 0, merged: int = 0):
+        self.cfg = ServerConfig(lanes, max_width, max_height, max_spp, max_depth, rr_depth, film_kahan,
+                                int(merged), budget_bytes)
         h = C.c_void_p()
         check(lib().mt_server_create(ctx.h, C.byref(self.cfg), C.byref(h)))
         self.h = h

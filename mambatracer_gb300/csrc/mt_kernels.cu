@@ -656,7 +656,7 @@ __global__ void k_raygen_batch(BatchFrames B, int total, Ctrl* ctrl, FrameBufs f
 
 int launch_batch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const int* d_start, const int* d_film,
                       const PassParams* d_pp, int nframes, int total, int max_depth, int kahan, Ctrl* ctrl,
-                      FrameBufs fb, int num_sms, unsigned long long* totals) {
+                      FrameBufs fb, int num_sms, unsigned long long* totals, bool shared) {
   const BatchFrames B{d_start, d_film, d_pp, nframes};
   static int shade_bps = 0;
   if (shade_bps == 0) shade_bps = shade_blocks_per_sm(4);
@@ -664,12 +664,12 @@ int launch_batch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const
   const int sgrid = std::max(1, std::min(num_sms * shade_bps, tiles));
   k_raygen_batch<<<(total + 255) / 256, 256, 0, st>>>(B, total, ctrl, fb);
   for (int b = 1; b <= max_depth; ++b) {
-    launch_trace(st, S, ctrl, b, 1, fb, kahan, true, total, num_sms, false);
+    launch_trace(st, S, ctrl, b, 1, fb, kahan, true, total, num_sms, shared);
     if (S.tex_on)
       k_shade<4, true, 0, BatchFrames><<<sgrid, kShadeThreads, 0, st>>>(S, E, B, ctrl, b, fb);
     else
       k_shade<4, false, 0, BatchFrames><<<sgrid, kShadeThreads, 0, st>>>(S, E, B, ctrl, b, fb);
-    launch_trace(st, S, ctrl, b, 1, fb, kahan, false, total, num_sms, false);
+    launch_trace(st, S, ctrl, b, 1, fb, kahan, false, total, num_sms, shared);
   }
   if (totals) k_accumulate<<<1, 32, 0, st>>>(ctrl, max_depth, total, totals);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;

@@ -33,7 +33,7 @@ struct FrameBufs {
 // d_film[k], its parameters are d_pp[k]. total = d_start[nframes].
 int launch_batch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const int* d_start, const int* d_film,
                       const PassParams* d_pp, int nframes, int total, int max_depth, int kahan, Ctrl* ctrl,
-                      FrameBufs fb, int num_sms, unsigned long long* totals);
+                      FrameBufs fb, int num_sms, unsigned long long* totals, bool shared = false);
 int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassParams* d_pp, int mode,
                 int max_depth, int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb,
                 unsigned long long* status, size_t status_stride, int num_sms, cudaEvent_t* events,

@@ -16,6 +16,22 @@
 // host callback on the lane's stream wakes the scheduler, which measures the
 // request's latency from submission. Scenes are reference-counted while
 // requests use them.
+//
+// Merged mode (config `merged` = m >= 1): the running requests share wavefront
+// queues instead of a lane each. The slots are split over m merge streams
+// (slot k on stream k mod m); each stream works in rounds, a round being, per
+// scene, one merged pass (launch_batch_pass) holding the next pass of every
+// running request of the stream's slots, so each bounce is one launch per
+// kernel for all of them, and the streams overlap one another's last bounces.
+// Requests join at their stream's next round and leave when their last pass is
+// issued (continuous batching at pass granularity); a cancelled running request
+// stops at the next round. Slot k's film is the arena's k-th frame-sized
+// region, a stream's path state its slots' share of the arena. Per-round frame
+// tables live in a ring of kRounds entries per stream; a host callback at the
+// end of each round frees its entry, which also keeps the scheduler at most
+// kRounds rounds ahead of the GPU on each stream. A merged pass keys every
+// path's samples on its own frame's pixel and frame number, so each film equals
+// the request rendered alone, bit for bit.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -60,9 +76,37 @@ struct Lane {
   Request* req = nullptr;
   bool finished = false;  // set by the host callback
   struct mt_server* server = nullptr;
+  int pass = 0;         // merged mode: passes of `req` issued so far
+  bool issued = false;  // merged mode: the request's completion is on the stream
+  int group = -1;       // merged mode: its merge stream
+};
+
+// One merged-mode round's frame tables: per scene group the first path of each
+// frame and the total (n + 1 ints), the frames' film offsets (n ints), their
+// pass parameters, and a control block.
+struct Round {
+  int* h_tab = nullptr;  // pinned
+  PassParams* h_pp = nullptr;
+  int* d_tab = nullptr;
+  PassParams* d_pp = nullptr;
+  Ctrl* d_ctrl = nullptr;
+  cudaEvent_t done = nullptr;
+  bool used = false;
 };
 
 constexpr size_t kPathBytesPerPixel = 196;
+constexpr int kRounds = 3;
+
+// One merge stream: its slots, its share of the queues, its round ring.
+struct MergeGroup {
+  struct mt_server* server = nullptr;
+  cudaStream_t stream = nullptr;
+  std::vector<int> slots;
+  FrameBufs fb{};  // path state of its slots' paths; the films of the whole arena
+  Round rounds[kRounds];
+  int next_round = 0;
+  int inflight = 0;  // rounds whose end callback has not run (server lock)
+};
 
 }  // namespace
 
@@ -86,9 +130,24 @@ struct mt_server {
   size_t max_queue = 0;
   Clock::time_point t_first_submit, t_last_done;
   bool any_submit = false;
+  // merged mode
+  FrameBufs mfb{};  // queues for lanes x slot_px paths; slot k's film at k x slot_px
+  size_t slot_px = 0;
+  std::vector<MergeGroup> groups;  // sized once at creation (callbacks hold their addresses)
+  std::string broken;  // set when a round failed: later requests fail with it
 };
 
 namespace {
+
+void CUDART_CB round_done(void* p) {
+  MergeGroup* G = static_cast<MergeGroup*>(p);
+  mt_server* s = G->server;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    --G->inflight;
+  }
+  s->cv.notify_all();
+}
 
 void CUDART_CB lane_done(void* p) {
   Lane* L = static_cast<Lane*>(p);
@@ -194,6 +253,184 @@ void release_scene(Request* R) {
   R->scene = nullptr;
 }
 
+void free_merged(mt_server* s) {
+  for (auto* p : {&s->mfb.q_o[0], &s->mfb.q_o[1], &s->mfb.q_d[0], &s->mfb.q_d[1], &s->mfb.thr, &s->mfb.ps,
+                  &s->mfb.s_o, &s->mfb.s_d, &s->mfb.s_c, &s->mfb.film, &s->mfb.film_c})
+    dfree(*p);
+  dfree(s->mfb.hit_t);
+  dfree(s->mfb.hit_prim);
+  dfree(s->mfb.flag);
+  for (MergeGroup& G : s->groups) {
+    for (Round& Rd : G.rounds) {
+      if (Rd.h_tab) cudaFreeHost(Rd.h_tab);
+      if (Rd.h_pp) cudaFreeHost(Rd.h_pp);
+      Rd.h_tab = nullptr;
+      Rd.h_pp = nullptr;
+      dfree(Rd.d_tab);
+      dfree(Rd.d_pp);
+      dfree(Rd.d_ctrl);
+      if (Rd.done) cudaEventDestroy(Rd.done);
+      Rd.done = nullptr;
+    }
+    if (G.stream) cudaStreamDestroy(G.stream);
+    G.stream = nullptr;
+  }
+}
+
+// Merged mode: the queues for lanes x N paths, the slots' films and pinned
+// staging, and per merge stream its slots, its share of the queues, its round
+// ring and its stream.
+int alloc_merged(mt_server* s, size_t N, int m) {
+  const size_t P = N * s->lanes.size();
+  const int lanes = (int)s->lanes.size();
+  s->groups.resize((size_t)m);
+  for (int k = 0; k < lanes; ++k) {
+    s->lanes[k].group = k % m;
+    s->groups[k % m].slots.push_back(k);
+  }
+  int r = MT_OK;
+  for (auto* p : {&s->mfb.q_o[0], &s->mfb.q_o[1], &s->mfb.q_d[0], &s->mfb.q_d[1], &s->mfb.thr, &s->mfb.ps,
+                  &s->mfb.s_o, &s->mfb.s_d, &s->mfb.s_c, &s->mfb.film, &s->mfb.film_c})
+    if (!r) r = dalloc(p, P);
+  if (!r) r = dalloc(&s->mfb.hit_t, P);
+  if (!r) r = dalloc(&s->mfb.hit_prim, P);
+  if (!r) r = dalloc(&s->mfb.flag, P);
+  for (Lane& L : s->lanes)
+    if (!r && cudaMallocHost((void**)&L.h_stage, sizeof(float4) * N) != cudaSuccess)
+      r = fail(MT_ERR_NOMEM, "pinned film staging");
+  size_t base = 0;  // first path of the group's share
+  for (MergeGroup& G : s->groups) {
+    G.server = s;
+    const int n = (int)G.slots.size();
+    for (Round& Rd : G.rounds) {
+      if (!r && cudaMallocHost((void**)&Rd.h_tab, sizeof(int) * 3 * n) != cudaSuccess)
+        r = fail(MT_ERR_NOMEM, "pinned round tables");
+      if (!r && cudaMallocHost((void**)&Rd.h_pp, sizeof(PassParams) * n) != cudaSuccess)
+        r = fail(MT_ERR_NOMEM, "pinned round tables");
+      if (!r) r = dalloc(&Rd.d_tab, (size_t)3 * n);
+      if (!r) r = dalloc(&Rd.d_pp, (size_t)n);
+      if (!r) r = dalloc(&Rd.d_ctrl, (size_t)n);
+      if (!r && cudaEventCreateWithFlags(&Rd.done, cudaEventDisableTiming) != cudaSuccess)
+        r = fail(MT_ERR_CUDA, "event create");
+    }
+    if (!r && cudaStreamCreateWithFlags(&G.stream, cudaStreamNonBlocking) != cudaSuccess)
+      r = fail(MT_ERR_CUDA, "stream create");
+    if (r) break;
+    G.fb = s->mfb;  // films stay whole: slot k's film is at k x N
+    for (int q = 0; q < 2; ++q) {
+      G.fb.q_o[q] += base;
+      G.fb.q_d[q] += base;
+    }
+    G.fb.hit_t += base;
+    G.fb.hit_prim += base;
+    G.fb.thr += base;
+    G.fb.ps += base;
+    G.fb.flag += base;
+    G.fb.s_o += base;
+    G.fb.s_d += base;
+    G.fb.s_c += base;
+    base += (size_t)n * N;
+  }
+  s->slot_px = N;
+  return r;
+}
+
+// Merged mode: enqueues one round of merge stream G over the slots in `work`
+// (scheduler thread, context lock held, server lock not held). cancel[i]: slot
+// work[i]'s request was cancelled; it gets no more passes and completes
+// without a film.
+int issue_round(mt_server* s, MergeGroup& G, const std::vector<int>& work, const std::vector<char>& cancel) {
+  const mt_server_config& c = s->cfg;
+  const size_t N = s->slot_px;
+  cudaStream_t st = G.stream;
+  Round& Rd = G.rounds[G.next_round];
+  G.next_round = (G.next_round + 1) % kRounds;
+  if (Rd.used) CU(cudaEventSynchronize(Rd.done));  // its tables were read, its passes ran
+  Rd.used = true;
+  std::vector<int> go;
+  for (size_t i = 0; i < work.size(); ++i) {
+    Lane& L = s->lanes[work[i]];
+    if (cancel[i]) {
+      CU(cudaLaunchHostFunc(st, lane_done, &L));
+      L.issued = true;
+      continue;
+    }
+    if (L.pass == 0) {
+      CU(cudaMemsetAsync(s->mfb.film + N * work[i], 0, (size_t)L.req->width * L.req->height * 16, st));
+      CU(cudaMemsetAsync(s->mfb.film_c + N * work[i], 0, (size_t)L.req->width * L.req->height * 16, st));
+    }
+    go.push_back(work[i]);
+  }
+  // scene groups in slot order; per group: starts (n + 1), film offsets (n), pass parameters (n)
+  struct Group {
+    mt_scene* scene;
+    int tab, pp, n, total;
+  };
+  std::vector<Group> groups;
+  std::vector<char> taken(go.size(), 0);
+  int ti = 0, pi = 0;
+  for (size_t a = 0; a < go.size(); ++a) {
+    if (taken[a]) continue;
+    Group Gr{s->lanes[go[a]].req->scene, ti, pi, 0, 0};
+    std::vector<int> members;
+    for (size_t b = a; b < go.size(); ++b)
+      if (!taken[b] && s->lanes[go[b]].req->scene == Gr.scene) {
+        taken[b] = 1;
+        members.push_back(go[b]);
+      }
+    Gr.n = (int)members.size();
+    int* start = Rd.h_tab + ti;
+    int* film = start + Gr.n + 1;
+    for (int m = 0; m < Gr.n; ++m) {
+      const Lane& L = s->lanes[members[m]];
+      const Request* R = L.req;
+      PassParams& pp = Rd.h_pp[pi + m];
+      std::memset(&pp, 0, sizeof(pp));
+      camera_constants(R->camera, R->width, R->height, pp);
+      pp.frame_count = R->frame_count + (float)L.pass;
+      pp.width = R->width;
+      pp.height = R->height;
+      pp.max_depth = c.max_depth;
+      pp.mode = 1;
+      pp.rr_depth = c.rr_depth;
+      pp.kahan = c.film_kahan;
+      pp.grid_accum = 0;
+      start[m] = Gr.total;
+      film[m] = (int)(N * members[m]);
+      Gr.total += R->width * R->height;
+    }
+    start[Gr.n] = Gr.total;
+    ti += 2 * Gr.n + 1;
+    pi += Gr.n;
+    groups.push_back(Gr);
+  }
+  if (!groups.empty()) {
+    CU(cudaMemcpyAsync(Rd.d_tab, Rd.h_tab, sizeof(int) * ti, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(Rd.d_pp, Rd.h_pp, sizeof(PassParams) * pi, cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(Rd.d_ctrl, 0, sizeof(Ctrl) * groups.size(), st));
+  }
+  for (size_t g = 0; g < groups.size(); ++g) {
+    const Group& Gr = groups[g];
+    const DevScene S = Gr.scene->view();
+    const DevEnv E = Gr.scene->env_view();  // full-map environment sampling
+    if (launch_batch_pass(st, S, E, Rd.d_tab + Gr.tab, Rd.d_tab + Gr.tab + Gr.n + 1, Rd.d_pp + Gr.pp, Gr.n,
+                          Gr.total, c.max_depth, c.film_kahan, Rd.d_ctrl + g, G.fb, s->ctx->num_sms, s->d_totals,
+                          s->groups.size() > 1))
+      return fail(MT_ERR_CUDA, "merged pass launch: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  for (int k : go) {
+    Lane& L = s->lanes[k];
+    if (++L.pass < L.req->spp) continue;
+    CU(cudaMemcpyAsync(L.h_stage, s->mfb.film + N * k, (size_t)L.req->width * L.req->height * 16,
+                       cudaMemcpyDeviceToHost, st));
+    CU(cudaLaunchHostFunc(st, lane_done, &L));
+    L.issued = true;
+  }
+  CU(cudaEventRecord(Rd.done, st));
+  CU(cudaLaunchHostFunc(st, round_done, &G));
+  return MT_OK;
+}
+
 void worker_main(mt_server* s) {
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
@@ -215,6 +452,8 @@ void worker_main(mt_server* s) {
       release_scene(R);
       L.req = nullptr;
       L.finished = false;
+      L.pass = 0;
+      L.issued = false;
       s->done_cv.notify_all();
     }
     // admissions: first come, first served within the lanes and the byte budget
@@ -228,19 +467,49 @@ void worker_main(mt_server* s) {
         continue;
       }
       Lane* free_lane_p = nullptr;
-      for (Lane& L : s->lanes)
-        if (!L.req) {
-          free_lane_p = &L;
-          break;
+      if (!s->groups.empty()) {
+        // merged: a free slot of the merge stream with the fewest running pixels
+        size_t best = ~(size_t)0;
+        for (const MergeGroup& G : s->groups) {
+          size_t px = 0;
+          Lane* slot = nullptr;
+          for (int k : G.slots) {
+            Lane& L = s->lanes[k];
+            if (L.req)
+              px += (size_t)L.req->width * L.req->height;
+            else if (!slot)
+              slot = &L;
+          }
+          if (slot && px < best) {
+            best = px;
+            free_lane_p = slot;
+          }
         }
+      } else {
+        for (Lane& L : s->lanes)
+          if (!L.req) {
+            free_lane_p = &L;
+            break;
+          }
+      }
       if (!free_lane_p || (s->running > 0 && s->used_bytes + R->bytes > s->cfg.budget_bytes)) break;
       s->pending.pop_front();
+      if (!s->broken.empty()) {
+        R->state = kFailed;
+        R->error = s->broken;
+        release_scene(R);
+        s->done_cv.notify_all();
+        continue;
+      }
       R->state = kRunning;
       R->t_start = Clock::now();
       s->used_bytes += R->bytes;
       ++s->running;
       free_lane_p->req = R;
       free_lane_p->finished = false;
+      free_lane_p->pass = 0;
+      free_lane_p->issued = false;
+      if (s->cfg.merged) continue;  // its passes join its merge stream's next round
       lk.unlock();
       int r;
       {
@@ -261,11 +530,62 @@ void worker_main(mt_server* s) {
         s->done_cv.notify_all();
       }
     }
+    // merged mode: on each merge stream with a free round entry, the next round
+    // over its running requests with passes to go
+    bool issued_round = false;
+    for (MergeGroup& G : s->groups) {
+      if (G.inflight >= kRounds || !s->broken.empty()) continue;
+      std::vector<int> work;
+      std::vector<char> cancel;
+      for (int k : G.slots)
+        if (s->lanes[k].req && !s->lanes[k].issued) {
+          work.push_back(k);
+          cancel.push_back(s->lanes[k].req->cancel ? 1 : 0);
+        }
+      if (work.empty()) continue;
+      ++G.inflight;
+      issued_round = true;
+      lk.unlock();
+      int r;
+      {
+        std::lock_guard<std::recursive_mutex> ck(s->ctx->mu);
+        cudaSetDevice(s->ctx->device);
+        r = issue_round(s, G, work, cancel);
+        if (r)
+          for (MergeGroup& H : s->groups) cudaStreamSynchronize(H.stream);
+      }
+      lk.lock();
+      if (r) {
+        // every running request fails, and so does every later one
+        s->broken = mt_last_error();
+        for (Lane& L : s->lanes) {
+          if (!L.req) continue;
+          L.req->state = kFailed;
+          L.req->error = s->broken;
+          L.req->t_done = Clock::now();
+          s->used_bytes -= L.req->bytes;
+          --s->running;
+          release_scene(L.req);
+          L.req = nullptr;
+          L.finished = false;
+          L.issued = false;
+          L.pass = 0;
+        }
+        s->done_cv.notify_all();
+        break;
+      }
+    }
+    if (issued_round) continue;
     if (s->stop && s->running == 0) break;
     s->cv.wait(lk, [&] {
       if (s->stop && s->running == 0) return true;
       for (Lane& L : s->lanes)
         if (L.req && L.finished) return true;
+      if (s->broken.empty())
+        for (const MergeGroup& G : s->groups)
+          if (G.inflight < kRounds)
+            for (int k : G.slots)
+              if (s->lanes[k].req && !s->lanes[k].issued) return true;
       if (s->pending.empty()) return false;
       if (s->pending.front()->cancel) return true;
       for (Lane& L : s->lanes)
@@ -295,6 +615,9 @@ extern "C" int mt_server_create(mt_context* ctx, const mt_server_config* cfg, mt
     return fail(MT_ERR_INVALID, "largest frame %d x %d", c.max_width, c.max_height);
   if (c.max_spp < 1 || c.max_spp > 4096) return fail(MT_ERR_INVALID, "max_spp %d", c.max_spp);
   if (c.max_depth < 1 || c.max_depth > kMaxDepth) return fail(MT_ERR_INVALID, "max_depth %d", c.max_depth);
+  if (c.merged < 0 || c.merged > c.lanes) return fail(MT_ERR_INVALID, "merged %d (0..lanes)", c.merged);
+  if (c.merged && (long long)c.lanes * c.max_width * c.max_height > (1ll << 30))
+    return fail(MT_ERR_INVALID, "merged: lanes x largest frame above 2^30 paths");
   *out = nullptr;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   CU(cudaSetDevice(ctx->device));
@@ -308,12 +631,14 @@ extern "C" int mt_server_create(mt_context* ctx, const mt_server_config* cfg, mt
   int r = dalloc(&s->d_totals, 4);
   for (Lane& L : s->lanes) {
     L.server = s;
-    if (!r) r = alloc_lane(L, N, c.max_spp, c.max_depth, s->status_stride);
+    if (!r && !c.merged) r = alloc_lane(L, N, c.max_spp, c.max_depth, s->status_stride);
   }
+  if (!r && c.merged) r = alloc_merged(s, N, c.merged);
   if (!r && cudaMemset(s->d_totals, 0, 32) != cudaSuccess) r = fail(MT_ERR_CUDA, "memset");
   if (r) {
     std::string keep = mt_last_error();
     for (Lane& L : s->lanes) free_lane(L);
+    free_merged(s);
     dfree(s->d_totals);
     delete s;
     return fail(r, "%s", keep.c_str());
@@ -336,10 +661,13 @@ extern "C" int mt_server_destroy(mt_server* s) {
   {
     std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
     cudaSetDevice(s->ctx->device);
+    for (MergeGroup& G : s->groups)
+      if (G.stream) cudaStreamSynchronize(G.stream);
     for (Lane& L : s->lanes) {
       if (L.stream) cudaStreamSynchronize(L.stream);
       free_lane(L);
     }
+    free_merged(s);
     dfree(s->d_totals);
     auto& v = s->ctx->servers;
     v.erase(std::remove(v.begin(), v.end(), s), v.end());
@@ -478,7 +806,10 @@ extern "C" int mt_server_stats(mt_server* s, mt_served_stats* out) {
 }
 
 void servers_sync(mt_context* ctx) {
-  for (mt_server* s : ctx->servers)
+  for (mt_server* s : ctx->servers) {
+    for (MergeGroup& G : s->groups)
+      if (G.stream) cudaStreamSynchronize(G.stream);
     for (Lane& L : s->lanes)
       if (L.stream) cudaStreamSynchronize(L.stream);
+  }
 }

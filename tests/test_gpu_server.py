@@ -40,9 +40,14 @@ def served_scenes(ctx, orc):
         S.close()
 
 
-def test_served_films_equal_plain_jobs(ctx, served_scenes):
+@pytest.mark.parametrize("merged", [0, 1, 2])
+def test_served_films_equal_plain_jobs(ctx, served_scenes, merged):
+    """Lanes (a stream each) or merged queues on one or two streams (rounds of one pass
+    per scene over the stream's running requests): every film equals the job rendered
+    alone."""
     rng = np.random.default_rng(11)
-    srv = api.Server(ctx, lanes=4, max_width=256, max_height=256, max_spp=8, max_depth=DEPTH, rr_depth=RR)
+    srv = api.Server(ctx, lanes=4, max_width=256, max_height=256, max_spp=8, max_depth=DEPTH, rr_depth=RR,
+                     merged=merged)
     reqs = []
     for k in range(14):
         name = ("room", "soup", "stadium")[k % 3]
@@ -71,10 +76,12 @@ def test_served_films_equal_plain_jobs(ctx, served_scenes):
     srv.close()
 
 
-def test_cancel_poll_wait_and_busy_scene(ctx, served_scenes):
+@pytest.mark.parametrize("merged", [0, 1])
+def test_cancel_poll_wait_and_busy_scene(ctx, served_scenes, merged):
     sc, S = served_scenes["soup"]
     rng = np.random.default_rng(12)
-    srv = api.Server(ctx, lanes=1, max_width=512, max_height=512, max_spp=16, max_depth=DEPTH, rr_depth=RR)
+    srv = api.Server(ctx, lanes=1, max_width=512, max_height=512, max_spp=16, max_depth=DEPTH, rr_depth=RR,
+                     merged=merged)
     big = srv.submit(S, sphere_camera(rng, 512, 512, 3.0), 512, 512, 16, 1.0)
     queued = [srv.submit(S, sphere_camera(rng, 64, 64, 3.0), 64, 64, 1, float(100 + i)) for i in range(3)]
     with pytest.raises(MTError, match="still"):
@@ -90,4 +97,32 @@ def test_cancel_poll_wait_and_busy_scene(ctx, served_scenes):
     assert st["completed"] == 3 and st["cancelled"] == 1 and st["max_queue"] >= 3
     with pytest.raises(MTError):
         srv.submit(S, sc.camera, 1024, 1024, 1)  # larger than the server's largest frame
+    srv.close()
+
+
+def test_merged_cancel_running_request(ctx, served_scenes):
+    """Merged mode stops a cancelled running request at the next round; the
+    requests sharing its rounds, and those after it, still equal jobs alone."""
+    _, S = served_scenes["soup"]
+    rng = np.random.default_rng(13)
+    srv = api.Server(ctx, lanes=3, max_width=384, max_height=384, max_spp=64, max_depth=DEPTH, rr_depth=RR,
+                     merged=2)
+    big = srv.submit(S, sphere_camera(rng, 384, 384, 3.0), 384, 384, 64, 1.0)
+    reqs = []
+    for k in range(5):
+        w, h = int(rng.integers(16, 120)), int(rng.integers(16, 120))
+        cam = sphere_camera(rng, w, h, 3.0)
+        reqs.append((srv.submit(S, cam, w, h, 2, float(500 + k)), cam, w, h))
+    srv.cancel(big)
+    srv.drain()
+    assert srv.poll(big)[0] == api.Server.CANCELLED
+    st = srv.stats()
+    assert st["completed"] == 5 and st["cancelled"] == 1 and st["failed"] == 0
+    for k, (rid, cam, w, h) in enumerate(reqs):
+        assert srv.poll(rid)[0] == api.Server.DONE
+        J = api.Job(ctx, S, w, h, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, spp=2)
+        J.set_camera(cam)
+        J.render(None, float(500 + k))
+        assert srv.film(rid).tobytes() == J.film().tobytes()
+        J.close()
     srv.close()
