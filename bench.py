@@ -73,6 +73,20 @@ def make_scene(kind, small, width, height):
     return scenes.soup(200_000 if small else NTRI, seed=1, width=width, height=height)
 
 
+TUNED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "mambatracer_gb300", "tuning_gb300.json")
+
+
+def apply_tuning():
+    """Installs the launch shapes the autotuner (mambatracer_gb300.tune) persisted for
+    this GPU model, when the file exists and matches; returns what the run uses."""
+    from mambatracer_gb300 import api, tune
+    res = tune.load(TUNED) if os.path.exists(TUNED) else None
+    if res is None:
+        return {"source": "built-in defaults", "tuning": api.get_tuning()}
+    return {"source": "autotuned (mambatracer_gb300/tuning_gb300.json: " + res["workload"] + ")",
+            "tuning": api.get_tuning()}
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -244,6 +258,7 @@ def run_gpu(args):
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     from mambatracer_gb300 import api, build, scenes
     build.build()
+    launch_shapes = apply_tuning()
 
     width, height = (640, 360) if args.small and args.workload != "room" else (W_DEFAULT, H_DEFAULT)
     spp = WORKLOADS[args.workload]["spp"]
@@ -411,7 +426,7 @@ def run_gpu(args):
             "msamples_per_s": round(width * height * spp * args.steps * world / (ms * 1e-3) / 1e6, 2),
             "bvh_depth": S.depth, "bvh_build_ms": round(bvh_build_ms, 2), "bvh_build": "GPU, level-synchronous",
             "bvh_records": "FP16 child boxes rounded outward, 32 B" if args.precision else "FP32 child boxes, 64 B",
-            "alg_bytes_seconds": round(t_alg, 1),
+            "alg_bytes_seconds": round(t_alg, 1), "launch_shapes": launch_shapes,
         }
     job.close()
     S.close()
@@ -484,6 +499,7 @@ def run_served(args):
     the served-mode scheduler, against the same requests run one at a time."""
     from mambatracer_gb300 import api, build, scenes
     build.build()
+    launch_shapes = apply_tuning()
     ctx = api.Context(0)
     env = scenes.sky_env(ENV_W, ENV_H)
     S = {}
@@ -558,6 +574,7 @@ def run_served(args):
             "bvh_records": "FP16 child boxes rounded outward, 32 B" if args.precision else "FP32 child boxes, 64 B",
             "latency": "submission to film in host memory (pinned staging), host clock",
             "equal_error": "the sequential run renders the same requests with the same spp",
+            "launch_shapes": launch_shapes,
         },
     }
     for sc_h in S.values():

@@ -287,6 +287,26 @@ void* mt_buf_device_ptr(mt_buffer* buf);
 int mt_compact_isects_noalloc(void* stream, const void* isects_in, const int32_t* pixels_in, int n,
                               void* isects_out, int32_t* pixels_out, int32_t* count_io);
 
+/* ------------------------------------------------------ launch shapes */
+
+/* The hot kernels' launch shapes, process-wide (no reference counterpart: its
+ * local sizes are fixed, src/cl/device/CDeviceGI.java:122). The reference's
+ * block size, queue length and regeneration threshold map to: the traversal
+ * and shading builds (resident blocks per SM their registers are bounded
+ * for), the persistent traversal grid of a launch that shares the GPU with
+ * other frames, and the traversal steps between refills of finished lanes.
+ * Every choice renders the same films; mambatracer_gb300.tune searches them
+ * and persists the best as JSON. Render jobs capture their graphs again after
+ * a change; set it between frames. */
+typedef struct mt_tuning {
+  int closest_minb, shadow_minb; /* traversal builds: 8, 12 or 16 blocks of 128 threads per SM */
+  int closest_grid, shadow_grid; /* blocks per SM of a shared traversal launch, 0..32 (0: half of what fits) */
+  int shade_minb;                /* shading build: 3, 4 or 5 blocks of 256 threads per SM */
+  int refill_steps;              /* traversal steps between lane refills, 4..1024 */
+} mt_tuning;
+int mt_tuning_get(mt_tuning* out);
+int mt_tuning_set(const mt_tuning* in); /* MT_ERR_INVALID when a field is out of range */
+
 /* ------------------------------------------------------- ray queries */
 
 /* Closest hit over n rays in the reference Ray layout (80 B each, tMax is

@@ -41,6 +41,12 @@ class ServerConfig(C.Structure):
                 ("budget_bytes", C.c_uint64)]
 
 
+class Tuning(C.Structure):
+    """mt_tuning"""
+    _fields_ = [("closest_minb", C.c_int), ("shadow_minb", C.c_int), ("closest_grid", C.c_int),
+                ("shadow_grid", C.c_int), ("shade_minb", C.c_int), ("refill_steps", C.c_int)]
+
+
 class ServedStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("cancelled", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64),
                 ("running", C.c_int64), ("max_queue", C.c_int64), ("rays", C.c_int64 * 3), ("p50_ms", C.c_double),
@@ -81,6 +87,8 @@ SIGNATURES = {
     "mt_scene_light_count": (I, [P]),
     "mt_batch_render": (I, [P, P, P, I, I, I, I, P, P]),
     "mt_obj_parse": (I, [P, C.c_size_t, P, P, P, P, P]),
+    "mt_tuning_get": (I, [C.POINTER(Tuning)]),
+    "mt_tuning_set": (I, [C.POINTER(Tuning)]),
     "mt_scene_set_texture": (I, [P, I, I, P, I, I]),
     "mt_scene_layout_read": (I, [P, P, P, PI, PI]),
     "mt_scene_destroy": (I, [P]),

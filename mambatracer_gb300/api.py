@@ -13,7 +13,7 @@ import threading
 import numpy as np
 
 from . import layout
-from ._lib import BatchFrame, RenderConfig, ServedStats, ServerConfig, check, lib
+from ._lib import BatchFrame, RenderConfig, ServedStats, ServerConfig, Tuning, check, lib
 
 
 def _p(a):
@@ -415,6 +415,25 @@ class Server:
             check(lib().mt_server_destroy(self.h))
             self.h = None
 
+
+
+TUNING_FIELDS = tuple(f for f, _ in Tuning._fields_)
+
+
+def get_tuning() -> dict:
+    """The process's launch shapes (mt_tuning_get)."""
+    t = Tuning()
+    check(lib().mt_tuning_get(C.byref(t)))
+    return {f: getattr(t, f) for f in TUNING_FIELDS}
+
+
+def set_tuning(tuning: dict | None = None, **fields):
+    """Install launch shapes (mt_tuning_set); fields not given keep their values."""
+    cur = get_tuning()
+    cur.update(tuning or {})
+    cur.update(fields)
+    t = Tuning(*(int(cur[f]) for f in TUNING_FIELDS))
+    check(lib().mt_tuning_set(C.byref(t)))
 
 
 def batch_render(ctx: Context, scene: Scene, frames, max_depth: int = 8, rr_depth: int = 3, film_kahan: int = 1):

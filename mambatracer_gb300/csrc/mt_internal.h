@@ -198,6 +198,7 @@ struct mt_job {
   const float4* film() const { return nslots > 1 ? d_film : slots[0].fb.film; }
   // adaptive light grid (mode 1, scene grid on, environment present)
   unsigned scene_version = 0;
+  unsigned tune_version = 0;  // launch-shape version the graphs were captured with
   int grid_on = 0, grid_fp64 = 0;
   int nu = 0, nv = 0, rx = 0, ry = 0;
   float* d_grid_func = nullptr;

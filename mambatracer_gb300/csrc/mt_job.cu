@@ -405,6 +405,16 @@ extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_coun
     if (r) return r;
     j->scene_version = j->scene->version;
   }
+  if (j->tune_version != tuning_version()) {
+    // new launch shapes: capture the frames' graphs again, once their frames ran
+    for (JobSlot& t : j->slots)
+      if (t.graph) {
+        CU(cudaStreamSynchronize(t.stream));
+        cudaGraphExecDestroy(t.graph);
+        t.graph = nullptr;
+      }
+    j->tune_version = tuning_version();
+  }
   JobSlot& s = j->slots[j->next];
   // The slot's previous frame must have consumed its pinned parameters; frames
   // on the other slots keep running meanwhile.

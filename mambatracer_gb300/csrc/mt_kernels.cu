@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 
 #include "mt_device.cuh"
@@ -137,8 +138,9 @@ struct ShadowResolve {
     }
   }
 };
-// traversal steps between two refill points of a warp: measured 576, 588, 608,
-// 614, 608, 595 Mrays/s at 8, 16, 32, 64, 128, 256 on the 1M soup
+// traversal steps between two refill points of a warp (the default of
+// Tuning::refill_steps): measured 576, 588, 608, 614, 608, 595 Mrays/s at 8,
+// 16, 32, 64, 128, 256 on the 1M soup
 constexpr int kSteps = 64;
 }  // namespace
 
@@ -147,25 +149,26 @@ constexpr int kSteps = 64;
 // the price of registers).
 // PREC: the BVH record format (0 FP32 child boxes, 1 FP16 outward-rounded).
 template <int MINB, int PREC>
-__global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_closest(DevScene S, Ctrl* ctrl, int b, FrameBufs fb) {
+__global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_closest(DevScene S, Ctrl* ctrl, int b, FrameBufs fb,
+                                                                       int steps) {
   const int count = ctrl->count[b];
   bool overflow = false;
   tr::trace_persistent<false, kSteps, QueueRays, HitOut, PREC>(
       S, count, &ctrl->work[2 * b], QueueRays{fb.q_o[(b + 1) & 1], fb.q_d[(b + 1) & 1]}, HitOut{fb.hit_t, fb.hit_prim},
-      &overflow);
+      &overflow, steps);
   if (overflow) atomicExch(&ctrl->error, kDevErrStack);
 }
 
 template <int MINB, int PREC>
 __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_shadow(DevScene S, Ctrl* ctrl, int b, int mode,
-                                                                      FrameBufs fb, int kahan) {
+                                                                      FrameBufs fb, int kahan, int steps) {
   // mode 0: shadow slots are the compacted survivor slots (flagged by pixel >= 0)
   const int count = mode == 0 ? ctrl->count[b + 1] : ctrl->shadow[b];
   bool overflow = false;
   unsigned traced = 0;
   tr::trace_persistent<true, kSteps, ShadowRays, ShadowResolve, PREC>(
       S, count, &ctrl->work[2 * b + 1], ShadowRays{fb.s_o, fb.s_d},
-      ShadowResolve{fb.s_o, fb.s_c, fb.film, fb.film_c, kahan, &traced}, &overflow);
+      ShadowResolve{fb.s_o, fb.s_c, fb.film, fb.film_c, kahan, &traced}, &overflow, steps);
   unsigned long long tot = traced;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
@@ -521,32 +524,31 @@ int grid_bps(const char* name, int dflt) {
   int x = e ? std::atoi(e) : dflt;
   return x >= 0 && x <= 32 ? x : dflt;
 }
-int trace_grid_bps() {
-  static int v = grid_bps("MT_TRACE_GRID", 0);
-  return v;
-}
-int shadow_grid_bps() {
-  static int v = grid_bps("MT_SHADOW_GRID", 0);
-  return v;
-}
-int trace_minb() {
-  static int v = env_minb("MT_TRACE_MINB", kTraceMinBlocksClosest);
-  return v;
-}
-int shadow_minb() {
-  static int v = env_minb("MT_SHADOW_MINB", kTraceMinBlocksShadow);
-  return v;
-}
 // Resident 256-thread blocks per SM the benchmark-semantics shading kernel is
 // bounded for (MT_SHADE_MINB: 3, 4 or 5).
-int shade_minb() {
-  static int v = [] {
-    const char* e = std::getenv("MT_SHADE_MINB");
-    int x = e ? std::atoi(e) : kShadeMinBlocks;
-    return (x == 3 || x == 4 || x == 5) ? x : kShadeMinBlocks;
-  }();
-  return v;
+int env_shade_minb() {
+  const char* e = std::getenv("MT_SHADE_MINB");
+  int x = e ? std::atoi(e) : kShadeMinBlocks;
+  return (x == 3 || x == 4 || x == 5) ? x : kShadeMinBlocks;
 }
+int env_steps() {
+  const char* e = std::getenv("MT_REFILL_STEPS");
+  int x = e ? std::atoi(e) : kSteps;
+  return x >= 4 && x <= 1024 ? x : kSteps;
+}
+// The process's launch shapes: the defaults above, the MT_* knobs, then
+// whatever set_tuning installs.
+Tuning& tuning_ref() {
+  static Tuning t = {env_minb("MT_TRACE_MINB", kTraceMinBlocksClosest), env_minb("MT_SHADOW_MINB", kTraceMinBlocksShadow),
+                     grid_bps("MT_TRACE_GRID", 0), grid_bps("MT_SHADOW_GRID", 0), env_shade_minb(), env_steps()};
+  return t;
+}
+std::atomic<unsigned> g_tuning_version{1};
+int trace_grid_bps() { return tuning_ref().closest_grid; }
+int shadow_grid_bps() { return tuning_ref().shadow_grid; }
+int trace_minb() { return tuning_ref().closest_minb; }
+int shadow_minb() { return tuning_ref().shadow_minb; }
+int shade_minb() { return tuning_ref().shade_minb; }
 // Resident blocks per SM of the benchmark-semantics shading kernel (its grid is
 // one resident wave of persistent warps).
 int shade_blocks_per_sm(int minb) {
@@ -565,19 +567,35 @@ int trace_blocks_per_sm() {
 template <int MINB>
 void launch_traces(cudaStream_t st, int grid, const DevScene& S, Ctrl* ctrl, int b, int mode, FrameBufs fb, int kahan,
                    bool closest) {
+  const int steps = tuning_ref().refill_steps;
   if (closest) {
     if (S.precision == 1)
-      k_trace_closest<MINB, 1><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb);
+      k_trace_closest<MINB, 1><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, steps);
     else
-      k_trace_closest<MINB, 0><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb);
+      k_trace_closest<MINB, 0><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, steps);
   } else {
     if (S.precision == 1)
-      k_trace_shadow<MINB, 1><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan);
+      k_trace_shadow<MINB, 1><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan, steps);
     else
-      k_trace_shadow<MINB, 0><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan);
+      k_trace_shadow<MINB, 0><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan, steps);
   }
 }
 }  // namespace
+
+Tuning get_tuning() { return tuning_ref(); }
+
+bool set_tuning(const Tuning& t) {
+  auto minb_ok = [](int x) { return x == 8 || x == 12 || x == 16; };
+  if (!minb_ok(t.closest_minb) || !minb_ok(t.shadow_minb) || t.closest_grid < 0 || t.closest_grid > 32 ||
+      t.shadow_grid < 0 || t.shadow_grid > 32 || t.shade_minb < 3 || t.shade_minb > 5 || t.refill_steps < 4 ||
+      t.refill_steps > 1024)
+    return false;
+  tuning_ref() = t;
+  g_tuning_version.fetch_add(1);
+  return true;
+}
+
+unsigned tuning_version() { return g_tuning_version.load(); }
 
 // One persistent traversal launch over a queue of at most N rays.
 void launch_trace(cudaStream_t st, const DevScene& S, Ctrl* ctrl, int b, int mode, FrameBufs fb, int kahan, bool closest,

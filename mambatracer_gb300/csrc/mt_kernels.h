@@ -22,6 +22,20 @@ struct FrameBufs {
   float4* film_c;   // Kahan compensation per pixel
 };
 
+// Launch shapes of the hot kernels, process-wide (one GPU per process):
+// closest_minb / shadow_minb: the traversal build, by the resident blocks per
+// SM its registers are bounded for (8, 12, 16); closest_grid / shadow_grid:
+// blocks per SM of a traversal launch that shares the GPU with other frames (0:
+// half of what fits); shade_minb: the benchmark-semantics shading build (3, 4,
+// 5); refill_steps: traversal steps between refills of finished lanes (4..1024).
+// Every choice gives the same results; only the speed differs.
+struct Tuning {
+  int closest_minb, shadow_minb, closest_grid, shadow_grid, shade_minb, refill_steps;
+};
+Tuning get_tuning();
+bool set_tuning(const Tuning& t);  // false when a field is out of range
+unsigned tuning_version();         // bumped by every set_tuning (jobs recapture their graphs)
+
 // events: optional array of 2 + 3 * max_depth events recorded around each launch.
 // totals: optional running ray counts [primary, extension, shadow, error] of the job.
 // shared: other frames or requests run beside this pass on the GPU (frames in

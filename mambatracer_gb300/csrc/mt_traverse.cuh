@@ -217,9 +217,11 @@ __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref,
 // finished its ray takes the next one from the global counter, so warps stay
 // full while rays of very different lengths run side by side.
 // Src: RayT load(int i); Dst: void store(int i, const RayT&, int hit_face).
+// steps: traversal steps a lane runs between two refill points (STEPS unless
+// given at run time).
 template <bool ANY, int STEPS, class Src, class Dst, int PREC = 0>
 __device__ __forceinline__ void trace_persistent(const DevScene& S, int count, int* work, Src src, Dst dst,
-                                                 bool* overflow) {
+                                                 bool* overflow, int steps = STEPS) {
   const int lane = threadIdx.x & 31;
   typename StackEntry<ANY>::type stack[kStackDepth];
   int i = -1;
@@ -250,7 +252,7 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, int count, i
     }
     const bool active = i >= 0;
     if (!__any_sync(0xffffffffu, active)) break;
-    if (active && trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, STEPS, overflow)) {
+    if (active && trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, steps, overflow)) {
       dst(i, r, hit);
       i = -1;
     }

@@ -1,0 +1,66 @@
+"""The launch-shape autotuner's host side: the coordinate-descent search, the
+tuning table behind mt_tuning_get / mt_tuning_set (no GPU needed) and the JSON a
+search persists."""
+import json
+
+import pytest
+
+from mambatracer_gb300 import api, tune
+from mambatracer_gb300._lib import MTError
+
+
+def test_search_finds_the_best_of_a_separable_score():
+    space = {"a": (1, 2, 3), "b": (10, 20, 30), "c": (0, 5)}
+    best_of = {"a": 3, "b": 20, "c": 5}
+    calls = []
+
+    def measure(t):
+        calls.append(dict(t))
+        return -sum(abs(t[k] - best_of[k]) for k in space)
+
+    best, score, trials = tune.search(measure, {"a": 1, "b": 10, "c": 0}, space, rounds=3)
+    assert best == best_of and score == 0
+    assert len(trials) == len(calls)  # each tuning measured once
+    assert len({tuple(sorted(t.items())) for t in calls}) == len(calls)
+
+
+def test_search_keeps_the_start_when_nothing_beats_it():
+    space = {"a": (1, 2), "b": (3, 4)}
+    best, score, trials = tune.search(lambda t: 1.0 if t == {"a": 1, "b": 3} else 0.5, {"a": 1, "b": 3}, space)
+    assert best == {"a": 1, "b": 3} and score == 1.0 and len(trials) == 3
+
+
+def test_tuning_table_round_trip_and_range_checks():
+    before = api.get_tuning()
+    assert set(before) == set(tune.SPACE)
+    try:
+        api.set_tuning(closest_minb=8, shadow_minb=16, closest_grid=3, shadow_grid=0, shade_minb=5, refill_steps=32)
+        assert api.get_tuning() == {"closest_minb": 8, "shadow_minb": 16, "closest_grid": 3, "shadow_grid": 0,
+                                    "shade_minb": 5, "refill_steps": 32}
+        for bad in ({"closest_minb": 10}, {"shadow_minb": 4}, {"closest_grid": 33}, {"shadow_grid": -1},
+                    {"shade_minb": 6}, {"refill_steps": 2}, {"refill_steps": 2048}):
+            with pytest.raises(MTError, match="out of range"):
+                api.set_tuning(bad)
+        assert api.get_tuning()["closest_minb"] == 8  # a refused tuning leaves the table alone
+    finally:
+        api.set_tuning(before)
+    assert api.get_tuning() == before
+
+
+def test_persisted_tuning_loads_only_on_a_matching_device(tmp_path, monkeypatch):
+    before = api.get_tuning()
+    dev = {"name": "a GPU", "sms": 152}
+    monkeypatch.setattr(tune, "device_info", lambda device=0: dict(dev))
+    res = {"device": dict(dev), "workload": "w", "tuning": dict(before, refill_steps=128), "mrays_per_s": 1.0,
+           "start": {"tuning": before, "mrays_per_s": 0.9}, "trials": []}
+    path = tmp_path / "t.json"
+    tune.save(str(path), res)
+    assert json.loads(path.read_text()) == res
+    try:
+        assert tune.load(str(path)) == res and api.get_tuning()["refill_steps"] == 128
+        api.set_tuning(before)
+        dev["sms"] = 148
+        assert tune.load(str(path)) is None and api.get_tuning() == before
+        assert tune.load(str(path), require_match=False) == res and api.get_tuning()["refill_steps"] == 128
+    finally:
+        api.set_tuning(before)
