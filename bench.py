@@ -76,11 +76,16 @@ def make_scene(kind, small, width, height):
 TUNED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "mambatracer_gb300", "tuning_gb300.json")
 
 
-def apply_tuning():
+def apply_tuning(workload_key=None):
     """Installs the launch shapes the autotuner (mambatracer_gb300.tune) persisted for
-    this GPU model, when the file exists and matches; returns what the run uses."""
+    this GPU model and for this workload, when the file exists and matches; returns
+    what the run uses."""
     from mambatracer_gb300 import api, tune
-    res = tune.load(TUNED) if os.path.exists(TUNED) else None
+    res = None
+    if workload_key and os.path.exists(TUNED):
+        with open(TUNED) as f:
+            if json.load(f).get("workload_key") == workload_key:
+                res = tune.load(TUNED)
     if res is None:
         return {"source": "built-in defaults", "tuning": api.get_tuning()}
     return {"source": "autotuned (mambatracer_gb300/tuning_gb300.json: " + res["workload"] + ")",
@@ -258,7 +263,8 @@ def run_gpu(args):
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     from mambatracer_gb300 import api, build, scenes
     build.build()
-    launch_shapes = apply_tuning()
+    launch_shapes = apply_tuning(f"soup{NTRI}_{W_DEFAULT}x{H_DEFAULT}"
+                                 if args.workload == "soup" and not args.small else None)
 
     width, height = (640, 360) if args.small and args.workload != "room" else (W_DEFAULT, H_DEFAULT)
     spp = WORKLOADS[args.workload]["spp"]
@@ -499,7 +505,20 @@ def run_served(args):
     the served-mode scheduler, against the same requests run one at a time."""
     from mambatracer_gb300 import api, build, scenes
     build.build()
-    launch_shapes = apply_tuning()
+    launch_shapes = apply_tuning()  # the built-in launch shapes: the file's are for the soup
+    served_shape = {"lanes": 64, "merge_streams": 4, "source": "built-in defaults"}
+    if os.path.exists(TUNED):
+        from mambatracer_gb300 import tune
+        with open(TUNED) as f:
+            tuned_file = json.load(f)
+        tuned = tuned_file.get("served") if tuned_file.get("device") == tune.device_info() else None
+        if tuned:
+            served_shape = {"lanes": tuned["lanes"], "merge_streams": tuned["merge_streams"],
+                            "source": "autotuned (mambatracer_gb300/tuning_gb300.json)"}
+    if args.merged_lanes is not None or args.merge_streams is not None:
+        served_shape = {"lanes": args.merged_lanes or served_shape["lanes"],
+                        "merge_streams": args.merge_streams or served_shape["merge_streams"], "source": "command line"}
+    launch_shapes["merged_queues"] = served_shape
     ctx = api.Context(0)
     env = scenes.sky_env(ENV_W, ENV_H)
     S = {}
@@ -521,7 +540,7 @@ def run_served(args):
     # warm-up: a few small requests through a one-lane server
     run_requests(ctx, S, [(0.0, k, 64, 64, 1, 1) for k in keys], 1, budget, api)
     res = {}
-    for name, lanes, merged in (("served_merged", args.merged_lanes, args.merge_streams),
+    for name, lanes, merged in (("served_merged", served_shape["lanes"], served_shape["merge_streams"]),
                                 ("concurrent", args.lanes, 0), ("sequential", 1, 0)):
         st, wall = run_requests(ctx, S, reqs, lanes, budget, api, merged)
         rays = int(sum(st["rays"]))
@@ -551,7 +570,7 @@ def run_served(args):
                          "how": "mt_batch_render per scene (its 32 requests through one set of queues), "
                                 "queues allocated and films copied to host inside the timed region"}
     pixels = sum(w * h * spp for _, _, w, h, spp, _ in reqs)
-    # the scheduler with merged queues (64 requests in flight on 4 streams); the batched
+    # the scheduler with merged queues (autotuned requests in flight and streams); the batched
     # workload also reports one mt_batch_render call per scene ("merged")
     head = res["served_merged"]
     out = {
@@ -707,8 +726,10 @@ def main():
                     help="BVH records: 0 FP32 child boxes (64 B), 1 FP16 outward-rounded (32 B)")
     ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS) + ["batched", "served", "plain"])
     ap.add_argument("--lanes", type=int, default=8, help="batched/served: requests in flight, a stream each")
-    ap.add_argument("--merged-lanes", type=int, default=64, help="batched/served: requests in flight, merged queues")
-    ap.add_argument("--merge-streams", type=int, default=4, help="batched/served: streams of the merged queues")
+    ap.add_argument("--merged-lanes", type=int, default=None,
+                    help="batched/served: requests sharing the merged queues (default: the autotuned value, else 64)")
+    ap.add_argument("--merge-streams", type=int, default=None,
+                    help="batched/served: streams of the merged queues (default: the autotuned value, else 4)")
     ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="served: seconds of arrivals")
     args = ap.parse_args()

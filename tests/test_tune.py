@@ -64,3 +64,24 @@ def test_persisted_tuning_loads_only_on_a_matching_device(tmp_path, monkeypatch)
         assert tune.load(str(path), require_match=False) == res and api.get_tuning()["refill_steps"] == 128
     finally:
         api.set_tuning(before)
+
+
+def test_search_ignores_gains_inside_the_noise_and_confirms_the_winner():
+    space = {"a": (1, 2, 3)}
+    # a=2 scores 0.5 % above the start: inside min_gain, never adopted
+    best, _, _ = tune.search(lambda t: {1: 100.0, 2: 100.5, 3: 99.0}[t["a"]], {"a": 1}, space, min_gain=0.01)
+    assert best == {"a": 1}
+    # a=3 looks 5 % better once, but not when measured again: the start is kept
+    seen = {"n": 0}
+
+    def flaky(t):
+        if t["a"] == 3:
+            seen["n"] += 1
+            return 105.0 if seen["n"] == 1 else 99.0
+        return 100.0
+
+    best, score, trials = tune.search(flaky, {"a": 1}, space, min_gain=0.01, confirm=2)
+    assert best == {"a": 1} and score == 100.0 and seen["n"] == 3
+    # a real gain survives the confirmation
+    best, score, _ = tune.search(lambda t: 100.0 + 3 * (t["a"] == 3), {"a": 1}, space, min_gain=0.01, confirm=2)
+    assert best == {"a": 3} and score == 103.0
