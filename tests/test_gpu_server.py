@@ -126,3 +126,40 @@ def test_merged_cancel_running_request(ctx, served_scenes):
         assert srv.film(rid).tobytes() == J.film().tobytes()
         J.close()
     srv.close()
+
+
+def test_merged_mixed_scenes_equal_jobs_alone(ctx):
+    """One merged server over a textured scene, a scene with FP16 records and a scene
+    with FP32 records: rounds hold one merged pass per scene, and every film equals the
+    request rendered alone as a job."""
+    rng = np.random.default_rng(14)
+    tex = scenes.textured_room(64, 48)
+    S_tex = api.Scene(ctx, tex)
+    S_tex.build_bvh_device(want_arrays=False)
+    soup = scenes.soup(20000, seed=9, extent=0.8)
+    S16 = api.Scene(ctx, soup)
+    S16.build_bvh_device(want_arrays=False)
+    S16.set_env(scenes.sky_env(256, 128), 256, 128)
+    S16.set_precision(1)
+    S32 = api.Scene(ctx, soup)
+    S32.build_bvh_device(want_arrays=False)
+    S32.set_env(scenes.sky_env(256, 128), 256, 128)
+    srv = api.Server(ctx, lanes=5, max_width=160, max_height=120, max_spp=4, max_depth=DEPTH, rr_depth=RR, merged=2)
+    reqs = []
+    for k in range(12):
+        S, sc = ((S_tex, tex), (S16, soup), (S32, soup))[k % 3]
+        w, h = int(rng.integers(16, 160)), int(rng.integers(16, 120))
+        cam = tex.camera.copy() if S is S_tex else sphere_camera(rng, w, h, 3.0)
+        spp, fc = int(rng.integers(1, 5)), float(3 + 7 * k)
+        reqs.append((srv.submit(S, cam, w, h, spp, fc), S, cam, w, h, spp, fc))
+    srv.drain()
+    assert srv.stats()["completed"] == len(reqs)
+    for rid, S, cam, w, h, spp, fc in reqs:
+        J = api.Job(ctx, S, w, h, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, spp=spp)
+        J.set_camera(cam)
+        J.render(None, fc)
+        assert srv.film(rid).tobytes() == J.film().tobytes(), (rid, w, h, spp)
+        J.close()
+    srv.close()
+    for S in (S_tex, S16, S32):
+        S.close()
