@@ -303,6 +303,7 @@ typedef struct mt_tuning {
   int closest_grid, shadow_grid; /* blocks per SM of a shared traversal launch, 0..32 (0: half of what fits) */
   int shade_minb;                /* shading build: 3, 4 or 5 blocks of 256 threads per SM */
   int refill_steps;              /* traversal steps between lane refills, 4..1024 */
+  int shadow_stream;             /* 1: a frame's shadow rays run beside its next bounce's extension rays; 0 or 1 */
 } mt_tuning;
 int mt_tuning_get(mt_tuning* out);
 int mt_tuning_set(const mt_tuning* in); /* MT_ERR_INVALID when a field is out of range */

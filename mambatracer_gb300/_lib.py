@@ -44,7 +44,8 @@ class ServerConfig(C.Structure):
 class Tuning(C.Structure):
     """mt_tuning"""
     _fields_ = [("closest_minb", C.c_int), ("shadow_minb", C.c_int), ("closest_grid", C.c_int),
-                ("shadow_grid", C.c_int), ("shade_minb", C.c_int), ("refill_steps", C.c_int)]
+                ("shadow_grid", C.c_int), ("shade_minb", C.c_int), ("refill_steps", C.c_int),
+                ("shadow_stream", C.c_int)]
 
 
 class ServedStats(C.Structure):

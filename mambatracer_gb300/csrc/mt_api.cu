@@ -869,17 +869,20 @@ extern "C" int mt_trace_closest(mt_scene* s, const void* rays, int n, float* t_o
 extern "C" int mt_tuning_get(mt_tuning* out) {
   if (!out) return fail(MT_ERR_INVALID, "NULL argument");
   const Tuning t = get_tuning();
-  *out = mt_tuning{t.closest_minb, t.shadow_minb, t.closest_grid, t.shadow_grid, t.shade_minb, t.refill_steps};
+  *out = mt_tuning{t.closest_minb, t.shadow_minb, t.closest_grid, t.shadow_grid, t.shade_minb, t.refill_steps,
+                   t.shadow_stream};
   return MT_OK;
 }
 
 extern "C" int mt_tuning_set(const mt_tuning* in) {
   if (!in) return fail(MT_ERR_INVALID, "NULL argument");
-  const Tuning t{in->closest_minb, in->shadow_minb, in->closest_grid, in->shadow_grid, in->shade_minb, in->refill_steps};
+  const Tuning t{in->closest_minb, in->shadow_minb, in->closest_grid, in->shadow_grid,
+                 in->shade_minb,   in->refill_steps, in->shadow_stream};
   if (!set_tuning(t))
     return fail(MT_ERR_INVALID, "tuning out of range: minb %d/%d (8, 12, 16), grids %d/%d (0..32), shade %d (3..5), "
-                                "steps %d (4..1024)",
-                t.closest_minb, t.shadow_minb, t.closest_grid, t.shadow_grid, t.shade_minb, t.refill_steps);
+                                "steps %d (4..1024), shadow_stream %d (0, 1)",
+                t.closest_minb, t.shadow_minb, t.closest_grid, t.shadow_grid, t.shade_minb, t.refill_steps,
+                t.shadow_stream);
   return MT_OK;
 }
 

@@ -158,6 +158,8 @@ struct JobSlot {
   PassParams* h_pp = nullptr;              // pinned, one per pass
   PassParams* d_pp = nullptr;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // shadow rays beside the next bounce's extension rays
+  cudaEvent_t sfork = nullptr, sjoin = nullptr;
   cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr, done = nullptr;
   cudaGraphExec_t graph = nullptr;
   unsigned graph_version = 0;  // scene version the graph was captured against

@@ -109,12 +109,14 @@ void free_slot(JobSlot& s) {
   s.h_pp = nullptr;
   if (s.graph) cudaGraphExecDestroy(s.graph);
   s.graph = nullptr;
-  for (cudaEvent_t* e : {&s.fork, &s.ev0, &s.ev1, &s.done}) {
+  for (cudaEvent_t* e : {&s.fork, &s.ev0, &s.ev1, &s.done, &s.sfork, &s.sjoin}) {
     if (*e) cudaEventDestroy(*e);
     *e = nullptr;
   }
   if (s.stream) cudaStreamDestroy(s.stream);
   s.stream = nullptr;
+  if (s.side) cudaStreamDestroy(s.side);
+  s.side = nullptr;
 }
 
 void free_job(mt_job* j) {
@@ -187,8 +189,12 @@ int alloc_slot(JobSlot& s, size_t N, int spp, int max_depth, size_t status_strid
     r = fail(MT_ERR_NOMEM, "pinned pass parameters");
   if (!r && cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess)
     r = fail(MT_ERR_CUDA, "stream create");
+  if (!r && cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking) != cudaSuccess)
+    r = fail(MT_ERR_CUDA, "stream create");
   for (cudaEvent_t* e : {&s.fork, &s.ev0, &s.ev1, &s.done})
     if (!r && cudaEventCreate(e) != cudaSuccess) r = fail(MT_ERR_CUDA, "event create");
+  for (cudaEvent_t* e : {&s.sfork, &s.sjoin})
+    if (!r && cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) r = fail(MT_ERR_CUDA, "event create");
   if (!r) std::memset(s.h_pp, 0, sizeof(PassParams) * spp);
   return r;
 }
@@ -378,7 +384,7 @@ int enqueue_frame(mt_job* j, JobSlot& s) {
     cudaEvent_t* ev = j->kev.empty() ? nullptr : j->kev.data() + per_pass_events * p;
     if (launch_pass(s.stream, S, E, s.d_pp + p, c.mode, c.max_depth, c.film_kahan, c.width, c.height, s.d_ctrl + p,
                     s.fb, s.d_status + j->status_stride * (size_t)c.max_depth * p, j->status_stride, ctx->num_sms,
-                    ev, j->d_totals, j->nslots > 1))
+                    ev, j->d_totals, j->nslots > 1, s.side, s.sfork, s.sjoin))
       return fail(MT_ERR_CUDA, "pass launch: %s", cudaGetErrorString(cudaGetLastError()));
   }
   return MT_OK;

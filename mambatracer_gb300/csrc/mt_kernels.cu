@@ -540,7 +540,8 @@ int env_steps() {
 // whatever set_tuning installs.
 Tuning& tuning_ref() {
   static Tuning t = {env_minb("MT_TRACE_MINB", kTraceMinBlocksClosest), env_minb("MT_SHADOW_MINB", kTraceMinBlocksShadow),
-                     grid_bps("MT_TRACE_GRID", 0), grid_bps("MT_SHADOW_GRID", 0), env_shade_minb(), env_steps()};
+                     grid_bps("MT_TRACE_GRID", 0), grid_bps("MT_SHADOW_GRID", 0), env_shade_minb(), env_steps(),
+                     std::getenv("MT_SHADOW_STREAM") && std::atoi(std::getenv("MT_SHADOW_STREAM")) == 0 ? 0 : 1};
   return t;
 }
 std::atomic<unsigned> g_tuning_version{1};
@@ -588,7 +589,7 @@ bool set_tuning(const Tuning& t) {
   auto minb_ok = [](int x) { return x == 8 || x == 12 || x == 16; };
   if (!minb_ok(t.closest_minb) || !minb_ok(t.shadow_minb) || t.closest_grid < 0 || t.closest_grid > 32 ||
       t.shadow_grid < 0 || t.shadow_grid > 32 || t.shade_minb < 3 || t.shade_minb > 5 || t.refill_steps < 4 ||
-      t.refill_steps > 1024)
+      t.refill_steps > 1024 || (t.shadow_stream != 0 && t.shadow_stream != 1))
     return false;
   tuning_ref() = t;
   g_tuning_version.fetch_add(1);
@@ -614,9 +615,16 @@ void launch_trace(cudaStream_t st, const DevScene& S, Ctrl* ctrl, int b, int mod
 
 int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassParams* d_pp, int mode, int max_depth,
                 int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb, unsigned long long* status,
-                size_t status_stride, int num_sms, cudaEvent_t* ev, unsigned long long* totals, bool shared) {
+                size_t status_stride, int num_sms, cudaEvent_t* ev, unsigned long long* totals, bool shared,
+                cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
   const int N = width * height;
   static int shade_bps[6] = {};
+  // shadow rays of bounce b beside the extension rays of bounce b + 1 (benchmark
+  // semantics, no per-kernel events): both read only what shading b wrote, and
+  // shading b + 1, which rewrites the shadow queue and adds to the film after
+  // the shadow kernel's adds, waits for them
+  const bool split = side && fork && join && mode == 1 && !ev && tuning_ref().shadow_stream;
+  if (split) shared = true;
   auto trace = [&](bool closest, int b) { launch_trace(st, S, ctrl, b, mode, fb, kahan, closest, N, num_sms, shared); };
   // persistent traversal: one resident wave, or fewer blocks for a small frame
   // (a queue never exceeds the frame's pixels), leaving SMs to other streams
@@ -628,6 +636,7 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
   for (int b = 1; b <= max_depth; ++b) {
     trace(true, b);
     if (ev) cudaEventRecord(ev[e++], st);
+    if (split && b > 1) cudaStreamWaitEvent(st, join, 0);
     unsigned long long* stb = status + (size_t)(b - 1) * status_stride;
     if (mode == 0) {
       if (S.tex_on)
@@ -651,9 +660,17 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
         k_shade<3><<<sgrid, kShadeThreads, 0, st>>>(S, E, OneFrame{d_pp}, ctrl, b, fb);
     }
     if (ev) cudaEventRecord(ev[e++], st);
-    trace(false, b);
+    if (split) {
+      cudaEventRecord(fork, st);
+      cudaStreamWaitEvent(side, fork, 0);
+      launch_trace(side, S, ctrl, b, mode, fb, kahan, false, N, num_sms, shared);
+      cudaEventRecord(join, side);
+    } else {
+      trace(false, b);
+    }
     if (ev) cudaEventRecord(ev[e++], st);
   }
+  if (split) cudaStreamWaitEvent(st, join, 0);
   if (totals) k_accumulate<<<1, 32, 0, st>>>(ctrl, max_depth, N, totals);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -27,10 +27,12 @@ struct FrameBufs {
 // SM its registers are bounded for (8, 12, 16); closest_grid / shadow_grid:
 // blocks per SM of a traversal launch that shares the GPU with other frames (0:
 // half of what fits); shade_minb: the benchmark-semantics shading build (3, 4,
-// 5); refill_steps: traversal steps between refills of finished lanes (4..1024).
+// 5); refill_steps: traversal steps between refills of finished lanes (4..1024);
+// shadow_stream: a frame's shadow rays of bounce b run on a second stream beside
+// its extension rays of bounce b + 1 (1) or after them on one stream (0).
 // Every choice gives the same results; only the speed differs.
 struct Tuning {
-  int closest_minb, shadow_minb, closest_grid, shadow_grid, shade_minb, refill_steps;
+  int closest_minb, shadow_minb, closest_grid, shadow_grid, shade_minb, refill_steps, shadow_stream;
 };
 Tuning get_tuning();
 bool set_tuning(const Tuning& t);  // false when a field is out of range
@@ -41,6 +43,8 @@ unsigned tuning_version();         // bumped by every set_tuning (jobs recapture
 // shared: other frames or requests run beside this pass on the GPU (frames in
 // flight, served lanes): each persistent traversal launch then takes half the
 // blocks an SM can hold, leaving room for their kernels.
+// side, fork, join: a second stream and two events of the caller's; with the
+// tuning's shadow_stream on, benchmark-semantics shadow rays run there.
 // A merged batch pass (benchmark semantics, full-map environment sampling):
 // frames 0 .. nframes-1 share the queues; path g belongs to the frame k with
 // d_start[k] <= g < d_start[k+1] (pixel g - d_start[k]), its film slots start at
@@ -51,7 +55,8 @@ int launch_batch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const
 int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassParams* d_pp, int mode,
                 int max_depth, int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb,
                 unsigned long long* status, size_t status_stride, int num_sms, cudaEvent_t* events,
-                unsigned long long* totals, bool shared = false);
+                unsigned long long* totals, bool shared = false, cudaStream_t side = nullptr,
+                cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 
 int launch_query(cudaStream_t st, const DevScene& S, const float4* rays, int n, int any, float* t_out,
                  int* prim_out, int* work, int* err, int num_sms);

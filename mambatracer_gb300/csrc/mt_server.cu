@@ -67,6 +67,8 @@ struct Request {
 
 struct Lane {
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // shadow rays beside the next bounce's extension rays
+  cudaEvent_t sfork = nullptr, sjoin = nullptr;
   FrameBufs fb{};
   Ctrl* d_ctrl = nullptr;
   unsigned long long* d_status = nullptr;
@@ -183,6 +185,12 @@ void free_lane(Lane& L) {
   L.h_stage = nullptr;
   if (L.stream) cudaStreamDestroy(L.stream);
   L.stream = nullptr;
+  if (L.side) cudaStreamDestroy(L.side);
+  L.side = nullptr;
+  for (cudaEvent_t* e : {&L.sfork, &L.sjoin}) {
+    if (*e) cudaEventDestroy(*e);
+    *e = nullptr;
+  }
 }
 
 int alloc_lane(Lane& L, size_t N, int spp, int depth, size_t stride) {
@@ -210,6 +218,10 @@ int alloc_lane(Lane& L, size_t N, int spp, int depth, size_t stride) {
     r = fail(MT_ERR_NOMEM, "pinned film staging");
   if (!r && cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking) != cudaSuccess)
     r = fail(MT_ERR_CUDA, "stream create");
+  if (!r && cudaStreamCreateWithFlags(&L.side, cudaStreamNonBlocking) != cudaSuccess)
+    r = fail(MT_ERR_CUDA, "stream create");
+  for (cudaEvent_t* e : {&L.sfork, &L.sjoin})
+    if (!r && cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) r = fail(MT_ERR_CUDA, "event create");
   if (!r) std::memset(L.h_pp, 0, sizeof(PassParams) * spp);
   return r;
 }
@@ -241,7 +253,7 @@ int start_request(mt_server* s, Lane& L, Request* R) {
   for (int p = 0; p < R->spp; ++p)
     if (launch_pass(L.stream, S, E, L.d_pp + p, 1, c.max_depth, c.film_kahan, R->width, R->height, L.d_ctrl + p,
                     L.fb, L.d_status + stride * (size_t)c.max_depth * p, stride, s->ctx->num_sms, nullptr,
-                    s->d_totals, s->lanes.size() > 1))
+                    s->d_totals, s->lanes.size() > 1, L.side, L.sfork, L.sjoin))
       return fail(MT_ERR_CUDA, "pass launch: %s", cudaGetErrorString(cudaGetLastError()));
   CU(cudaMemcpyAsync(L.h_stage, L.fb.film, N * 16, cudaMemcpyDeviceToHost, L.stream));
   CU(cudaLaunchHostFunc(L.stream, lane_done, &L));
@@ -521,6 +533,7 @@ void worker_main(mt_server* s) {
       if (r) {
         // nothing of this request is left on the lane's stream that could call back
         cudaStreamSynchronize(free_lane_p->stream);
+        cudaStreamSynchronize(free_lane_p->side);
         R->state = kFailed;
         R->error = mt_last_error();
         s->used_bytes -= R->bytes;
@@ -664,7 +677,8 @@ extern "C" int mt_server_destroy(mt_server* s) {
     for (MergeGroup& G : s->groups)
       if (G.stream) cudaStreamSynchronize(G.stream);
     for (Lane& L : s->lanes) {
-      if (L.stream) cudaStreamSynchronize(L.stream);
+      for (cudaStream_t q : {L.stream, L.side})
+        if (q) cudaStreamSynchronize(q);
       free_lane(L);
     }
     free_merged(s);
@@ -810,6 +824,7 @@ void servers_sync(mt_context* ctx) {
     for (MergeGroup& G : s->groups)
       if (G.stream) cudaStreamSynchronize(G.stream);
     for (Lane& L : s->lanes)
-      if (L.stream) cudaStreamSynchronize(L.stream);
+      for (cudaStream_t q : {L.stream, L.side})
+        if (q) cudaStreamSynchronize(q);
   }
 }

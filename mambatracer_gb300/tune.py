@@ -36,6 +36,7 @@ SPACE = {
     "shadow_grid": (0, 3, 4, 6),
     "shade_minb": (3, 4, 5),
     "refill_steps": (32, 64, 128),
+    "shadow_stream": (0, 1),
 }
 
 

@@ -11,7 +11,7 @@ from tests.helpers import bvh_build
 pytestmark = pytest.mark.gpu
 
 OTHER = {"closest_minb": 8, "shadow_minb": 16, "closest_grid": 3, "shadow_grid": 6, "shade_minb": 3,
-         "refill_steps": 16}
+         "refill_steps": 16, "shadow_stream": 0}
 
 
 @pytest.fixture

@@ -34,11 +34,12 @@ def test_tuning_table_round_trip_and_range_checks():
     before = api.get_tuning()
     assert set(before) == set(tune.SPACE)
     try:
-        api.set_tuning(closest_minb=8, shadow_minb=16, closest_grid=3, shadow_grid=0, shade_minb=5, refill_steps=32)
+        api.set_tuning(closest_minb=8, shadow_minb=16, closest_grid=3, shadow_grid=0, shade_minb=5, refill_steps=32,
+                       shadow_stream=1)
         assert api.get_tuning() == {"closest_minb": 8, "shadow_minb": 16, "closest_grid": 3, "shadow_grid": 0,
-                                    "shade_minb": 5, "refill_steps": 32}
+                                    "shade_minb": 5, "refill_steps": 32, "shadow_stream": 1}
         for bad in ({"closest_minb": 10}, {"shadow_minb": 4}, {"closest_grid": 33}, {"shadow_grid": -1},
-                    {"shade_minb": 6}, {"refill_steps": 2}, {"refill_steps": 2048}):
+                    {"shade_minb": 6}, {"refill_steps": 2}, {"refill_steps": 2048}, {"shadow_stream": 2}):
             with pytest.raises(MTError, match="out of range"):
                 api.set_tuning(bad)
         assert api.get_tuning()["closest_minb"] == 8  # a refused tuning leaves the table alone
