@@ -619,11 +619,12 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
                 cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
   const int N = width * height;
   static int shade_bps[6] = {};
-  // shadow rays of bounce b beside the extension rays of bounce b + 1 (benchmark
-  // semantics, no per-kernel events): both read only what shading b wrote, and
-  // shading b + 1, which rewrites the shadow queue and adds to the film after
-  // the shadow kernel's adds, waits for them
-  const bool split = side && fork && join && mode == 1 && !ev && tuning_ref().shadow_stream;
+  // shadow rays of bounce b beside the extension rays of bounce b + 1 (no
+  // per-kernel events): both read only what shading b wrote (in reference
+  // semantics both read its survivor count), and shading b + 1, which rewrites
+  // the shadow queue and adds to the film after the shadow kernel's adds, waits
+  // for them
+  const bool split = side && fork && join && !ev && tuning_ref().shadow_stream;
   if (split) shared = true;
   auto trace = [&](bool closest, int b) { launch_trace(st, S, ctrl, b, mode, fb, kahan, closest, N, num_sms, shared); };
   // persistent traversal: one resident wave, or fewer blocks for a small frame

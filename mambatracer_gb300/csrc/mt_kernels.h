@@ -44,7 +44,7 @@ unsigned tuning_version();         // bumped by every set_tuning (jobs recapture
 // flight, served lanes): each persistent traversal launch then takes half the
 // blocks an SM can hold, leaving room for their kernels.
 // side, fork, join: a second stream and two events of the caller's; with the
-// tuning's shadow_stream on, benchmark-semantics shadow rays run there.
+// tuning's shadow_stream on, the shadow rays run there.
 // A merged batch pass (benchmark semantics, full-map environment sampling):
 // frames 0 .. nframes-1 share the queues; path g belongs to the frame k with
 // d_start[k] <= g < d_start[k+1] (pixel g - d_start[k]), its film slots start at
