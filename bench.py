@@ -540,8 +540,11 @@ def run_served(args):
     # warm-up: a few small requests through a one-lane server
     run_requests(ctx, S, [(0.0, k, 64, 64, 1, 1) for k in keys], 1, budget, api)
     res = {}
+    arms = set(args.arms.split(",")) | {"served_merged"}
     for name, lanes, merged in (("served_merged", served_shape["lanes"], served_shape["merge_streams"]),
                                 ("concurrent", args.lanes, 0), ("sequential", 1, 0)):
+        if name not in arms:
+            continue
         st, wall = run_requests(ctx, S, reqs, lanes, budget, api, merged)
         rays = int(sum(st["rays"]))
         res[name] = {"lanes": lanes, "merge_streams": merged, "mrays_per_s": round(rays / (st["span_ms"] * 1e-3) / 1e6, 2),
@@ -549,7 +552,7 @@ def run_served(args):
                      "p99_ms": round(st["p99_ms"], 2), "max_ms": round(st["max_ms"], 2),
                      "span_s": round(st["span_ms"] * 1e-3, 3), "wall_s": round(wall, 3),
                      "completed": st["completed"], "max_queue": st["max_queue"], "rays": st["rays"]}
-    if args.workload == "batched":
+    if args.workload == "batched" and "merged" in arms:
         # merged: each scene's requests as one batch through shared wavefront queues
         t0 = time.perf_counter()
         rays3 = np.zeros(3, np.int64)
@@ -578,9 +581,10 @@ def run_served(args):
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (procedural scenes and sky; no dataset)",
         "workload": args.workload, "requests": len(reqs), "samples": pixels,
         "latency_ms": {k: head[k] for k in ("p50_ms", "p95_ms", "p99_ms", "max_ms")},
-        "served_merged": res["served_merged"], "concurrent": res["concurrent"], "sequential": res["sequential"],
-        "merged": res.get("merged"),
-        "speedup_vs_sequential": round(head["mrays_per_s"] / res["sequential"]["mrays_per_s"], 3),
+        "served_merged": res["served_merged"], "concurrent": res.get("concurrent"),
+        "sequential": res.get("sequential"), "merged": res.get("merged"),
+        "speedup_vs_sequential": (round(head["mrays_per_s"] / res["sequential"]["mrays_per_s"], 3)
+                                  if "sequential" in res else None),
         "config": {
             "requests": ("64 jobs submitted at once, soup and stadium alternately, 4 spp" if args.workload == "batched"
                          else f"Poisson arrivals at {args.rate}/s for {args.duration} s, box room / soup / stadium "
@@ -732,6 +736,8 @@ def main():
                     help="batched/served: streams of the merged queues (default: the autotuned value, else 4)")
     ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="served: seconds of arrivals")
+    ap.add_argument("--arms", default="served_merged,concurrent,sequential,merged",
+                    help="batched/served: the schedulers to run (served_merged always runs: it is the value)")
     args = ap.parse_args()
     w = WORKLOADS.get(args.workload)
     if w is not None and "depth" in w:  # a workload with its own frame, depth and lighting
