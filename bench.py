@@ -515,6 +515,12 @@ def run_served(args):
         if tuned:
             served_shape = {"lanes": tuned["lanes"], "merge_streams": tuned["merge_streams"],
                             "source": "autotuned (mambatracer_gb300/tuning_gb300.json)"}
+    if args.workload == "served":
+        # a request stream keeps thousands queued: more slots fill each merged round
+        # (measured on this stream: 64 1287, 96 1348, 128 1390, 160 1418, 192 1429, 256 1436
+        # Mrays/s on 4 streams); the batched search above sees only 64 requests
+        served_shape = {"lanes": 192, "merge_streams": served_shape["merge_streams"],
+                        "source": "measured on the served request stream (192 slots)"}
     if args.merged_lanes is not None or args.merge_streams is not None:
         served_shape = {"lanes": args.merged_lanes or served_shape["lanes"],
                         "merge_streams": args.merge_streams or served_shape["merge_streams"], "source": "command line"}

@@ -338,7 +338,7 @@ int mt_trace_closest_dev(mt_scene* scene, mt_buffer* rays, int n, mt_buffer* t_o
  * for bit, in both modes. */
 typedef struct mt_server mt_server;
 typedef struct mt_server_config {
-  int lanes;                 /* requests in flight at once (1..64) */
+  int lanes;                 /* requests in flight at once (1..256) */
   int max_width, max_height; /* largest frame (its pixel count bounds every request) */
   int max_spp;               /* largest spp per request */
   int max_depth;             /* bounces per path */

@@ -623,7 +623,7 @@ double percentile(std::vector<double> v, double q) {
 extern "C" int mt_server_create(mt_context* ctx, const mt_server_config* cfg, mt_server** out) {
   if (!ctx || !cfg || !out) return fail(MT_ERR_INVALID, "NULL argument");
   const mt_server_config& c = *cfg;
-  if (c.lanes < 1 || c.lanes > 64) return fail(MT_ERR_INVALID, "lanes %d (1..64)", c.lanes);
+  if (c.lanes < 1 || c.lanes > 256) return fail(MT_ERR_INVALID, "lanes %d (1..256)", c.lanes);
   if (c.max_width <= 0 || c.max_height <= 0 || (long long)c.max_width * c.max_height > (1ll << 26))
     return fail(MT_ERR_INVALID, "largest frame %d x %d", c.max_width, c.max_height);
   if (c.max_spp < 1 || c.max_spp > 4096) return fail(MT_ERR_INVALID, "max_spp %d", c.max_spp);
