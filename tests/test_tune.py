@@ -86,3 +86,25 @@ def test_search_ignores_gains_inside_the_noise_and_confirms_the_winner():
     # a real gain survives the confirmation
     best, score, _ = tune.search(lambda t: 100.0 + 3 * (t["a"] == 3), {"a": 1}, space, min_gain=0.01, confirm=2)
     assert best == {"a": 3} and score == 103.0
+
+
+def test_bench_installs_shapes_only_for_their_workload_and_device(tmp_path, monkeypatch):
+    import bench
+    before = api.get_tuning()
+    dev = {"name": "a GPU", "sms": 152}
+    monkeypatch.setattr(tune, "device_info", lambda device=0: dict(dev))
+    path = tmp_path / "tuning.json"
+    tune.save(str(path), {"device": dict(dev), "workload": "the soup", "workload_key": "soup1000000_1920x1080",
+                          "tuning": dict(before, refill_steps=32), "mrays_per_s": 1.0, "start": {}, "trials": []})
+    monkeypatch.setattr(bench, "TUNED", str(path))
+    try:
+        assert bench.apply_tuning(None)["source"] == "built-in defaults"
+        assert bench.apply_tuning("stadium3310720_1920x1080")["source"] == "built-in defaults"
+        assert api.get_tuning() == before
+        got = bench.apply_tuning("soup1000000_1920x1080")
+        assert got["source"].startswith("autotuned") and got["tuning"]["refill_steps"] == 32
+        api.set_tuning(before)
+        dev["sms"] = 148  # another GPU model
+        assert bench.apply_tuning("soup1000000_1920x1080")["source"] == "built-in defaults"
+    finally:
+        api.set_tuning(before)
