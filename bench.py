@@ -108,7 +108,9 @@ def config_dict(kind, width, height, ntri, world, inflight=1, small=False):
                        if ENV_ON else "none"),
         "resolution": f"{width}x{height}", "spp_per_step": w["spp"], "max_depth": DEPTH, "rr_from_bounce": RR,
         "rng": "per-pixel seed pixel ^ 0x9E3779B9 into the reference WangHash chain",
-        "film": "FP32 Kahan-compensated", "launch": "CUDA graph per frame" + (f", {inflight} frames in flight on separate streams" if inflight > 1 else ""),
+        "film": "FP32 Kahan-compensated",
+        "launch": ("CUDA graph per frame, its shadow rays of bounce b on a second stream beside its extension rays "
+                   "of bounce b+1" + (f", {inflight} frames in flight on separate streams" if inflight > 1 else "")),
         "l2": w["l2"],
         "parallelism": f"replicas x{world} (pixels/frames independent, no collective)",
     }
