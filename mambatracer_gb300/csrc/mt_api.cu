@@ -426,7 +426,7 @@ extern "C" int mt_scene_destroy(mt_scene* s) {
 // CNormalBVH.build (src/cl/scene/CNormalBVH.java:45-148): recursive split at the
 // centre of the centroid bound's longest axis, one triangle per leaf, children
 // allocated as adjacent pairs in preorder, node.bound = node index. The
-// partition (CNormalBVH.java:132) is an un-vendored library routine; this build
+// partition (CNormalBVH.java:132) is an un-vendored library routine; this builder
 // uses a stable split "centroid[dim] < split", falling back to the middle index
 // when one side would be empty (CNormalBVH.java:135-136).
 namespace {

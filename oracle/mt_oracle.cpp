@@ -1198,7 +1198,7 @@ void render_frame(const Scene& S, const Env<R>& E, const CameraF& cam_in, const 
 
 // ------------------------------------------------------------ BVH build
 // CNormalBVH.java:45-148. The partition of CNormalBVH.java:132 lives in an
-// un-vendored library; this build (and the product's) uses a stable split
+// un-vendored library; this builder (and the product's) uses a stable split
 // "centroid[dim] < split" on the triangle bounds' centres.
 struct BvhBuilder {
   const float* pts;

@@ -1,7 +1,7 @@
 // CPU restatement of MambaTracer's wavefront GI path (test infrastructure).
 //
-// This is the oracle: tests, __graft_entry__.smoke() and bench.py's CPU
-// baseline call it as the checker. The product (mambatracer_gb300) never
+// This is the oracle: tests and __graft_entry__.smoke() check results against
+// it, and bench.py's CPU baseline times it. The product (mambatracer_gb300) never
 // includes, links or calls anything here.
 //
 // Templated on the scalar type: R = float restates the reference kernels in
