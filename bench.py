@@ -15,8 +15,8 @@ into pinned host memory.
 Under torchrun (N > 1) each rank renders its own frames of the same job
 (weak scaling: per-GPU work fixed), with no collective on the data path.
 The reference arm times the reference algorithm on the host cores: the
-restatement in oracle/ (the reference's OpenCL C cannot run on the GPU host,
-which has neither an OpenCL runtime nor the reference sources).
+restatement in oracle/ (the reference's OpenCL C needs an OpenCL runtime, and the
+machine that runs the benchmark has none, nor the reference sources).
 """
 from __future__ import annotations
 
@@ -720,7 +720,7 @@ def run_reference(args):
                          "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": ("the reference's OpenCL kernels need an OpenCL runtime (none on this host: no ICD, no PoCL) and "
-                 "its sources are not on the GPU host; its algorithm runs as the oracle restatement"),
+                 "its sources do not ship with this repository; its algorithm runs as the oracle restatement"),
     }
     print(json.dumps(out), flush=True)
 

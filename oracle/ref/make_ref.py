@@ -8,7 +8,7 @@ parses the former as a cast of a comma expression; the two below), and compiles 
 together with oracle/ref/ref_harness.cpp through the shim oracle/ref/clshim.h.
 
 Everything it writes goes to oracle/_ref/ (git-ignored). When the reference tree
-is absent (the GPU host), it does nothing and returns False.
+is absent (a machine without the reference sources), it does nothing and returns False.
 """
 from __future__ import annotations
 
