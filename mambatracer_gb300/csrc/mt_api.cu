@@ -936,9 +936,9 @@ extern "C" int mt_compact_isects(mt_context* ctx, const void* isects_in, const i
     if (r) return r;
     ctx->cs_tiles = tiles ? tiles : 1;
   }
-  if (launch_compact_isects(ctx->stream, isects_in, pixels_in, n, isects_out, pixels_out, count_io,
-                            CompactScratch{ctx->cs_status, ctx->cs_words}))
-    return fail(MT_ERR_CUDA, "compaction launch: %s", cudaGetErrorString(cudaGetLastError()));
+  const cudaError_t le = launch_compact_isects(ctx->stream, isects_in, pixels_in, n, isects_out, pixels_out,
+                                               count_io, CompactScratch{ctx->cs_status, ctx->cs_words});
+  if (le != cudaSuccess) return fail(MT_ERR_CUDA, "compaction launch: %s", cudaGetErrorString(le));
   int err = 0;
   CU(cudaMemcpyAsync(&err, ctx->cs_words + 2, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));

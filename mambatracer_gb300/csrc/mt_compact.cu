@@ -8,6 +8,7 @@
 // its output equals a serial CompactAtomic bit for bit. Slots start at the
 // value *count holds on entry, as atomic_inc's would, and *count ends at
 // entry value + kept.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -52,19 +53,23 @@ __global__ void __launch_bounds__(kCompactThreads)
   if (tile == ntiles - 1 && threadIdx.x == 0) *count = b0 + (int)(s_excl + tot);
 }
 
-int launch_compact_isects(cudaStream_t st, const void* isects_in, const int32_t* pixels_in, int n, void* isects_out,
-                          int32_t* pixels_out, int32_t* count_io, CompactScratch s) {
+cudaError_t launch_compact_isects(cudaStream_t st, const void* isects_in, const int32_t* pixels_in, int n,
+                                  void* isects_out, int32_t* pixels_out, int32_t* count_io, CompactScratch s) {
   const int ntiles = (n + kCompactThreads - 1) / kCompactThreads;
-  if (cudaMemsetAsync(s.status, 0, sizeof(unsigned long long) * (size_t)(ntiles > 0 ? ntiles : 1), st) != cudaSuccess)
-    return -1;
-  if (cudaMemsetAsync(s.words, 0, 4 * sizeof(int), st) != cudaSuccess) return -1;
+  cudaError_t e = cudaMemsetAsync(s.status, 0, sizeof(unsigned long long) * (size_t)(ntiles > 0 ? ntiles : 1), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(s.words, 0, 4 * sizeof(int), st);
+  if (e != cudaSuccess) return e;
   // words: [0] tile counter, [1] entry value of *count, [2] device error
-  if (cudaMemcpyAsync(s.words + 1, count_io, sizeof(int), cudaMemcpyDeviceToDevice, st) != cudaSuccess) return -1;
-  if (ntiles > 0)
+  e = cudaMemcpyAsync(s.words + 1, count_io, sizeof(int), cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  if (ntiles > 0) {
     k_compact_isects<<<ntiles, kCompactThreads, 0, st>>>(
         static_cast<const float4*>(isects_in), pixels_in, n, static_cast<float4*>(isects_out), pixels_out, count_io,
         s.status, s.words, s.words + 1, s.words + 2);
-  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    e = cudaGetLastError();
+  }
+  return e;
 }
 
 // ------------------------------------------------------- no-allocation variant
@@ -91,7 +96,17 @@ __attribute__((visibility("hidden"))) void set_last_error(const char* msg);  // 
 namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
-unsigned long long* g_noalloc_addr[kMaxDevices] = {};
+// The scratch array's device address as looked up in one CUDA context: an
+// address from cudaGetSymbolAddress holds only in the context current at the
+// lookup. Contexts are told apart by cuCtxGetId, which never reuses an id in a
+// process, so a new primary context (after cudaDeviceReset) or another context
+// a host made current on the device gets a fresh lookup.
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;  // 0: no lookup yet
+  unsigned long long* ptr = nullptr;
+};
+ScratchAddr g_noalloc_addr[kMaxDevices];
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
 
 int noalloc_fail(int code, const char* msg, cudaError_t e = cudaSuccess) {
   std::string m = msg;
@@ -101,6 +116,23 @@ int noalloc_fail(int code, const char* msg, cudaError_t e = cudaSuccess) {
   }
   mt::set_last_error(m.c_str());
   return code;
+}
+
+// Id of the context current on this thread. The driver function is fetched
+// through the runtime, so the library needs no link to libcuda.
+int current_ctx_id(unsigned long long* id) {
+  static CtxGetIdFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetIdFn>(p);
+  });
+  if (!fn) return noalloc_fail(MT_ERR_CUDA, "cuCtxGetId is not available from the driver");
+  if (fn(nullptr, id) != CUDA_SUCCESS || *id == 0) return noalloc_fail(MT_ERR_CUDA, "no current CUDA context");
+  return MT_OK;
 }
 }  // namespace
 
@@ -114,22 +146,31 @@ extern "C" int mt_compact_isects_noalloc(void* stream, const void* isects_in, co
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return noalloc_fail(MT_ERR_CUDA, "cudaGetDevice", e);
   if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(MT_ERR_INVALID, "device index out of range");
+  // Make sure a context is current (the device's primary context unless the
+  // host made another one current), then identify it.
+  e = cudaStreamQuery(static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess && e != cudaErrorNotReady) return noalloc_fail(MT_ERR_CUDA, "stream", e);
+  unsigned long long ctx_id = 0;
+  if (int r = current_ctx_id(&ctx_id)) return r;
   unsigned long long* scratch;
   {
-    // Set-up on the first call on each device, with that device current.
+    // Set-up, once per device and context: the scratch array's device address
+    // in the current context.
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
+    ScratchAddr& a = g_noalloc_addr[dev];
+    if (a.ctx_id != ctx_id) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, mt::g_noalloc_scratch);
       if (e != cudaSuccess || !p) return noalloc_fail(MT_ERR_CUDA, "cudaGetSymbolAddress", e);
-      g_noalloc_addr[dev] = static_cast<unsigned long long*>(p);
+      a.ptr = static_cast<unsigned long long*>(p);
+      a.ctx_id = ctx_id;
     }
-    scratch = g_noalloc_addr[dev];
+    scratch = a.ptr;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   mt::CompactScratch s{scratch, reinterpret_cast<int*>(scratch + mt::kNoAllocTiles)};
-  if (mt::launch_compact_isects(st, isects_in, pixels_in, n, isects_out, pixels_out, count_io, s))
-    return noalloc_fail(MT_ERR_CUDA, "compaction launch", cudaGetLastError());
+  e = mt::launch_compact_isects(st, isects_in, pixels_in, n, isects_out, pixels_out, count_io, s);
+  if (e != cudaSuccess) return noalloc_fail(MT_ERR_CUDA, "compaction launch", e);
   int err = 0;
   e = cudaMemcpyAsync(&err, s.words + 2, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -15,7 +15,8 @@ struct CompactScratch {
   int* words;
 };
 
-int launch_compact_isects(cudaStream_t st, const void* isects_in, const int32_t* pixels_in, int n, void* isects_out,
-                          int32_t* pixels_out, int32_t* count_io, CompactScratch s);
+// Returns the error of the first call that failed (cudaSuccess: all enqueued).
+cudaError_t launch_compact_isects(cudaStream_t st, const void* isects_in, const int32_t* pixels_in, int n,
+                                  void* isects_out, int32_t* pixels_out, int32_t* count_io, CompactScratch s);
 
 }  // namespace mt

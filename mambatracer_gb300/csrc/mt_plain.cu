@@ -1306,9 +1306,10 @@ extern "C" int mt_launch_1d(mt_kernel* k, size_t global, size_t local) {
         if (r) return r;
         ctx->cs_tiles = tiles;
       }
-      if (launch_compact_isects(st, ptr<void>(k, 0), ptr<int>(k, 2), n, ptr<void>(k, 1), ptr<int>(k, 3),
-                                ptr<int>(k, 4), CompactScratch{ctx->cs_status, ctx->cs_words}))
-        return fail(MT_ERR_CUDA, "compaction launch: %s", cudaGetErrorString(cudaGetLastError()));
+      const cudaError_t le = launch_compact_isects(st, ptr<void>(k, 0), ptr<int>(k, 2), n, ptr<void>(k, 1),
+                                                   ptr<int>(k, 3), ptr<int>(k, 4),
+                                                   CompactScratch{ctx->cs_status, ctx->cs_words});
+      if (le != cudaSuccess) return fail(MT_ERR_CUDA, "compaction launch: %s", cudaGetErrorString(le));
       break;
     }
     case kTransferIsect:

@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 def _dev(ctx, nbytes, host=None):
     b = C.c_void_p()
-    if host is None:
+    if host is None or host.nbytes == 0:
         _lib.check(_lib.lib().mt_buf_alloc(ctx.h, max(nbytes, 4), C.byref(b)))
     else:
         _lib.check(_lib.lib().mt_buf_create_from(ctx.h, host.ctypes.data_as(C.c_void_p), max(host.nbytes, 4),
@@ -69,6 +69,23 @@ def test_no_alloc_matches_regular_entry_point(ctx):
                                             C.c_void_p]
     # two calls in a row on the shared scratch: a large queue, then a smaller one
     for n, frac, start, seed in ((2_073_600, 0.53, 0, 1), (300_001, 0.2, 17, 2)):
+        isects, pixels = _case(n, frac, seed)
+        ref = _compact(ctx, L.mt_compact_isects, isects, pixels, start, False)
+        got = _compact(ctx, L.mt_compact_isects_noalloc, isects, pixels, start, True)
+        assert got[2] == ref[2] == start + int((isects["hit"] != 0).sum())
+        k = got[2]
+        assert np.array_equal(got[0][96 * start:96 * k], ref[0][96 * start:96 * k])
+        assert np.array_equal(got[1][start:k], ref[1][start:k])
+
+
+def test_no_alloc_empty_and_full_scratch(ctx):
+    L = _lib.lib()
+    L.mt_compact_isects_noalloc.restype = C.c_int
+    L.mt_compact_isects_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                            C.c_void_p]
+    # n = 0: nothing is launched and the count keeps its entry value; then
+    # exactly the largest queue the fixed scratch holds (every tile slot in use)
+    for n, frac, start, seed in ((0, 0.5, 5, 3), (1 << 22, 0.61, 3, 4)):
         isects, pixels = _case(n, frac, seed)
         ref = _compact(ctx, L.mt_compact_isects, isects, pixels, start, False)
         got = _compact(ctx, L.mt_compact_isects_noalloc, isects, pixels, start, True)
