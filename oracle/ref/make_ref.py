@@ -1,7 +1,8 @@
 """Build oracle/_ref/libmtref.so: the reference's own OpenCL kernels compiled as C++.
 
 Test infrastructure only. Reads MambaTracer's kernel sources where they lie
-(/root/reference/src/cl/kernel), concatenates them in the order of
+(src/cl/kernel under the checkout that MT_REFERENCE_ROOT names, else the
+default checkout location below), concatenates them in the order of
 src/cl/kernel/CSource.java:18-38, applies mechanical rewrites (OpenCL vector
 literals "(float4)(a, b, c, d)" become calls "clv_float4(a, b, c, d)", since C++
 parses the former as a cast of a comma expression; the two below), and compiles the result
@@ -17,7 +18,10 @@ import re
 import subprocess
 import sys
 
-REF_KERNELS = "/root/reference/src/cl/kernel"
+# Root of the MambaTracer checkout: MT_REFERENCE_ROOT, else where this build
+# environment mounts it.
+REF_ROOT = os.environ.get("MT_REFERENCE_ROOT") or "/root/reference"
+REF_KERNELS = os.path.join(REF_ROOT, "src", "cl", "kernel")
 # src/cl/kernel/CSource.java:18-38
 TU_ORDER = [
     "Print.cl", "Util.cl", "SAT.cl", "RGBSpace.cl", "Sampling.cl", "Matrix.cl",

@@ -84,8 +84,8 @@ def _reference_cornell_box():
     import os
     import re
 
-    from oracle.ref.make_ref import REF_KERNELS
-    REF_TRACER_API = os.path.join(os.path.dirname(REF_KERNELS), "ui", "fx", "main", "TracerAPI.java")
+    from oracle.ref.make_ref import REF_ROOT
+    REF_TRACER_API = os.path.join(REF_ROOT, "src", "cl", "ui", "fx", "main", "TracerAPI.java")
     if not os.path.exists(REF_TRACER_API):
         pytest.skip("reference tree not present")
     src = open(REF_TRACER_API, encoding="latin-1").read()
