@@ -257,34 +257,129 @@ def algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_count, t
 
 
 # ------------------------------------------------------------- GPU arm
+def bench_scene(ctx, kind, small, width, height, precision):
+    """The workload's scene on the device as every step renders it: the BVH built on
+    the GPU (CNormalBVH.build's tree), the record format, the sky environment with
+    its FP64 SAT and the light grid with FP64 per-cell SATs. Returns (host scene,
+    device scene, reference-layout nodes and bounds, environment map, build ms)."""
+    from mambatracer_gb300 import api, scenes
+    sc = make_scene(kind, small, width, height)
+    env = scenes.sky_env(ENV_W, ENV_H)
+    S = api.Scene(ctx, sc)
+    t_bvh = time.perf_counter()
+    nodes, bounds = S.build_bvh_device()  # CNormalBVH.build's tree, built level by level on the GPU
+    bvh_build_ms = (time.perf_counter() - t_bvh) * 1e3
+    if precision:
+        S.set_precision(1)  # FP16 child boxes rounded outward, 32-byte records
+    if ENV_ON:
+        S.set_env(env, ENV_W, ENV_H)
+        S.grid_config(*GRID, enable=2)  # grid-guided environment sampling, FP64 per-cell SATs
+    return sc, S, nodes, bounds, env, bvh_build_ms
+
+
+def bench_job(ctx, S, width, height, spp, inflight, grid_updates):
+    """The render job every soup/stadium/room step runs: benchmark semantics, depth
+    DEPTH, Russian roulette from RR, Kahan film, one CUDA graph per frame."""
+    from mambatracer_gb300 import api
+    return api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, use_graph=1,
+                   inflight=inflight, grid_updates=grid_updates, spp=spp)
+
+
+def image_check(ctx, S, sc, nodes, bounds, env, width, height, spp, inflight, steps=16, stride=8, orc=None,
+                parity=True):
+    """The benchmark job's film against the FP64 oracle, and its parity figures.
+
+    Renders a fresh job exactly as the timed one (same scene, environment, light
+    grid, job settings, GRID_UPDATES grid-updating warm-up frames, then `steps`
+    steps of spp passes from a cleared film), then with the oracle (after all GPU
+    work; it is the checker here):
+      * the FP64 oracle renders every stride-th pixel in x and y at the same frame
+        counts on the grid the GPU froze: relative RMSE of the linear film;
+      * (parity) the FP32 oracle, the reference's algorithm in the reference's
+        precision, renders the same samples: its own error against the FP64
+        oracle (the image error of any FP32 run of this algorithm at these samples:
+        discrete decisions, an edge hit or missed, a Russian-roulette or lobe
+        choice, flip between FP32 and FP64 on a few samples, and a flipped path
+        that then sees the sun moves its pixel by a lot), and the GPU's against it;
+      * (parity) the FP32 oracle renders the last pass in full: its queue lengths and ray
+        counts against the GPU's (benchmark semantics: the reference's RR and BSDF
+        branches flip on last-ulp differences of CUDA's transcendentals, so counts
+        drift a little);
+      * the first pass's primary rays traced through the C-ABI (mt_trace_closest)
+        against the FP32 oracle traversal: hit-id mismatches, exact-t ties, rays
+        within 1e-6 barycentric of an edge.
+    env: (rgb, w, h) or None. Returns a dict."""
+    from oracle import check
+    from oracle.oracle import Oracle
+    orc = orc or Oracle()
+    job = bench_job(ctx, S, width, height, spp, inflight, GRID_UPDATES if env is not None else 0)
+    job.set_camera(sc.camera)
+    frame0 = lambda i: 1.0 + i * spp  # noqa: E731  (passes of a step take consecutive counts)
+    for i in range(GRID_UPDATES):
+        job.render(None, frame0(i))
+    job.clear()
+    fcs = []
+    for i in range(steps):
+        job.render(None, frame0(GRID_UPDATES + i))
+        fcs += [frame0(GRID_UPDATES + i) + k for k in range(spp)]
+    film = job.film()
+    rays_gpu, counts_gpu = job.stats()  # the last step; counts of its last pass
+    grid = None
+    if env is not None and S.grid[4]:
+        func, gsat, _ = job.grid()
+        grid = dict(func=func, sat=gsat, nu=S.grid[0], nv=S.grid[1], rx=S.grid[2], ry=S.grid[3])
+    job.close()
+    t0 = time.perf_counter()
+    px = check.strided_pixels(width, height, stride)
+    acc64, _, _ = check.subset_frames(orc, sc, nodes, bounds, width, height, DEPTH, RR, fcs, px, env, True, grid)
+    err = check.rel_rmse(film[px], acc64)
+    res = {"rel_rmse_fp64": float(f"{err:.4e}"), "spp": len(fcs), "pixels": int(len(px)),
+           "pixel_subset": f"every {stride}th pixel in x and y ({len(px)} of {width * height})",
+           "film": "linear accumulated radiance (CImage accum), Kahan FP32 on the GPU, FP64 in the oracle"}
+    if not parity:
+        res["oracle_seconds"] = round(time.perf_counter() - t0, 1)
+        return res
+    acc32, _, _ = check.subset_frames(orc, sc, nodes, bounds, width, height, DEPTH, RR, fcs, px, env, False, grid)
+    res["reference_fp32_rel_rmse_fp64"] = float(f"{check.rel_rmse(acc32, acc64):.4e}")
+    res["rel_rmse_vs_reference_fp32"] = float(f"{check.rel_rmse(film[px], acc32):.4e}")
+    allpx = np.arange(width * height, dtype=np.int32)
+    _, c32, r32 = check.subset_frames(orc, sc, nodes, bounds, width, height, DEPTH, RR, [fcs[-1]], allpx, env, False,
+                                      grid)
+    rays = check.primary_rays(orc, sc.camera, width, height, fcs[0])
+    t_gpu, p_gpu = S.trace_closest(rays)
+    t_ref, p_ref = check.trace_oracle(orc, sc, nodes, bounds, rays)
+    hits = check.hit_parity(sc, rays, t_gpu, p_gpu, t_ref, p_ref)
+    last_rays_gpu = rays_gpu if spp == 1 else None
+    drift = (np.abs(counts_gpu.astype(np.int64) - c32) / np.maximum(c32, 1)).tolist()
+    res.update({
+        "queue_lengths_gpu": counts_gpu.tolist(), "queue_lengths_fp32_oracle": c32.tolist(),
+        "queue_length_rel_drift": [round(x, 5) for x in drift],
+        "rays_last_pass_gpu": None if last_rays_gpu is None else last_rays_gpu.tolist(),
+        "rays_last_pass_fp32_oracle": r32.tolist(),
+        "primary_hits": hits, "oracle_seconds": round(time.perf_counter() - t0, 1),
+    })
+    return res
+
+
 def run_gpu(args):
     import torch
     rank, world, local = dist_env()
     if world > 1:
         torch.cuda.set_device(local)
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from mambatracer_gb300 import api, build, scenes
+    from mambatracer_gb300 import api, build
     build.build()
+    default_shapes = api.get_tuning()
     launch_shapes = apply_tuning(f"soup{NTRI}_{W_DEFAULT}x{H_DEFAULT}"
                                  if args.workload == "soup" and not args.small else None)
 
     width, height = (640, 360) if args.small and args.workload != "room" else (W_DEFAULT, H_DEFAULT)
     spp = WORKLOADS[args.workload]["spp"]
-    sc = make_scene(args.workload, args.small, width, height)
-    ntri = sc.ntri
-    env = scenes.sky_env(ENV_W, ENV_H)
     ctx = api.Context(local)
-    S = api.Scene(ctx, sc)
-    t_bvh = time.perf_counter()
-    nodes, bounds = S.build_bvh_device()  # CNormalBVH.build's tree, built level by level on the GPU
-    bvh_build_ms = (time.perf_counter() - t_bvh) * 1e3
-    if args.precision:
-        S.set_precision(1)  # FP16 child boxes rounded outward, 32-byte records
-    if ENV_ON:
-        S.set_env(env, ENV_W, ENV_H)
-        S.grid_config(*GRID, enable=2)  # grid-guided environment sampling, FP64 per-cell SATs
-    job = api.Job(ctx, S, width, height, max_depth=DEPTH, mode=1, rr_depth=RR, film_kahan=1, use_graph=1,
-                  inflight=args.inflight, grid_updates=min(GRID_UPDATES, args.warmup), spp=spp)
+    sc, S, nodes, bounds, env, bvh_build_ms = bench_scene(ctx, args.workload, args.small, width, height,
+                                                          args.precision)
+    ntri = sc.ntri
+    job = bench_job(ctx, S, width, height, spp, args.inflight, min(GRID_UPDATES, args.warmup))
     cam = sc.camera.copy()
     job.set_camera(cam)
 
@@ -421,6 +516,11 @@ def run_gpu(args):
         cpu_baseline = {"value": round(crays / csec / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                         "sample": f"{cframes} frames of {cw}x{ch} (1/16 of the pixels, same scene, camera, depth, RR) "
                                   f"in {threads} threads for {csec:.1f} s; oracle/mt_oracle.cpp (FP32)"}
+        # the same job's film against the FP64 oracle, and its parity figures (a check, after the timed region)
+        image_error = None
+        if not args.no_check:
+            image_error = image_check(ctx, S, sc, nodes, bounds, (env, ENV_W, ENV_H) if ENV_ON else None, width,
+                                      height, spp, args.inflight, steps=max(1, 16 // spp), orc=orc)
         out = {
             "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
@@ -434,15 +534,52 @@ def run_gpu(args):
             "msamples_per_s": round(width * height * spp * args.steps * world / (ms * 1e-3) / 1e6, 2),
             "bvh_depth": S.depth, "bvh_build_ms": round(bvh_build_ms, 2), "bvh_build": "GPU, level-synchronous",
             "bvh_records": "FP16 child boxes rounded outward, 32 B" if args.precision else "FP32 child boxes, 64 B",
-            "alg_bytes_seconds": round(t_alg, 1), "launch_shapes": launch_shapes,
+            "alg_bytes_seconds": round(t_alg, 1), "launch_shapes": launch_shapes, "image_error": image_error,
         }
     job.close()
     S.close()
     ctx.close()
+    if out is not None and world == 1 and not args.small and args.workload == "soup" and not args.no_arms:
+        api.set_tuning(default_shapes)  # the other arms' own launch shapes (run_served installs the merged ones)
+        out["batched"], out["plain"] = baseline_metric_arms(args)
+        b, pl = out["batched"], out["plain"]
+        out["batched_vs_plain"] = round(b["merged_queues"]["mrays_per_s"] / pl["plain_mrays_per_s"], 3)
     if world > 1:
         torch.distributed.destroy_process_group()
     if out is not None:
         print(json.dumps(out), flush=True)
+
+
+def baseline_metric_arms(args):
+    """The workload metric's own arms, run after the timed soup steps: the batched
+    configuration (64 jobs of uneven size, soup and stadium, 4 spp) through the
+    merged-queue server against the same requests one at a time, with job
+    latencies; and the reference's plain wavefront loop (its kernels by name,
+    CDeviceGI.loop and CCompact, host-driven) against the fused frame on the same
+    soup frames."""
+    ns = argparse.Namespace(**vars(args))
+    ns.workload, ns.arms = "batched", "served_merged,sequential"
+    ns.merged_lanes = ns.merge_streams = None
+    r = run_served(ns, emit=False)
+    batched = {
+        "requests": r["requests"], "samples": r["samples"],
+        "merged_queues": {k: r["served_merged"][k] for k in ("lanes", "merge_streams", "mrays_per_s", "p50_ms",
+                                                             "p95_ms", "p99_ms", "max_ms", "span_s")},
+        "sequential": {k: r["sequential"][k] for k in ("mrays_per_s", "p50_ms", "p95_ms", "p99_ms", "max_ms",
+                                                       "span_s")},
+        "speedup_vs_sequential": r["speedup_vs_sequential"],
+        "config": {k: r["config"][k] for k in ("requests", "resolution", "camera", "max_depth", "rr_from_bounce",
+                                               "latency", "equal_error")},
+    }
+    ns = argparse.Namespace(**vars(args))
+    ns.workload, ns.warmup, ns.steps = "plain", 2, 4
+    p = run_plain(ns, emit=False)
+    plain = {"plain_mrays_per_s": p["value"], "plain_ms_per_frame": p["plain_ms_per_frame"],
+             "fused_mrays_per_s": p["fused_mrays_per_s"], "fused_ms_per_frame": p["fused_ms_per_frame"],
+             "fused_inflight4_mrays_per_s": p["fused_inflight4_mrays_per_s"],
+             "speedup_fused_vs_plain": p["speedup_fused_vs_plain"], "frames": ns.steps,
+             "rays_per_frame": p["rays_per_frame"], "config": p["config"]}
+    return batched, plain
 
 
 # --------------------------------------------------- batched and served
@@ -502,9 +639,10 @@ def run_requests(ctx, S, reqs, lanes, budget, api, merged=0):
     return st, wall
 
 
-def run_served(args):
+def run_served(args, emit=True):
     """Batched (64 uneven jobs at once) or served (Poisson arrivals) rendering through
-    the served-mode scheduler, against the same requests run one at a time."""
+    the served-mode scheduler, against the same requests run one at a time. Prints
+    the JSON line (emit) and returns it."""
     from mambatracer_gb300 import api, build, scenes
     build.build()
     launch_shapes = apply_tuning()  # the built-in launch shapes: the file's are for the soup
@@ -611,11 +749,13 @@ def run_served(args):
     for sc_h in S.values():
         sc_h.close()
     ctx.close()
-    print(json.dumps(out), flush=True)
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
 
 
 # ------------------------------------------------------ plain wavefront
-def run_plain(args):
+def run_plain(args, emit=True):
     """The reference's own loop through the kernel-by-name layer (one launch per
     reference kernel, reference buffer layouts, host-driven) against the fused path
     on the same frames: reference semantics (seeds per allocateState call, no
@@ -685,7 +825,9 @@ def run_plain(args):
     }
     S.close()
     ctx.close()
-    print(json.dumps(out), flush=True)
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
 
 
 # ------------------------------------------------------- reference arm
@@ -733,6 +875,8 @@ def main():
     ap.add_argument("--impl", default="mambatracer", choices=["mambatracer", "reference"])
     ap.add_argument("--small", action="store_true", help="small case for profiler captures")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-check", action="store_true", help="skip the image-error check against the oracle")
+    ap.add_argument("--no-arms", action="store_true", help="skip the batched and plain-wavefront arms")
     ap.add_argument("--inflight", type=int, default=6, help="frames kept in flight on separate streams (1..8)")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
                     help="BVH records: 0 FP32 child boxes (64 B), 1 FP16 outward-rounded (32 B)")

@@ -900,6 +900,11 @@ struct RenderParams {
   float frame_count; // State.frameCount (1 for the first frame)
   int rr_depth;      // mode 1: Russian roulette from this bounce on (0 = off)
   bool grid_accum = false;  // mode 1 with the grid on: environment hits accumulate into it
+  // mode 1 only: render just these pixels of the frame (npix of them); queue slot
+  // q starts pixel pix_of[q], keyed on it as the full frame keys it, and
+  // accumulates into accum[q]. NULL: every pixel, accum indexed by pixel.
+  const int* pix_of = nullptr;
+  int npix = 0;
 };
 
 // Config-mode seed pair of a (bounce, stage): stage 0 raygen, 1 light pick+sample,
@@ -993,7 +998,8 @@ template <class R>
 void render_frame(const Scene& S, const Env<R>& E, const CameraF& cam_in, const RenderParams& P,
                   const int* seeds /* mode 0: 1 + 2*max_depth pairs */, R* accum /* float4 per pixel */,
                   int* counts_out, RayCounts* rc) {
-  const int N = P.width * P.height;
+  const int N = P.pix_of ? P.npix : P.width * P.height;
+  auto pix = [&](int q) { return P.pix_of ? P.pix_of[q] : q; };  // the frame pixel of queue origin q
   CameraF cam = cam_in;
   cam.dimension[0] = (float)P.width;
   cam.dimension[1] = (float)P.height;
@@ -1017,10 +1023,10 @@ void render_frame(const Scene& S, const Env<R>& E, const CameraF& cam_in, const 
   int32_t sx = 0, sy = 0;
   if (P.mode == 0) next_state(&sx, &sy); else stage_seed(0, 0, &sx, &sy);
   for (int id = 0; id < N; ++id) {
-    Seed s = generate_seed(sx, sy, P.frame_count, P.mode == 0 ? id : pixel_gid(id));
+    Seed s = generate_seed(sx, sy, P.frame_count, P.mode == 0 ? id : pixel_gid(pix(id)));
     R r0 = R(get_random(s));
     R r1 = R(get_random(s));
-    camera_ray(cam, id, r0, r1, rays[id]);
+    camera_ray(cam, pix(id), r0, r1, rays[id]);
     Path<R>& pa = paths[id];
     pa.throughput = {R(1), R(1), R(1), R(1)};
     pa.lastSpecular = 1;
@@ -1115,7 +1121,7 @@ void render_frame(const Scene& S, const Env<R>& E, const CameraF& cam_in, const 
     for (int j = 0; j < count; ++j) {
       Isect<R>& is = isects[j];
       Path<R>& pa = paths[pixels[j]];
-      Seed s = generate_seed(lx, ly, P.frame_count, P.mode == 0 ? j : pixel_gid(pixels[j]));
+      Seed s = generate_seed(lx, ly, P.frame_count, P.mode == 0 ? j : pixel_gid(pix(pixels[j])));
       V4<R> dir = {R(0), R(0), R(0), R(0)};
       R dist = R(0), pdfW = R(0), pick = R(1);
       V4<R> smp = {R(get_random(s)), R(get_random(s)), R(get_random(s)), R(get_random(s))};
@@ -1164,7 +1170,7 @@ void render_frame(const Scene& S, const Env<R>& E, const CameraF& cam_in, const 
     for (int j = 0; j < count; ++j) {
       Isect<R>& is = isects[j];
       Path<R>& pa = paths[pixels[j]];
-      Seed s = generate_seed(bx, by, P.frame_count, P.mode == 0 ? j : pixel_gid(pixels[j]));
+      Seed s = generate_seed(bx, by, P.frame_count, P.mode == 0 ? j : pixel_gid(pix(pixels[j])));
       R s0 = R(get_random(s)), s1 = R(get_random(s)), s2 = R(get_random(s));
       V4<R> dir = {R(0), R(0), R(0), R(0)};
       R pdf = R(0), cosOut = R(0);
@@ -1176,7 +1182,7 @@ void render_frame(const Scene& S, const Env<R>& E, const CameraF& cam_in, const 
       pa.hitpoint = is.p;
       bool alive = true;
       if (P.mode == 1 && P.rr_depth > 0 && b >= P.rr_depth) {
-        Seed rs = generate_seed(rx, ry, P.frame_count, pixel_gid(pixels[j]));
+        Seed rs = generate_seed(rx, ry, P.frame_count, pixel_gid(pix(pixels[j])));
         R u = R(get_random(rs));
         R m = max_(pa.throughput.x, max_(pa.throughput.y, pa.throughput.z));
         R cont = min_(KF(0.95), m);
@@ -1585,6 +1591,15 @@ int or_bsdf_eval(const float* material, const float* n, const float* ng, const f
   return 1;
 }
 
+int or_render_frame_subset(const void* camera, int width, int height, int max_depth, int mode, int rr_depth,
+                           const int* seeds, float frame_count, const float* points, const float* uvs,
+                           const float* normals, const int* faces, int nfaces, const float* materials,
+                           const int* nodes, const float* bounds, const float* envmap, const void* env_lum,
+                           const void* env_sat, int env_w, int env_h, int env_present, int fp64, void* accum,
+                           int* counts_out, long long* ray_counts, const float* grid_func, const float* grid_sat,
+                           float* grid_accum, int nu, int nv, int rx, int ry, const float* cam_pos, int grid_on,
+                           int grid_accumulate, const int* pixels, int npixels);
+
 // One frame. fp64 != 0 runs the FP64 instantiation (accum is then double*).
 // env_sat/env_lum: FP32 arrays for fp64 == 0, FP64 arrays otherwise.
 // ray_counts: [primary, extension, shadow].
@@ -1596,6 +1611,23 @@ int or_render_frame_grid(const void* camera, int width, int height, int max_dept
                          int* counts_out, long long* ray_counts, const float* grid_func, const float* grid_sat,
                          float* grid_accum, int nu, int nv, int rx, int ry, const float* cam_pos, int grid_on,
                          int grid_accumulate) {
+  return or_render_frame_subset(camera, width, height, max_depth, mode, rr_depth, seeds, frame_count, points, uvs,
+                                normals, faces, nfaces, materials, nodes, bounds, envmap, env_lum, env_sat, env_w,
+                                env_h, env_present, fp64, accum, counts_out, ray_counts, grid_func, grid_sat,
+                                grid_accum, nu, nv, rx, ry, cam_pos, grid_on, grid_accumulate, nullptr, 0);
+}
+
+// or_render_frame_grid over a subset of the frame's pixels (mode 1 only; see
+// RenderParams::pix_of): accum holds one float4 (fp64: double4) per listed pixel.
+int or_render_frame_subset(const void* camera, int width, int height, int max_depth, int mode, int rr_depth,
+                           const int* seeds, float frame_count, const float* points, const float* uvs,
+                           const float* normals, const int* faces, int nfaces, const float* materials,
+                           const int* nodes, const float* bounds, const float* envmap, const void* env_lum,
+                           const void* env_sat, int env_w, int env_h, int env_present, int fp64, void* accum,
+                           int* counts_out, long long* ray_counts, const float* grid_func, const float* grid_sat,
+                           float* grid_accum, int nu, int nv, int rx, int ry, const float* cam_pos, int grid_on,
+                           int grid_accumulate, const int* pixels, int npixels) {
+  if (pixels && mode != 1) return -1;
   Scene S;
   S.mesh = mesh_of(points, uvs, normals, faces, nfaces);
   S.materials = reinterpret_cast<const SurfaceParameter*>(materials);
@@ -1606,6 +1638,8 @@ int or_render_frame_grid(const void* camera, int width, int height, int max_dept
   S.light_faces = lf.data();
   RenderParams P{width, height, max_depth, mode, frame_count, rr_depth};
   P.grid_accum = grid_accumulate != 0;
+  P.pix_of = pixels;
+  P.npix = npixels;
   RayCounts rc;
   const CameraF& cam = *static_cast<const CameraF*>(camera);
   auto set_grid = [&](auto& E) {

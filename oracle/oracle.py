@@ -64,6 +64,8 @@ class Oracle:
                                       P, P]
         L.or_render_frame_grid.restype = I
         L.or_render_frame_grid.argtypes = L.or_render_frame.argtypes + [P, P, P, I, I, I, I, P, I, I]
+        L.or_render_frame_subset.restype = I
+        L.or_render_frame_subset.argtypes = L.or_render_frame_grid.argtypes + [P, I]
         L.or_grid_init_func.argtypes = [P, P, I, I, I, I, I, I, P]
         L.or_env_grid_illuminate.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P, P]
         L.or_env_grid_radiance.argtypes = [P, P, P, I, I, P, P, I, I, I, I, P, P, P, P, P, P, P]
