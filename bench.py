@@ -47,7 +47,8 @@ WORKLOADS = {
     "soup": dict(name="soup1M_1920x1080_depth8_rr3_env2048x1024", spp=1,
                  scene="1,000,000-triangle soup, centroids U[-1,1]^3, edges N(0,0.005^2), GGX r U[0.05,0.8], "
                        "albedo U[0.2,0.9]",
-                 l2="no flush: per-step working set (path state + queues ~420 MB, BVH+triangles 112 MB) exceeds "
+                 l2="no flush: per-step working set (path state + queues ~420 MB, traversal records + triangles "
+                    "80-112 MB) exceeds "
                     "the 129 MB L2"),
     "room": dict(name="boxroom36_256x256_depth4", spp=1, width=256, height=256, depth=4, rr=0, env=False,
                  scene="box room: 36 triangles (walls, two GGX boxes r 0.3, a 0.25 x 0.25 ceiling emitter of "
@@ -62,6 +63,10 @@ WORKLOADS = {
                        "the 129 MB L2"),
 }
 WORKLOAD = WORKLOADS["soup"]["name"]
+# traversal formats (mt_scene_set_bvh_precision)
+RECORDS = {0: "FP32 child boxes, binary, 64 B records",
+           1: "FP16 child boxes rounded outward, binary, 32 B records",
+           2: "wide BVH: up to 8 children with 8-bit child boxes rounded outward, 80 B nodes"}
 
 
 def make_scene(kind, small, width, height):
@@ -270,7 +275,7 @@ def bench_scene(ctx, kind, small, width, height, precision):
     nodes, bounds = S.build_bvh_device()  # CNormalBVH.build's tree, built level by level on the GPU
     bvh_build_ms = (time.perf_counter() - t_bvh) * 1e3
     if precision:
-        S.set_precision(1)  # FP16 child boxes rounded outward, 32-byte records
+        S.set_precision(precision)  # 1: FP16 child boxes, 32-byte records; 2: wide BVH, 8-bit child boxes
     if ENV_ON:
         S.set_env(env, ENV_W, ENV_H)
         S.grid_config(*GRID, enable=2)  # grid-guided environment sampling, FP64 per-cell SATs
@@ -478,8 +483,20 @@ def run_gpu(args):
         orc = Oracle()
         threads = os.cpu_count() or 1
         t_alg = time.perf_counter()
-        alg_bytes, v_int, tri = algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_no(1), threads,
-                                                  rec_bytes=32 if args.precision else 64)
+        if args.precision == 2:
+            # the wide BVH has no oracle traversal: its node visits are counted on
+            # the device by the same traversal one ray per thread (mt_trace_counts)
+            from oracle import check
+            prays = check.primary_rays(orc, cam, width, height, frame_no(1))
+            _, _, cnt = S.trace_counts(prays)
+            v_int, tri = float(cnt[:, 0].mean()), float(cnt[:, 1].mean())
+            alg_bytes = int(width * height * 48 + 80 * int(cnt[:, 0].sum()) + 48 * int(cnt[:, 1].sum()))
+            visit_src = "wide-BVH node visits (80 B) counted on the device (mt_trace_counts)"
+        else:
+            alg_bytes, v_int, tri = algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_no(1),
+                                                      threads, rec_bytes=32 if args.precision == 1 else 64)
+            visit_src = (f"interior visits ({32 if args.precision == 1 else 64} B records) counted by the FP32 oracle "
+                         "traversal of the same rays")
         t_alg = time.perf_counter() - t_alg
         peaks = {}
         try:
@@ -502,6 +519,7 @@ def run_gpu(args):
                     "traffic_source": traffic_src,
                     "alg_bytes_per_launch": alg_bytes, "rays_per_launch": width * height,
                     "interior_visits_per_ray": round(v_int, 2), "triangle_tests_per_ray": round(tri, 2),
+                    "visit_counts": visit_src,
                     "launch_ms": round(t_b1, 4),
                     "trace_share_of_frame": round(trace_total / frame_total, 3), "per_kernel_ms": per_kernel}
         # CPU baseline: the oracle on the host cores, a bounded sample
@@ -533,7 +551,7 @@ def run_gpu(args):
             "inflight_frames": args.inflight,
             "msamples_per_s": round(width * height * spp * args.steps * world / (ms * 1e-3) / 1e6, 2),
             "bvh_depth": S.depth, "bvh_build_ms": round(bvh_build_ms, 2), "bvh_build": "GPU, level-synchronous",
-            "bvh_records": "FP16 child boxes rounded outward, 32 B" if args.precision else "FP32 child boxes, 64 B",
+            "bvh_records": RECORDS[args.precision],
             "alg_bytes_seconds": round(t_alg, 1), "launch_shapes": launch_shapes, "image_error": image_error,
         }
     job.close()
@@ -675,7 +693,7 @@ def run_served(args, emit=True):
         sc_h = api.Scene(ctx, sc)
         sc_h.build_bvh_device(want_arrays=False)
         if args.precision:
-            sc_h.set_precision(1)
+            sc_h.set_precision(args.precision)
         depth_of[key] = sc_h.depth
         if key != "room":
             sc_h.set_env(env, ENV_W, ENV_H)
@@ -740,7 +758,7 @@ def run_served(args, emit=True):
             "camera": "uniform on a sphere of radius 3 around the origin, looking at it, fov 45",
             "max_depth": DEPTH, "rr_from_bounce": RR, "semantics": "benchmark (mode 1), full-map environment sampling",
             "admission_budget_bytes": budget, "bvh_depth": depth_of,
-            "bvh_records": "FP16 child boxes rounded outward, 32 B" if args.precision else "FP32 child boxes, 64 B",
+            "bvh_records": RECORDS[args.precision],
             "latency": "submission to film in host memory (pinned staging), host clock",
             "equal_error": "the sequential run renders the same requests with the same spp",
             "launch_shapes": launch_shapes,
@@ -878,8 +896,10 @@ def main():
     ap.add_argument("--no-check", action="store_true", help="skip the image-error check against the oracle")
     ap.add_argument("--no-arms", action="store_true", help="skip the batched and plain-wavefront arms")
     ap.add_argument("--inflight", type=int, default=6, help="frames kept in flight on separate streams (1..8)")
-    ap.add_argument("--precision", type=int, default=0, choices=[0, 1],
-                    help="BVH records: 0 FP32 child boxes (64 B), 1 FP16 outward-rounded (32 B)")
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
+                    help="traversal format: 0 FP32 child boxes (64 B records), 1 FP16 outward-rounded (32 B, the "
+                         "default: the same hits, fastest), 2 wide BVH with 8-bit outward-rounded child boxes (80 B "
+                         "nodes)")
     ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS) + ["batched", "served", "plain"])
     ap.add_argument("--lanes", type=int, default=8, help="batched/served: requests in flight, a stream each")
     ap.add_argument("--merged-lanes", type=int, default=None,

@@ -319,6 +319,15 @@ int mt_tuning_set(const mt_tuning* in); /* MT_ERR_INVALID when a field is out of
 int mt_trace_closest(mt_scene* scene, const void* rays, int n, float* t_out, int32_t* prim_out);
 /* Any hit (testOcclusion, src/cl/kernel/NormalBVH.cl:235-317): 1 = occluded. */
 int mt_trace_any(mt_scene* scene, const void* rays, int n, int32_t* occluded_out);
+/* The same queries with the traversal work each ray costs: counts_out holds
+ * 2 ints per ray, interior-node visits and triangle tests, in the scene's
+ * record format (FP32 or FP16 binary records: the visits of the reference's
+ * stackless traversal, src/cl/kernel/NormalBVH.cl:14-92; the wide BVH: its
+ * 80-byte node visits). any != 0: any-hit (t_out unused, prim_out = occluded
+ * flags). No reference counterpart: it measures the algorithm's memory work
+ * (the roofline's algorithmic bytes). */
+int mt_trace_counts(mt_scene* scene, const void* rays, int n, int any, float* t_out, int32_t* prim_out,
+                    int32_t* counts_out);
 /* Device-resident variant for benchmarks: rays/outputs are mt_buffers. */
 int mt_trace_closest_dev(mt_scene* scene, mt_buffer* rays, int n, mt_buffer* t_out, mt_buffer* prim_out,
                          float* ms_out);

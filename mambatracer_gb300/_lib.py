@@ -130,6 +130,7 @@ SIGNATURES = {
     "mt_compact_isects_noalloc": (I, [P, P, P, I, P, P, P]),
     "mt_trace_closest": (I, [P, P, I, P, P]),
     "mt_trace_any": (I, [P, P, I, P]),
+    "mt_trace_counts": (I, [P, P, I, I, P, P, P]),
     "mt_trace_closest_dev": (I, [P, P, I, P, P, C.POINTER(C.c_float)]),
 }
 

@@ -167,6 +167,18 @@ class Scene:
         check(lib().mt_trace_any(self.h, _p(rays), rays.shape[0], _p(occ)))
         return occ
 
+    def trace_counts(self, rays: np.ndarray, any_hit: bool = False):
+        """Closest (or any) hits with the traversal work per ray: (t, prim or
+        occluded, int32 [n, 2] = interior-node visits, triangle tests)."""
+        rays = np.ascontiguousarray(rays)
+        assert rays.dtype == layout.RAY
+        n = rays.shape[0]
+        t = np.zeros(n, np.float32)
+        prim = np.zeros(n, np.int32)
+        counts = np.zeros((n, 2), np.int32)
+        check(lib().mt_trace_counts(self.h, _p(rays), n, int(any_hit), _p(t), _p(prim), _p(counts)))
+        return t, prim, counts
+
     def close(self):
         if self.h:
             check(lib().mt_scene_destroy(self.h))

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(os.path.dirname(HERE), "_build")
 LIB = os.path.join(HERE, "libmambatracer.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["mt_api.cu", "mt_kernels.cu", "mt_env.cu", "mt_compact.cu", "mt_job.cu", "mt_image.cu", "mt_server.cu", "mt_plain.cu", "mt_preview.cu", "mt_bvh.cu", "mt_obj.cpp", "mt_batch.cu"]
+SOURCES = ["mt_api.cu", "mt_kernels.cu", "mt_env.cu", "mt_compact.cu", "mt_job.cu", "mt_image.cu", "mt_server.cu", "mt_plain.cu", "mt_preview.cu", "mt_bvh.cu", "mt_obj.cpp", "mt_batch.cu", "mt_wide.cu"]
 
 
 def nvcc() -> str:

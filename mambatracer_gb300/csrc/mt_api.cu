@@ -257,6 +257,8 @@ void free_scene(mt_scene* s) {
   dfree(s->d_nodes);
   dfree(s->d_tris);
   dfree(s->d_qnodes);
+  dfree(s->d_wnodes);
+  dfree(s->d_wtris);
   dfree(s->d_env_rgb);
   dfree(s->d_env_lum);
   dfree(s->d_env_sat);
@@ -699,7 +701,8 @@ extern "C" int mt_bvh_import(mt_scene* s, const int32_t* nodes, const float* bou
 
 extern "C" int mt_scene_set_bvh_precision(mt_scene* s, int precision) {
   if (!s) return fail(MT_ERR_INVALID, "NULL scene");
-  if (precision != 0 && precision != 1) return fail(MT_ERR_INVALID, "BVH precision %d (0 FP32, 1 FP16)", precision);
+  if (precision < 0 || precision > 2)
+    return fail(MT_ERR_INVALID, "BVH precision %d (0 FP32, 1 FP16, 2 wide 8-bit)", precision);
   std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CU(cudaSetDevice(s->ctx->device));
   int q = quiesce(s->ctx);
@@ -827,7 +830,8 @@ extern "C" int mt_env_grid_sat(mt_context* ctx, const float* func, float* sat_ou
 
 // ------------------------------------------------------------- ray queries
 namespace {
-int query(mt_scene* s, const void* rays, int n, int any, float* t_out, int32_t* prim_out) {
+int query(mt_scene* s, const void* rays, int n, int any, float* t_out, int32_t* prim_out,
+          int32_t* counts_out = nullptr) {
   if (!s || (!rays && n) || !prim_out || (!any && !t_out) || n < 0) return fail(MT_ERR_INVALID, "bad argument");
   if (!s->has_bvh) return fail(MT_ERR_INVALID, "scene has no BVH");
   if (n == 0) return MT_OK;
@@ -837,19 +841,24 @@ int query(mt_scene* s, const void* rays, int n, int any, float* t_out, int32_t* 
   float4* d_rays = nullptr;
   float* d_t = nullptr;
   int* d_p = nullptr;
+  int* d_c = nullptr;
   int r = dalloc(&d_rays, 5 * (size_t)n);
   if (!r) r = dalloc(&d_t, (size_t)n);
   if (!r) r = dalloc(&d_p, (size_t)n);
+  if (!r && counts_out) r = dalloc(&d_c, 2 * (size_t)n);
   if (!r) {
     cudaMemcpyAsync(d_rays, rays, 80 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemsetAsync(ctx->d_scratch, 0, 8, ctx->stream);
-    if (launch_query(ctx->stream, s->view(), d_rays, n, any, d_t, d_p, ctx->d_scratch, ctx->d_scratch + 1, ctx->num_sms))
-      r = fail(MT_ERR_CUDA, "query launch: %s", cudaGetErrorString(cudaGetLastError()));
+    const int lr = counts_out ? launch_count(ctx->stream, s->view(), d_rays, n, any, d_t, d_p, d_c, ctx->d_scratch + 1)
+                              : launch_query(ctx->stream, s->view(), d_rays, n, any, d_t, d_p, ctx->d_scratch,
+                                             ctx->d_scratch + 1, ctx->num_sms);
+    if (lr) r = fail(MT_ERR_CUDA, "query launch: %s", cudaGetErrorString(cudaGetLastError()));
   }
   int err = 0;
   if (!r) {
     if (!any) cudaMemcpyAsync(t_out, d_t, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
     cudaMemcpyAsync(prim_out, d_p, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (counts_out) cudaMemcpyAsync(counts_out, d_c, 8 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
     cudaMemcpyAsync(&err, ctx->d_scratch + 1, 4, cudaMemcpyDeviceToHost, ctx->stream);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) r = fail(MT_ERR_CUDA, "query: %s", cudaGetErrorString(e));
@@ -858,9 +867,16 @@ int query(mt_scene* s, const void* rays, int n, int any, float* t_out, int32_t* 
   dfree(d_rays);
   dfree(d_t);
   dfree(d_p);
+  dfree(d_c);
   return r;
 }
 }  // namespace
+
+extern "C" int mt_trace_counts(mt_scene* s, const void* rays, int n, int any, float* t_out, int32_t* prim_out,
+                               int32_t* counts_out) {
+  if (!counts_out) return fail(MT_ERR_INVALID, "NULL counts");
+  return query(s, rays, n, any ? 1 : 0, any ? nullptr : t_out, prim_out, counts_out);
+}
 
 extern "C" int mt_trace_closest(mt_scene* s, const void* rays, int n, float* t_out, int32_t* prim_out) {
   return query(s, rays, n, 0, t_out, prim_out);

@@ -511,6 +511,7 @@ extern "C" int mt_bvh_build_device(mt_scene* s, int32_t* nodes_out, float* bound
 
 int refresh_qnodes(mt_scene* s) {
   dfree(s->d_qnodes);
+  if (int w = refresh_wide(s)) return w;
   if (s->precision != 1 || !s->has_bvh || s->nrec == 0) return MT_OK;
   int r = dalloc(&s->d_qnodes, 2 * (size_t)s->nrec);
   if (r) return r;

@@ -10,6 +10,7 @@ namespace mt {
 
 constexpr int kMaxDepth = 32;        // bounces per pass (reference: 15)
 constexpr int kStackDepth = 64;      // traversal stack = the reference's 64-bit bitstack
+constexpr int kWideStack = 32;       // wide-BVH traversal: node groups deferred (<= wide tree depth)
 constexpr int kTraceThreads = 128;   // threads per traversal CTA
 constexpr int kTraceMinBlocksClosest = 12;  // register bounds of the traversal kernels (CTAs per SM)
 constexpr int kTraceMinBlocksShadow = 8;
@@ -44,14 +45,27 @@ static_assert(sizeof(Material) == 144, "Material layout");
 //     (p2 - p1, 0), (p3 - p1, 0), the edges of the reference's Moller-Trumbore.
 //   qnodes: FP16 child boxes rounded outward (precision 1), 2 x 16 B per record:
 //     (L.x, L.y, R.x, R.y) as (lo, hi) half2 pairs, then (L.z, R.z, left ref, right ref).
+//   wnodes: the wide BVH (precision 2), 5 uint4 = 80 B per node, root 0:
+//     w0 = (origin x, y, z as float bits, ex | ey << 8 | ez << 16 | imask << 24):
+//          per-axis scale 2^(e - 127), imask bit s = slot s holds an interior node
+//     w1 = (first child node, first triangle, lmask, 0): lmask bit s = slot s holds
+//          a triangle; the child node in interior slot s is first child + the
+//          interior slots below s, the triangle in leaf slot s is wtris entry first
+//          triangle + the leaf slots below s
+//     w2 = (lo.x slots 0-3, lo.x 4-7, lo.y 0-3, lo.y 4-7), w3 = (lo.z .., hi.x ..),
+//     w4 = (hi.y .., hi.z ..): one quantised plane per byte, plane = origin + q 2^(e-127);
+//          an empty slot holds lo = 255, hi = 0 (never hit)
+//   wtris: the triangles in wide-leaf order, 3 float4 each as in tris.
 struct DevScene {
   const float4* nodes;
   const float4* qnodes;
   const float4* tris;
+  const uint4* wnodes;
+  const float4* wtris;
   int root_ref;
   int ntri;
   int nrec;
-  int precision;
+  int precision;  // traversal format: 0 FP32 records, 1 FP16 records, 2 the wide BVH
   // shading data in the reference layout
   const float4* points;
   const float2* uvs;

@@ -91,6 +91,9 @@ struct mt_scene {
   float4* d_nodes = nullptr;
   float4* d_tris = nullptr;
   uint4* d_qnodes = nullptr;  // FP16 records (precision 1)
+  uint4* d_wnodes = nullptr;  // wide BVH with 8-bit child boxes (precision 2)
+  float4* d_wtris = nullptr;
+  int nwide = 0, wdepth = 0;
   int nrec = 0, root_ref = 0, depth = 0, has_bvh = 0, precision = 0;
   // environment
   float4* d_env_rgb = nullptr;
@@ -121,7 +124,9 @@ struct mt_scene {
     s.root_ref = root_ref;
     s.ntri = ntri;
     s.nrec = nrec;
-    s.precision = (precision == 1 && d_qnodes) ? 1 : 0;
+    s.wnodes = d_wnodes;
+    s.wtris = d_wtris;
+    s.precision = (precision == 1 && d_qnodes) ? 1 : (precision == 2 && d_wnodes) ? 2 : 0;
     s.points = d_points;
     s.uvs = d_uvs;
     s.normals = d_normals;
@@ -235,8 +240,10 @@ void join_jobs(mt_context* ctx);
 int quiesce(mt_context* ctx);
 // Waits for the requests running on the context's servers' lanes.
 void servers_sync(mt_context* ctx);
-// Rebuild (precision 1) or drop the scene's FP16 records from its FP32 records.
+// Rebuild (precision 1) or drop the scene's FP16 records from its FP32 records,
+// and the wide BVH (precision 2, refresh_wide).
 int refresh_qnodes(mt_scene* s);
+int refresh_wide(mt_scene* s);
 // MT_CDF_TABLES=0 turns the CDF tables of environment sampling off (the samplers
 // then search the SATs directly; the tables hold the same values).
 bool cdf_tables_enabled();

@@ -565,17 +565,36 @@ int trace_blocks_per_sm() {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest<MINB, 0>, kTraceThreads, 0);
   return n > 0 ? n : 1;
 }
+// The wide-BVH kernels are built for 8 resident blocks per SM whatever the
+// tuning's bound (at 12 or 16 their 80-byte node tests spill registers), and
+// refill after an eighth of the binary kernels' steps (a wide step tests eight
+// child boxes; measured on the 1M soup at 1080p, refill every 4, 8, 12, 16, 32,
+// 64 wide steps: bounce-1 closest hits 1.73, 1.76, 1.81, 1.86, 2.02, 2.21 ms).
+constexpr int kWideMinBlocks = 8;
+int wide_steps_of(int steps) { return std::max(2, steps / 8); }
+int wide_blocks_per_sm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest<kWideMinBlocks, 2>, kTraceThreads, 0);
+  return n > 0 ? n : 1;
+}
 template <int MINB>
 void launch_traces(cudaStream_t st, int grid, const DevScene& S, Ctrl* ctrl, int b, int mode, FrameBufs fb, int kahan,
                    bool closest) {
   const int steps = tuning_ref().refill_steps;
   if (closest) {
-    if (S.precision == 1)
+    const int f = S.precision;
+    if (f == 2)
+      k_trace_closest<kWideMinBlocks, 2><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, wide_steps_of(steps));
+    else if (f == 1)
       k_trace_closest<MINB, 1><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, steps);
     else
       k_trace_closest<MINB, 0><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, steps);
   } else {
-    if (S.precision == 1)
+    const int f = S.precision;
+    if (f == 2)
+      k_trace_shadow<kWideMinBlocks, 2><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan,
+                                                                        wide_steps_of(steps));
+    else if (f == 1)
       k_trace_shadow<MINB, 1><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan, steps);
     else
       k_trace_shadow<MINB, 0><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan, steps);
@@ -602,11 +621,15 @@ unsigned tuning_version() { return g_tuning_version.load(); }
 void launch_trace(cudaStream_t st, const DevScene& S, Ctrl* ctrl, int b, int mode, FrameBufs fb, int kahan, bool closest,
                   int N, int num_sms, bool shared) {
   static int bps[17] = {};
+  static int wide_bps = 0;
   const int minb = closest ? trace_minb() : shadow_minb();
   if (bps[minb] == 0)
     bps[minb] = minb == 16 ? trace_blocks_per_sm<16>() : minb == 12 ? trace_blocks_per_sm<12>() : trace_blocks_per_sm<8>();
+  if (wide_bps == 0) wide_bps = wide_blocks_per_sm();
+  const bool wide = S.precision == 2;
+  const int fit = wide ? wide_bps : bps[minb];
   const int want = closest ? trace_grid_bps() : shadow_grid_bps();
-  const int per_sm = !shared ? bps[minb] : want > 0 ? std::min(want, bps[minb]) : std::max(1, bps[minb] / 2);
+  const int per_sm = !shared ? fit : want > 0 ? std::min(want, fit) : std::max(1, fit / 2);
   const int grid = std::max(1, std::min(num_sms * per_sm, (N + kTraceThreads - 1) / kTraceThreads));
   if (minb == 16) launch_traces<16>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
   else if (minb == 12) launch_traces<12>(st, grid, S, ctrl, b, mode, fb, kahan, closest);
@@ -741,13 +764,73 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_query(DevScene S, const fl
                                                             float* __restrict__ t_out, int* __restrict__ prim_out,
                                                             int* work, int* err) {
   bool overflow = false;
+  const int steps = PREC == 2 ? kSteps / 8 : kSteps;
   if (any)
     tr::trace_persistent<true, kSteps, RefRays, QueryOut, PREC>(S, n, work, RefRays{rays}, QueryOut{1, t_out, prim_out},
-                                                                &overflow);
+                                                                &overflow, steps);
   else
     tr::trace_persistent<false, kSteps, RefRays, QueryOut, PREC>(S, n, work, RefRays{rays},
-                                                                 QueryOut{0, t_out, prim_out}, &overflow);
+                                                                 QueryOut{0, t_out, prim_out}, &overflow, steps);
   if (overflow) atomicExch(err, kDevErrStack);
+}
+
+// Traversal work per ray: the same traversal as k_query, one step at a time,
+// counting interior-node visits and triangle tests (counts[2 i], counts[2 i + 1]).
+// Binary records: the visits the reference's algorithm makes (a step is one or
+// the other, classified before it runs); the wide BVH: its 80-byte node visits.
+template <int PREC, bool ANY>
+__global__ void __launch_bounds__(kTraceThreads) k_count(DevScene S, const float4* __restrict__ rays, int n,
+                                                         float* __restrict__ t_out, int* __restrict__ prim_out,
+                                                         int* __restrict__ counts, int* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  tr::RayT r = RefRays{rays}(i);
+  bool overflow = false;
+  int hit = -1, sp = 0, visits = 0, tests = 0;
+  if constexpr (PREC == 2) {
+    uint2 stack[kWideStack];
+    tr::WideState w;
+    tr::wide_init(r, w);
+    int cnt[2] = {0, 0};
+    while (!tr::wide_steps<ANY>(S, r, w, sp, hit, stack, 1, &overflow, cnt)) {
+    }
+    visits = cnt[0];
+    tests = cnt[1];
+  } else {
+    typename tr::StackEntry<ANY>::type stack[kStackDepth];
+    int ref = S.root_ref;
+    const bool finite = tr::ray_is_finite(r);
+    for (;;) {
+      const bool node = ref >= 0;
+      const bool done = tr::trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, 1, &overflow);
+      visits += node;
+      tests += !node;
+      if (done) break;
+    }
+  }
+  if (overflow) atomicExch(err, kDevErrStack);
+  QueryOut{ANY ? 1 : 0, t_out, prim_out}(i, r, hit);
+  counts[2 * i] = visits;
+  counts[2 * i + 1] = tests;
+}
+
+int launch_count(cudaStream_t st, const DevScene& S, const float4* rays, int n, int any, float* t_out, int* prim_out,
+                 int* counts, int* err) {
+  const int g = (n + kTraceThreads - 1) / kTraceThreads;
+  if (n <= 0) return 0;
+#define MT_COUNT(P)                                                                              \
+  if (any) k_count<P, true><<<g, kTraceThreads, 0, st>>>(S, rays, n, t_out, prim_out, counts, err); \
+  else k_count<P, false><<<g, kTraceThreads, 0, st>>>(S, rays, n, t_out, prim_out, counts, err);
+  const int f = S.precision;
+  if (f == 2) {
+    MT_COUNT(2)
+  } else if (f == 1) {
+    MT_COUNT(1)
+  } else {
+    MT_COUNT(0)
+  }
+#undef MT_COUNT
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_query(cudaStream_t st, const DevScene& S, const float4* rays, int n, int any, float* t_out, int* prim_out,
@@ -755,7 +838,10 @@ int launch_query(cudaStream_t st, const DevScene& S, const float4* rays, int n, 
   int bps = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_query<0>, kTraceThreads, 0);
   if (bps < 1) bps = 1;
-  if (S.precision == 1)
+  const int f = S.precision;
+  if (f == 2)
+    k_query<2><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
+  else if (f == 1)
     k_query<1><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
   else
     k_query<0><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);

@@ -58,6 +58,10 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
                 unsigned long long* totals, bool shared = false, cudaStream_t side = nullptr,
                 cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 
+// Closest or any hit of reference-layout rays with the traversal work per ray
+// (interior-node visits, triangle tests), one ray per thread.
+int launch_count(cudaStream_t st, const DevScene& S, const float4* rays, int n, int any, float* t_out, int* prim_out,
+                 int* counts, int* err);
 int launch_query(cudaStream_t st, const DevScene& S, const float4* rays, int n, int any, float* t_out,
                  int* prim_out, int* work, int* err, int num_sms);
 

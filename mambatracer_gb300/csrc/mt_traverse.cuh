@@ -213,15 +213,201 @@ __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref,
   return false;
 }
 
+// ------------------------------------------------------------------ wide BVH
+// Precision 2: the same tree collapsed into nodes of up to eight children whose
+// boxes are quantised to 8 bits per plane against the node's FP32 origin and a
+// power-of-two scale per axis, rounded outward (Ylitie, Karras, Laine,
+// "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs",
+// HPG 2017). A node is 80 bytes (see DevScene::wnodes); leaves stay single
+// triangles tested by the same FP32 Moller-Trumbore as above, so a hit is the
+// same triangle at the same distance: a quantised box contains the child's
+// FP32 box, so every triangle the binary traversal reaches is reached here.
+// Only the visit order differs: of two triangles hit at exactly the same
+// distance, the one tested first is kept.
+//
+// A child plane's distance is fma(2^23 + q, a, b') with a = 2^e / d and
+// b' = (origin - o) / d - 2^23 a: the float 2^23 + q is the byte q dropped into
+// the mantissa of 2^23 (one byte permute), and b' folds the 2^23 back in with
+// one rounding, whose error is at most half a grid step (a / 2) plus the
+// rounding of (origin - o) / d itself. The builder leaves one grid step of
+// margin outside every FP32 box, so the tested box still contains it.
+//
+// Traversal state: the current node group (first child node, and a 32-bit
+// mask: bits 24-31 = interior children still to visit, at bit 24 + (slot ^
+// octant), bits 0-7 = the node's interior-slot mask) and triangle group (first
+// triangle, bits 0-7 = hit leaf slots still to test, bits 8-15 = the node's
+// leaf-slot mask). Interior children are taken in descending bit order, which
+// for the ray's direction octant visits the child slots nearest the ray's
+// origin first (the builder places a child in the slot of its centre's
+// octant). Groups with children left are pushed.
+struct WideState {
+  uint2 ngroup, tgroup;
+  unsigned oct;       // the ray's direction octant: bit 2 x < 0, bit 1 y < 0, bit 0 z < 0
+  float jx, jy, jz;   // 1/d with infinities replaced by +-2^100 (box tests only)
+};
+
+__device__ __forceinline__ float finite_inv(float i) { return isinf(i) ? copysignf(0x1p100f, i) : i; }
+
+__device__ __forceinline__ void wide_init(const RayT& r, WideState& w) {
+  w.oct = (r.dx < 0.f ? 4u : 0u) | (r.dy < 0.f ? 2u : 0u) | (r.dz < 0.f ? 1u : 0u);
+  w.jx = finite_inv(r.ix);
+  w.jy = finite_inv(r.iy);
+  w.jz = finite_inv(r.iz);
+  // the root: node 0 as interior slot 0 of a virtual parent whose first child is node 0
+  w.ngroup = make_uint2(0u, (1u << (24u + w.oct)) | 1u);
+  w.tgroup = make_uint2(0u, 0u);
+}
+
+// 2^23 + (byte k of w), exactly: the byte placed in the mantissa of 2^23.
+__device__ __forceinline__ float qbyte(unsigned w, int k) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + k));
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+// The 8-bit slot mask m with slot s moved to slot s ^ x (x in 0..7).
+__device__ __forceinline__ unsigned xor_permute8(unsigned m, unsigned x) {
+  if (x & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+  if (x & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+  if (x & 4u) m = ((m & 0x0Fu) << 4) | (m >> 4);
+  return m;
+}
+
+// Intersects the ray with a wide node's eight child boxes; sets the next node
+// and triangle groups from the children hit.
+__device__ __forceinline__ void wide_node(const DevScene& S, const RayT& r, WideState& w, unsigned node) {
+  const uint4* p = S.wnodes + 5 * (size_t)node;
+  const uint4 w0 = __ldg(p + 0), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
+  const unsigned imask = w0.w >> 24, lmask = w1.z & 0xFFu;
+  const float ax = __uint_as_float((w0.w & 0xFFu) << 23) * w.jx;
+  const float ay = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23) * w.jy;
+  const float az = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23) * w.jz;
+  const float bx = __fmaf_rn(-8388608.f, ax, (__uint_as_float(w0.x) - r.ox) * w.jx);
+  const float by = __fmaf_rn(-8388608.f, ay, (__uint_as_float(w0.y) - r.oy) * w.jy);
+  const float bz = __fmaf_rn(-8388608.f, az, (__uint_as_float(w0.z) - r.oz) * w.jz);
+  unsigned hits = 0;
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    // near / far plane words of this half, picked by the direction's signs
+    const unsigned lox = half ? w2.y : w2.x, loy = half ? w2.w : w2.z, loz = half ? w3.y : w3.x;
+    const unsigned hix = half ? w3.w : w3.z, hiy = half ? w4.y : w4.x, hiz = half ? w4.w : w4.z;
+    const unsigned nx = r.sx ? hix : lox, fx = r.sx ? lox : hix;
+    const unsigned ny = r.sy ? hiy : loy, fy = r.sy ? loy : hiy;
+    const unsigned nz = r.sz ? hiz : loz, fz = r.sz ? loz : hiz;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float tn = max3f(__fmaf_rn(qbyte(nx, k), ax, bx), __fmaf_rn(qbyte(ny, k), ay, by),
+                             __fmaf_rn(qbyte(nz, k), az, bz));
+      const float tf = min3f(__fmaf_rn(qbyte(fx, k), ax, bx), __fmaf_rn(qbyte(fy, k), ay, by),
+                             __fmaf_rn(qbyte(fz, k), az, bz));
+      // the reference's slack on the far distance (Util.cl:707-732)
+      if (fmaxf(tn, r.tmin) <= fminf(tf * 1.00000024f, r.tmax)) hits |= 1u << (4 * half + k);
+    }
+  }
+  w.ngroup = make_uint2(w1.x, (xor_permute8(hits & imask, w.oct) << 24) | imask);
+  w.tgroup = make_uint2(w1.y, (hits & lmask) | (lmask << 8));
+}
+
+// Runs at most `steps` traversal steps (a step tests one triangle and, when the
+// current node has no triangle left to test, visits the next node); returns
+// true when the ray is finished (hit_face / r.tmax hold the result).
+// cnt (work counts, or NULL): [0] += node visits, [1] += triangle tests.
+template <bool ANY>
+__device__ __forceinline__ bool wide_steps(const DevScene& S, RayT& r, WideState& w, int& sp, int& hit_face,
+                                           uint2* stack, int steps, bool* overflow, int* cnt = nullptr) {
+  const float4* __restrict__ tris = S.wtris;
+  for (int it = 0; it < steps; ++it) {
+    if (w.tgroup.y & 0xFFu) {
+      if (cnt) ++cnt[1];
+      const unsigned k = __ffs(w.tgroup.y) - 1u;
+      const unsigned idx = w.tgroup.x + __popc((w.tgroup.y >> 8) & ((1u << k) - 1u));
+      w.tgroup.y &= ~(1u << k);
+      const float4* tp = tris + 3 * (size_t)idx;
+      const float4 p1 = __ldg(tp + 0), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+      const float t = tri_t(r, p1, e1, e2);
+      if ((r.tmin < t) && (t < r.tmax)) {
+        hit_face = __float_as_int(p1.w);
+        if (ANY) return true;
+        r.tmax = t;
+      }
+      if (w.tgroup.y & 0xFFu) continue;
+    }
+    if (w.ngroup.y <= 0x00FFFFFFu) {
+      if (sp == 0) return true;
+      w.ngroup = stack[--sp];
+    }
+    const unsigned b = 31u - __clz(w.ngroup.y);
+    const unsigned slot = (b - 24u) ^ w.oct;
+    const unsigned node = w.ngroup.x + __popc(w.ngroup.y & ((1u << slot) - 1u) & 0xFFu);
+    w.ngroup.y &= ~(1u << b);
+    if (w.ngroup.y > 0x00FFFFFFu) {
+      if (sp >= kWideStack) {
+        *overflow = true;
+        return true;
+      }
+      stack[sp++] = w.ngroup;
+    }
+    if (cnt) ++cnt[0];
+    wide_node(S, r, w, node);
+  }
+  return false;
+}
+
 // Persistent traversal over `count` rays with per-lane refill: every lane that
 // finished its ray takes the next one from the global counter, so warps stay
 // full while rays of very different lengths run side by side.
 // Src: RayT load(int i); Dst: void store(int i, const RayT&, int hit_face).
 // steps: traversal steps a lane runs between two refill points (STEPS unless
 // given at run time).
-template <bool ANY, int STEPS, class Src, class Dst, int PREC = 0>
-__device__ __forceinline__ void trace_persistent(const DevScene& S, int count, int* work, Src src, Dst dst,
-                                                 bool* overflow, int steps = STEPS) {
+template <bool ANY, int STEPS, class Src, class Dst>
+__device__ __forceinline__ void trace_persistent_wide(const DevScene& S, int count, int* work, Src src, Dst dst,
+                                                      bool* overflow, int steps) {
+  const int lane = threadIdx.x & 31;
+  uint2 stack[kWideStack];
+  int i = -1;
+  bool exhausted = false;
+  RayT r;
+  WideState w;
+  int sp = 0, hit = -1;
+  for (;;) {
+    const bool need = (i < 0) && !exhausted;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(work, __popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const int k = base + __popc(m & ((1u << lane) - 1u));
+        if (k < count) {
+          i = k;
+          r = src(i);
+          wide_init(r, w);
+          sp = 0;
+          hit = -1;
+        }
+      }
+      if (base + __popc(m) >= count) exhausted = true;
+    }
+    const bool active = i >= 0;
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active && wide_steps<ANY>(S, r, w, sp, hit, stack, steps, overflow)) {
+      dst(i, r, hit);
+      i = -1;
+    }
+  }
+}
+
+template <bool ANY, int STEPS, class Src, class Dst, int PREC>
+__device__ __forceinline__ void trace_persistent_binary(const DevScene& S, int count, int* work, Src src, Dst dst,
+                                                        bool* overflow, int steps) {
   const int lane = threadIdx.x & 31;
   typename StackEntry<ANY>::type stack[kStackDepth];
   int i = -1;
@@ -257,6 +443,17 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, int count, i
       i = -1;
     }
   }
+}
+
+// PREC: 0 FP32 records, 1 FP16 records (binary, the reference's visit order),
+// 2 the wide BVH with 8-bit child boxes.
+template <bool ANY, int STEPS, class Src, class Dst, int PREC = 0>
+__device__ __forceinline__ void trace_persistent(const DevScene& S, int count, int* work, Src src, Dst dst,
+                                                 bool* overflow, int steps = STEPS) {
+  if constexpr (PREC == 2)
+    trace_persistent_wide<ANY, STEPS>(S, count, work, src, dst, overflow, steps);
+  else
+    trace_persistent_binary<ANY, STEPS, Src, Dst, PREC>(S, count, work, src, dst, overflow, steps);
 }
 
 

@@ -9,7 +9,11 @@ The 1M-triangle soup and the 3.3M-triangle stadium of the benchmark:
     the closest hit, and the closest hit is found by an any-hit query that
     reaches just past it (both traversals enter a node exactly when its box
     passes the slab test for the ray's interval);
-  * FP16 records give the same distances as FP32 records.
+  * the traversal work of the FP32 records (mt_trace_counts): the oracle's
+    triangle tests exactly, and no more interior visits than the oracle (deferred
+    nodes beyond the closest hit are dropped);
+  * FP16 records and the wide BVH with 8-bit boxes give the same distances as
+    FP32 records, and the wide BVH visits fewer nodes.
 """
 import numpy as np
 import pytest
@@ -42,9 +46,12 @@ def _check_scene(ctx, orc, sc, nrays, nsample):
     # a sample against the oracle, bit for bit
     idx = np.random.default_rng(72).choice(nrays, nsample, replace=False)
     sub = np.ascontiguousarray(layout.make_rays(o[idx], d[idx]))
-    to, po = oracle_trace(orc, sc, hn, hb, sub)
+    to, po, oc = oracle_trace(orc, sc, hn, hb, sub, counts=True)
     assert np.array_equal(p[idx], po)
     assert t[idx].tobytes() == to.tobytes()
+    _, _, gc = S.trace_counts(sub)
+    assert np.array_equal(gc[:, 1], oc[:, 1])
+    assert np.all(gc[:, 0] <= oc[:, 0])
 
     # any-hit before the closest hit: never occluded; just past it: occluded
     before = layout.make_rays(o, d)
@@ -54,11 +61,16 @@ def _check_scene(ctx, orc, sc, nrays, nsample):
     past["tMax"] = t[hit] * np.float32(1.001) + np.float32(1e-6)
     assert S.trace_any(past).all()
 
-    # FP16 records: the same distances
-    S.set_precision(1)
-    t16, p16 = S.trace_closest(rays)
-    assert t16.tobytes() == t.tobytes()
-    assert (p16 != p).sum() <= max(2, nrays // 10000)
+    # FP16 records, the wide BVH: the same distances
+    for prec in (1, 2):
+        S.set_precision(prec)
+        tq, pq = S.trace_closest(rays)
+        assert tq.tobytes() == t.tobytes()
+        assert (pq != p).sum() <= max(2, nrays // 10000)
+    _, _, wc = S.trace_counts(sub)
+    print(f"interior visits per ray: oracle {oc[:, 0].mean():.1f}, FP32 records {gc[:, 0].mean():.1f}, "
+          f"wide BVH {wc[:, 0].mean():.1f}; triangle tests {oc[:, 1].mean():.2f} / {wc[:, 1].mean():.2f}")
+    assert wc[:, 0].mean() < 0.6 * gc[:, 0].mean()
     S.close()
 
 
