@@ -870,17 +870,36 @@ def run_reference(args):
     value = rays / secs / 1e6
     sample = (f"each step: {threads} frames of {width}x{height} (1/16 of the 1080p pixels) rendered in parallel, "
               f"one per host thread; oracle/mt_oracle.cpp, the FP32 restatement pinned bit-exact to the reference kernels")
+    cfg = config_dict(args.workload, width, height, sc.ntri, world)
+    cfg.update({
+        "resolution": f"{width}x{height} sample frames (1/16 of the {W_DEFAULT}x{H_DEFAULT} pixels), one per thread",
+        "threads": threads,
+        "film": "FP32, plain adds (the reference's addAccum order)",
+        "launch": "host threads, one frame each; no graphs, no streams",
+        "light_grid": (f"{GRID[0]}x{GRID[1]} grid of {GRID[2]}x{GRID[3]}-tile cells, FP32 per-cell SATs in the "
+                       "reference's order, initial function (tile integrals of the map), not updated"
+                       if ENV_ON else "none"),
+        "parallelism": f"{threads} host threads (rank 0 only)",
+    })
+    if ENV_ON:
+        cfg["environment"] = (f"{ENV_W}x{ENV_H} FP32 lat-long sky gradient + 0.5 deg Gaussian sun (peak 5e4); SAT "
+                              "built in FP32 in the reference's order")
+    cfg.pop("l2", None)
     out = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (procedural soup and sky; no dataset)",
-        "config": config_dict(args.workload, W_DEFAULT, H_DEFAULT, sc.ntri, world),
+        "config": cfg,
         "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": ("the reference's OpenCL kernels need an OpenCL runtime (none on this host: no ICD, no PoCL) and "
-                 "its sources do not ship with this repository; its algorithm runs as the oracle restatement"),
+                 "its sources do not ship with this repository; its algorithm runs as the oracle restatement, whose "
+                 "frames are pinned bit for bit to the reference's kernels compiled as C++. That compiled reference "
+                 "(unoptimised: optimised builds of it corrupt memory) renders the same frame 25x slower than the "
+                 "restatement at the same optimisation level (oracle/ref/time_ref.py), so this arm overstates the "
+                 "reference's own CPU speed"),
     }
     print(json.dumps(out), flush=True)
 
