@@ -13,6 +13,23 @@ def frame_number(step: int, rank: int, world: int) -> float:
     return float(1 + step * world + rank)
 
 
+def assign_requests(costs, world: int):
+    """Served mode over N replicas: the rank that serves each request, in arrival
+    order, given each request's cost (pixels x spp, the work its frame passes
+    cost). Each request goes to the replica with the least work assigned so far
+    (ties: the lower rank). Every replica holds every scene resident (BVHs are
+    read-only) and runs its own merged-queue server; a request's film comes back
+    from the one replica that rendered it, so no film is ever reduced across
+    ranks."""
+    load = [0.0] * world
+    out = []
+    for c in costs:
+        r = min(range(world), key=lambda k: (load[k], k))
+        out.append(r)
+        load[r] += float(c)
+    return out
+
+
 def reduce_max_sum(seconds: float, rays: int, device=None):
     """(max over ranks of seconds, sum over ranks of rays) through torch.distributed;
     identity when no process group is initialised."""
