@@ -339,7 +339,7 @@ int mt_trace_closest_dev(mt_scene* scene, mt_buffer* rays, int n, mt_buffer* t_o
  * benchmark-semantics passes (mode 1) of one camera and returns its
  * accumulated film. A scheduler thread admits requests first come, first
  * served onto `lanes` preallocated lanes (stream + path state for the largest
- * frame) within a budget of path-state bytes (196 B per pixel; 0 = no limit);
+ * frame) within a budget of path-state bytes (200 B per pixel; 0 = no limit);
  * no device memory is allocated while requests run. Scenes used by queued or
  * running requests cannot be destroyed (MT_ERR_BUSY).
  * merged = m (1..lanes): the running requests share wavefront queues (lanes x

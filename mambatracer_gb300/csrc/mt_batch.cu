@@ -25,6 +25,7 @@ void free_bufs(FrameBufs& fb) {
   dfree(fb.hit_t);
   dfree(fb.hit_prim);
   dfree(fb.flag);
+  dfree(fb.live);
 }
 
 int alloc_bufs(FrameBufs& fb, size_t n) {
@@ -35,6 +36,7 @@ int alloc_bufs(FrameBufs& fb, size_t n) {
   if (!r) r = dalloc(&fb.hit_t, n);
   if (!r) r = dalloc(&fb.hit_prim, n);
   if (!r) r = dalloc(&fb.flag, n);
+  if (!r) r = dalloc(&fb.live, n);
   return r;
 }
 

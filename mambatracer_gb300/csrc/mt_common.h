@@ -110,6 +110,8 @@ struct Ctrl {
   int shadow[kMaxDepth + 2];    // shadow rays emitted at bounce b
   int work[2 * (kMaxDepth + 2)];
   int tiles[kMaxDepth + 2];
+  int live[kMaxDepth + 2];      // paths that go on after the hit phase of bounce b (two-launch shading)
+  int tiles2[kMaxDepth + 2];    // chunk counter of the second shading launch
   int error;
   int pad;
   unsigned long long rays[3];   // primary, extension, shadow traced

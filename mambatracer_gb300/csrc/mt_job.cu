@@ -102,6 +102,7 @@ void free_slot(JobSlot& s) {
   dfree(s.fb.s_c);
   dfree(s.fb.film);
   dfree(s.fb.film_c);
+  dfree(s.fb.live);
   dfree(s.d_ctrl);
   dfree(s.d_status);
   dfree(s.d_pp);
@@ -182,6 +183,7 @@ int alloc_slot(JobSlot& s, size_t N, int spp, int max_depth, size_t status_strid
   if (!r) r = dalloc(&s.fb.s_c, N);
   if (!r) r = dalloc(&s.fb.film, N);
   if (!r) r = dalloc(&s.fb.film_c, N);
+  if (!r) r = dalloc(&s.fb.live, N);
   if (!r) r = dalloc(&s.d_ctrl, (size_t)spp);
   if (!r) r = dalloc(&s.d_status, status_stride * (size_t)max_depth * spp);
   if (!r) r = dalloc(&s.d_pp, (size_t)spp);

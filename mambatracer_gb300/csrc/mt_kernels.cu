@@ -301,6 +301,26 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const DevEnv& E, Re
   }
 }
 
+// A path that shade_hit kept going (benchmark semantics), loaded again from its
+// queue slot j: the hit record and BSDF set-up are recomputed from the same
+// inputs by the same code, so they equal what shade_hit computed.
+template <class Res>
+__device__ __forceinline__ void shade_load(const DevScene& S, Res res, int b, const FrameBufs& fb, int j,
+                                           PathState& P) {
+  const float4 qo = __ldg(fb.q_o[(b + 1) & 1] + j);
+  const float4 qd = __ldg(fb.q_d[(b + 1) & 1] + j);
+  const int pixel = __float_as_int(qo.w);
+  P.alive = true;
+  P.pixel = pixel;
+  res(pixel, P);
+  const V o = mk(qo.x, qo.y, qo.z, 0.f), d = mk(qd.x, qd.y, qd.z, 0.f);
+  P.thr = fb.thr[pixel];
+  P.ps = fb.ps[pixel];
+  P.spec = fb.flag[pixel];
+  hit_record(S, o, d, __ldg(fb.hit_t + j), __ldg(fb.hit_prim + j), P.H);
+  P.B = setup_bsdf(S, d, P.H.n, P.H.mat);
+}
+
 // gid: the work-item id the samples are keyed on (mode 0: the compacted slot,
 // mode 1: the pixel's id). Writes the path state back; P.alive turns false when
 // Russian roulette ends the path.
@@ -489,6 +509,79 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade(DevScene S, DevEn
   }
 }
 
+// Benchmark semantics in two launches (the default; MT_SHADE_SPLIT=0 runs the
+// single kernel above). k_shade_hit runs the hit record, the BSDF set-up and
+// LightHitPass over the whole queue and lists the slots of the paths that go
+// on; k_shade_cont runs the texture pass, DirectLight, SampleBSDFRayDirection
+// and Russian roulette over that list alone. Each is half the code (less
+// instruction fetch), and the second runs on full warps instead of warps whose
+// terminated paths idle through the light and BSDF samples. Samples are keyed on
+// the pixel, so the list's order carries no meaning.
+template <int MINB, int LEAN = 0, class Res = OneFrame>
+__global__ void __launch_bounds__(kShadeThreads, MINB) k_shade_hit(DevScene S, DevEnv E, Res res, Ctrl* ctrl, int b,
+                                                             FrameBufs fb) {
+  const int count = ctrl->count[b];
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  for (;;) {
+    int chunk = 0;
+    if (lane == 0) chunk = atomicAdd(&ctrl->tiles[b], 1);
+    chunk = __shfl_sync(0xffffffffu, chunk, 0);
+    if (chunk * 32 >= count) break;
+    const int j = chunk * 32 + lane;
+    PathState P;
+    shade_hit<1, LEAN>(S, E, res, b, fb, j, count, P);
+    const unsigned am = __ballot_sync(0xffffffffu, P.alive);
+    int base = 0;
+    if (lane == 0 && am) base = atomicAdd(&ctrl->live[b], __popc(am));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (P.alive) fb.live[base + __popc(am & lt)] = j;
+  }
+}
+
+template <int MINB, bool TEX = false, int LEAN = 0, class Res = OneFrame>
+__global__ void __launch_bounds__(kShadeThreads, MINB) k_shade_cont(DevScene S, DevEnv E, Res res, Ctrl* ctrl, int b,
+                                                              FrameBufs fb) {
+  const int count = ctrl->live[b];
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int nq = b & 1;  // queue written for bounce b + 1
+  for (;;) {
+    int chunk = 0;
+    if (lane == 0) chunk = atomicAdd(&ctrl->tiles2[b], 1);
+    chunk = __shfl_sync(0xffffffffu, chunk, 0);
+    if (chunk * 32 >= count) break;
+    const int k = chunk * 32 + lane;
+    PathState P;
+    P.alive = false;
+    ShadeOut R;
+    R.has_shadow = false;
+    if (k < count) {
+      shade_load(S, res, b, fb, __ldg(fb.live + k), P);
+      shade_continue<1, TEX, LEAN>(S, E, b, fb, pixel_gid(P.local), P, R);
+    }
+    const unsigned am = __ballot_sync(0xffffffffu, P.alive), sm = __ballot_sync(0xffffffffu, R.has_shadow);
+    int qa = 0, qs = 0;
+    if (lane == 0) {
+      if (am) qa = atomicAdd(&ctrl->count[b + 1], __popc(am));
+      if (sm) qs = atomicAdd(&ctrl->shadow[b], __popc(sm));
+    }
+    qa = __shfl_sync(0xffffffffu, qa, 0);
+    qs = __shfl_sync(0xffffffffu, qs, 0);
+    if (P.alive) {
+      const int slot = qa + __popc(am & lt);
+      fb.q_o[nq][slot] = mk(P.H.p.x, P.H.p.y, P.H.p.z, __int_as_float(P.pixel));
+      fb.q_d[nq][slot] = mk(R.ndir.x, R.ndir.y, R.ndir.z, 0.f);
+    }
+    if (R.has_shadow) {
+      const int sslot = qs + __popc(sm & lt);
+      fb.s_o[sslot] = R.sho;
+      fb.s_d[sslot] = R.shd;
+      fb.s_c[sslot] = R.shc;
+    }
+  }
+}
+
 // Adds a finished pass's ray counts into the job's running totals
 // [primary, extension, shadow].
 __global__ void k_accumulate(const Ctrl* ctrl, int max_depth, int n_pixels, unsigned long long* totals) {
@@ -530,6 +623,10 @@ int env_shade_minb() {
   const char* e = std::getenv("MT_SHADE_MINB");
   int x = e ? std::atoi(e) : kShadeMinBlocks;
   return (x == 3 || x == 4 || x == 5) ? x : kShadeMinBlocks;
+}
+bool shade_split() {
+  static const bool on = !(std::getenv("MT_SHADE_SPLIT") && std::atoi(std::getenv("MT_SHADE_SPLIT")) == 0);
+  return on;
 }
 int env_steps() {
   const char* e = std::getenv("MT_REFILL_STEPS");
@@ -667,6 +764,26 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
         k_shade_ref<3, true><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
       else
         k_shade_ref<3><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
+    } else if (shade_split()) {
+      const int sm = shade_minb();
+      if (shade_bps[sm] == 0) shade_bps[sm] = shade_blocks_per_sm(sm);
+      const int sgrid = std::max(1, std::min(num_sms * shade_bps[sm], tiles));
+      const bool lean = S.nlights == 0 && E.present && E.grid_on && !S.tex_on;
+      const OneFrame R1{d_pp};
+      if (lean)
+        k_shade_hit<4, 1><<<sgrid, kShadeThreads, 0, st>>>(S, E, R1, ctrl, b, fb);
+      else
+        k_shade_hit<4><<<sgrid, kShadeThreads, 0, st>>>(S, E, R1, ctrl, b, fb);
+      if (S.tex_on)
+        k_shade_cont<4, true><<<sgrid, kShadeThreads, 0, st>>>(S, E, R1, ctrl, b, fb);
+      else if (lean && sm == 4)
+        k_shade_cont<4, false, 1><<<sgrid, kShadeThreads, 0, st>>>(S, E, R1, ctrl, b, fb);
+      else if (sm == 4)
+        k_shade_cont<4><<<sgrid, kShadeThreads, 0, st>>>(S, E, R1, ctrl, b, fb);
+      else if (sm == 5)
+        k_shade_cont<5><<<sgrid, kShadeThreads, 0, st>>>(S, E, R1, ctrl, b, fb);
+      else
+        k_shade_cont<3><<<sgrid, kShadeThreads, 0, st>>>(S, E, R1, ctrl, b, fb);
     } else {
       const int sm = shade_minb();
       if (shade_bps[sm] == 0) shade_bps[sm] = shade_blocks_per_sm(sm);
@@ -724,7 +841,13 @@ int launch_batch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const
   k_raygen_batch<<<(total + 255) / 256, 256, 0, st>>>(B, total, ctrl, fb);
   for (int b = 1; b <= max_depth; ++b) {
     launch_trace(st, S, ctrl, b, 1, fb, kahan, true, total, num_sms, shared);
-    if (S.tex_on)
+    if (shade_split()) {
+      k_shade_hit<4, 0, BatchFrames><<<sgrid, kShadeThreads, 0, st>>>(S, E, B, ctrl, b, fb);
+      if (S.tex_on)
+        k_shade_cont<4, true, 0, BatchFrames><<<sgrid, kShadeThreads, 0, st>>>(S, E, B, ctrl, b, fb);
+      else
+        k_shade_cont<4, false, 0, BatchFrames><<<sgrid, kShadeThreads, 0, st>>>(S, E, B, ctrl, b, fb);
+    } else if (S.tex_on)
       k_shade<4, true, 0, BatchFrames><<<sgrid, kShadeThreads, 0, st>>>(S, E, B, ctrl, b, fb);
     else
       k_shade<4, false, 0, BatchFrames><<<sgrid, kShadeThreads, 0, st>>>(S, E, B, ctrl, b, fb);

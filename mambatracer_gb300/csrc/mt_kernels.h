@@ -20,6 +20,7 @@ struct FrameBufs {
   float4* s_c;      // shadow queue: contribution.xyz
   float4* film;     // accumulated radiance per pixel
   float4* film_c;   // Kahan compensation per pixel
+  int* live;        // queue slots of the paths that go on after the hit phase (two-launch shading)
 };
 
 // Launch shapes of the hot kernels, process-wide (one GPU per process):

@@ -11,7 +11,7 @@
 // requests run at once; their kernels overlap on the GPU (persistent traversal
 // grids are sized by the frame, so a small request leaves SMs to the others).
 // Admission is first come, first served within a budget of path-state and film
-// bytes (196 B per pixel). A completed request's film is copied to pinned
+// bytes (200 B per pixel). A completed request's film is copied to pinned
 // staging and from there to the caller's buffer by the scheduler thread; a
 // host callback on the lane's stream wakes the scheduler, which measures the
 // request's latency from submission. Scenes are reference-counted while
@@ -96,7 +96,7 @@ struct Round {
   bool used = false;
 };
 
-constexpr size_t kPathBytesPerPixel = 196;
+constexpr size_t kPathBytesPerPixel = 200;
 constexpr int kRounds = 3;
 
 // One merge stream: its slots, its share of the queues, its round ring.
@@ -176,6 +176,7 @@ void free_lane(Lane& L) {
   dfree(L.fb.s_c);
   dfree(L.fb.film);
   dfree(L.fb.film_c);
+  dfree(L.fb.live);
   dfree(L.d_ctrl);
   dfree(L.d_status);
   dfree(L.d_pp);
@@ -209,6 +210,7 @@ int alloc_lane(Lane& L, size_t N, int spp, int depth, size_t stride) {
   if (!r) r = dalloc(&L.fb.s_c, N);
   if (!r) r = dalloc(&L.fb.film, N);
   if (!r) r = dalloc(&L.fb.film_c, N);
+  if (!r) r = dalloc(&L.fb.live, N);
   if (!r) r = dalloc(&L.d_ctrl, (size_t)spp);
   if (!r) r = dalloc(&L.d_status, stride * (size_t)depth * spp);
   if (!r) r = dalloc(&L.d_pp, (size_t)spp);
@@ -272,6 +274,7 @@ void free_merged(mt_server* s) {
   dfree(s->mfb.hit_t);
   dfree(s->mfb.hit_prim);
   dfree(s->mfb.flag);
+  dfree(s->mfb.live);
   for (MergeGroup& G : s->groups) {
     for (Round& Rd : G.rounds) {
       if (Rd.h_tab) cudaFreeHost(Rd.h_tab);
@@ -307,6 +310,7 @@ int alloc_merged(mt_server* s, size_t N, int m) {
   if (!r) r = dalloc(&s->mfb.hit_t, P);
   if (!r) r = dalloc(&s->mfb.hit_prim, P);
   if (!r) r = dalloc(&s->mfb.flag, P);
+  if (!r) r = dalloc(&s->mfb.live, P);
   for (Lane& L : s->lanes)
     if (!r && cudaMallocHost((void**)&L.h_stage, sizeof(float4) * N) != cudaSuccess)
       r = fail(MT_ERR_NOMEM, "pinned film staging");
@@ -341,6 +345,7 @@ int alloc_merged(mt_server* s, size_t N, int m) {
     G.fb.s_o += base;
     G.fb.s_d += base;
     G.fb.s_c += base;
+    G.fb.live += base;
     base += (size_t)n * N;
   }
   s->slot_px = N;

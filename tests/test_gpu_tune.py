@@ -56,3 +56,47 @@ def test_films_do_not_depend_on_the_tuning(ctx, soup_scene):
             assert all(x.tobytes() == y.tobytes() for x, y in zip(a, b)) and np.array_equal(ra, rb)
     finally:
         api.set_tuning(before)
+
+
+_SINGLE_LAUNCH = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r})
+from mambatracer_gb300 import api, scenes
+from oracle.oracle import Oracle, bvh_build
+sc = scenes.soup(20000, seed=8, extent=0.8, width=96, height=64)
+nodes, bounds, _, _ = bvh_build(Oracle(), sc)
+ctx = api.Context(0)
+S = api.Scene(ctx, sc)
+S.import_bvh(nodes, bounds)
+S.set_env(scenes.sky_env(256, 128), 256, 128)
+S.grid_config(160, 160, 16, 32, {grid})
+J = api.Job(ctx, S, 96, 64, max_depth=6, mode=1, rr_depth=3, film_kahan=1, use_graph=1, inflight=2)
+J.set_camera(sc.camera)
+for f in range(4):
+    J.render(None, float(f + 1))
+np.save({out!r}, J.film())
+rays = J.total_rays()
+np.save({out!r} + ".rays.npy", rays)
+J.close(); S.close(); ctx.close()
+"""
+
+
+@pytest.mark.parametrize("grid", [0, 2])
+def test_two_launch_shading_equals_one_launch(ctx, soup_scene, tmp_path, grid):
+    """Benchmark-semantics shading runs in two launches (hit phase, then the
+    paths that go on); MT_SHADE_SPLIT=0 (read once per process) runs the single
+    kernel. Films and ray counts are bit-identical either way."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    films = []
+    for split in ("1", "0"):
+        out = str(tmp_path / f"film{split}.npy")
+        env = dict(os.environ, MT_SHADE_SPLIT=split)
+        subprocess.run([sys.executable, "-c", _SINGLE_LAUNCH.format(root=root, out=out, grid=grid)], env=env,
+                       check=True, timeout=600)
+        films.append((np.load(out), np.load(out + ".rays.npy")))
+    assert films[0][0].tobytes() == films[1][0].tobytes()
+    assert np.array_equal(films[0][1], films[1][1])
+    assert films[0][0][:, :3].sum() > 0
