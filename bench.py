@@ -261,6 +261,49 @@ def algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_count, t
     return int(n * 48 + rec_bytes * v_int + 48 * tri), float(v_int) / n, float(tri) / n
 
 
+def kernel_rooflines(kprof, per_kernel, peak, rays, counts, closest_alg_bytes, closest_ms):
+    """Per-kernel roofline of the bounce-1 launches: each memory level's bytes per
+    launch from one ncu capture of that launch (profiles/kernels_soup1M_1080p.json)
+    over the launch's CUDA-event time in this run, with the warp efficiency and the
+    stalls that bound it. Algorithmic fractions: the closest-hit traversal's (the
+    headline roofline); shading's over the whole frame, from the frame's device
+    counts as a lower bound (queue entry 32 + hit 8 + path state 36 B read by the
+    hit phase; for every path that goes on, list 8 + the same 76 read + path state
+    36 + next queue 32 written; 48 B per shadow ray written; the paths that Russian
+    roulette ends after their sample and the film adds are left out); the shadow
+    rays' visit counts are not known off the device, so their fraction is absent."""
+    if kprof is None:
+        return None
+    ks = kprof["kernels"]
+    out = {}
+
+    def level_rates(names, ms):
+        d = {k: sum(ks[n][k] for n in names) for k in ("dram_bytes", "l2_bytes", "l1_global_bytes", "l1_local_bytes")}
+        s = ms * 1e-3
+        r = {"launch_ms": round(ms, 4), **d,
+             "dram_gbs": round(d["dram_bytes"] / s / 1e9, 1), "l2_gbs": round(d["l2_bytes"] / s / 1e9, 1),
+             "l1_global_gbs": round(d["l1_global_bytes"] / s / 1e9, 1),
+             "l1_local_gbs": round(d["l1_local_bytes"] / s / 1e9, 1),
+             "dram_frac_of_measured_peak": round(d["dram_bytes"] / s / 1e9 / peak, 4)}
+        for k in ("simt_efficiency", "stall_long_scoreboard_per_issue", "stall_no_instruction_per_issue",
+                  "issue_active_pct", "registers", "grid"):
+            r[k] = [ks[n][k] for n in names] if len(names) > 1 else ks[names[0]][k]
+        return r
+
+    out["k_trace_closest"] = level_rates(["k_trace_closest"], per_kernel["trace_closest_b1"])
+    out["k_trace_closest"]["alg_gbs"] = round(closest_alg_bytes / (closest_ms * 1e-3) / 1e9, 1)
+    out["k_trace_shadow"] = level_rates(["k_trace_shadow"], per_kernel["trace_shadow_b1"])
+    out["k_shade_hit+k_shade_cont"] = level_rates(["k_shade_hit", "k_shade_cont"], per_kernel["shade_b1"])
+    queue = int(rays[0] + rays[1])
+    goes_on = int(np.sum(counts))
+    alg = queue * 76 + goes_on * (8 + 76 + 68) + int(rays[2]) * 48
+    shade_ms = sum(v for k, v in per_kernel.items() if k.startswith("shade_"))
+    out["k_shade_hit+k_shade_cont"]["frame_alg_bytes_lower_bound"] = alg
+    out["k_shade_hit+k_shade_cont"]["frame_ms"] = round(shade_ms, 4)
+    out["k_shade_hit+k_shade_cont"]["frame_alg_frac_lower_bound"] = round(alg / (shade_ms * 1e-3) / 1e9 / peak, 4)
+    return out
+
+
 # ------------------------------------------------------------- GPU arm
 def bench_scene(ctx, kind, small, width, height, precision):
     """The workload's scene on the device as every step renders it: the BVH built on
@@ -478,6 +521,7 @@ def run_gpu(args):
         per_kernel = {n: round(float(v), 4) for n, v in zip(names, kms)}
         trace_total = float(sum(v for n, v in per_kernel.items() if n.startswith("trace_")))
         frame_total = float(kms.sum())
+        prof_rays, prof_counts = pj.stats()  # the last profiled frame
         pj.close()
         from oracle.oracle import Oracle
         orc = Oracle()
@@ -506,12 +550,14 @@ def run_gpu(args):
         peak = float(peaks.get("hbm_gbs", 6800.0))
         t_b1 = per_kernel["trace_closest_b1"]
         traffic, traffic_src = None, None
-        tp = os.path.join(ROOT, "profiles", "trace_closest_soup1M_1080p.json")
-        if not args.small and args.workload == "soup" and os.path.exists(tp):
-            tj = json.load(open(tp))
-            key = "dram_bytes_per_launch_fp16_records" if args.precision else "dram_bytes_per_launch"
-            traffic, traffic_src = tj.get(key), tj["source"]
+        kp = os.path.join(ROOT, "profiles", "kernels_soup1M_1080p.json")
+        kprof = None
+        if not args.small and args.workload == "soup" and args.precision == 1 and os.path.exists(kp):
+            kprof = json.load(open(kp))
+            traffic = kprof["kernels"]["k_trace_closest"]["dram_bytes"]
+            traffic_src = "profiles/kernels_soup1M_1080p.json (" + kprof["source"] + ")"
         achieved = alg_bytes / (t_b1 * 1e-3) / 1e9
+        per_kernel_roofline = kernel_rooflines(kprof, per_kernel, peak, prof_rays, prof_counts, alg_bytes, t_b1)
         roofline = {"bound": "hbm", "kernel": "k_trace_closest (bounce 1, primary rays)",
                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
@@ -521,7 +567,8 @@ def run_gpu(args):
                     "interior_visits_per_ray": round(v_int, 2), "triangle_tests_per_ray": round(tri, 2),
                     "visit_counts": visit_src,
                     "launch_ms": round(t_b1, 4),
-                    "trace_share_of_frame": round(trace_total / frame_total, 3), "per_kernel_ms": per_kernel}
+                    "trace_share_of_frame": round(trace_total / frame_total, 3), "per_kernel_ms": per_kernel,
+                    "per_kernel": per_kernel_roofline}
         # CPU baseline: the oracle on the host cores, a bounded sample
         cw, ch = width // 4, height // 4
         csc, cn, cb, cenv, clum, csat = sc, nodes, bounds, env, None, None
