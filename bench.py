@@ -472,7 +472,7 @@ def run_gpu(args):
     import ctypes as C
 
     from mambatracer_gb300._lib import check, lib
-    nbuf = 5  # read i completes when read i + 4 is enqueued (four stay pending): its buffer is free for read i + 5
+    nbuf = 9  # read i completes when read i + 8 is enqueued (eight stay pending): its buffer is free for read i + 9
     film_host = [torch.empty((width * height, 4), dtype=torch.float32, pin_memory=True) for _ in range(nbuf)]
     cam_host = torch.empty(64, dtype=torch.uint8, pin_memory=True)
     cam_host.numpy()[:] = np.frombuffer(cam.tobytes(), np.uint8)

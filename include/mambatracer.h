@@ -215,10 +215,10 @@ int mt_render_frame(mt_job* job, const int32_t* seeds, float frame_count);
 int mt_film_read(mt_job* job, float* rgba, int resolve);
 /* The same read, enqueued: copies the film as of every frame submitted so far
  * into rgba (pinned host memory for an asynchronous copy) and returns at once,
- * so the next frames can be submitted while this one finishes. Up to four
- * reads stay pending; a fifth first completes the oldest. rgba must stay valid
+ * so the next frames can be submitted while this one finishes. Up to eight
+ * reads stay pending; a ninth first completes the oldest. rgba must stay valid
  * until its read completes (mt_film_wait, mt_film_read, mt_film_clear, or the
- * fifth read after it); resolve is applied then. No counterpart in the
+ * ninth read after it); resolve is applied then. No counterpart in the
  * reference, whose image read (CImage.processImage/readImage) blocks. */
 int mt_film_read_async(mt_job* job, float* rgba, int resolve);
 int mt_film_wait(mt_job* job);

@@ -218,7 +218,7 @@ class Job:
         """Enqueue a read of the film into `out` (float32, width*height x 4; pinned
         memory for a copy that overlaps the next frame); complete it with wait()."""
         assert out.dtype == np.float32 and out.size == self.width * self.height * 4 and out.flags.c_contiguous
-        self._pending = (getattr(self, "_pending", []) + [out])[-4:]
+        self._pending = (getattr(self, "_pending", []) + [out])[-8:]
         check(lib().mt_film_read_async(self.h, _p(out), int(resolve)))
 
     def wait(self):

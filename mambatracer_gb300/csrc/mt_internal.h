@@ -190,7 +190,7 @@ struct mt_job {
   unsigned long long* d_totals = nullptr;  // running [primary, extension, shadow, error]
   std::vector<Ctrl> h_ctrl;
   // asynchronous film reads
-  static constexpr int kMaxReads = 4;
+  static constexpr int kMaxReads = 8;
   struct Read {
     float* host = nullptr;
     int resolve = 0;

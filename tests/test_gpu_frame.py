@@ -166,7 +166,7 @@ def test_inflight_frames_match_one_stream(ctx, orc, inflight):
                 per_frame.append(J.film(resolve=True))
             else:
                 # pipelined reads: the film after frame f is read while later frames
-                # render; the fifth pending read completes the oldest
+                # render; the ninth pending read completes the oldest
                 J.film_async(bufs[f], resolve=True)
         if n > 1:
             J.wait()
