@@ -920,12 +920,12 @@ __global__ void __launch_bounds__(kTraceThreads) k_count(DevScene S, const float
     visits = cnt[0];
     tests = cnt[1];
   } else {
-    typename tr::StackEntry<ANY>::type stack[kStackDepth];
+    typename tr::StackEntry<ANY>::type stack[kStackDepth], top;
     int ref = S.root_ref;
     const bool finite = tr::ray_is_finite(r);
     for (;;) {
       const bool node = ref >= 0;
-      const bool done = tr::trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, 1, &overflow);
+      const bool done = tr::trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, top, 1, &overflow);
       visits += node;
       tests += !node;
       if (done) break;
