@@ -214,16 +214,20 @@ def main():
     ap.add_argument("--frames", type=int, default=24)
     ap.add_argument("--rounds", type=int, default=2)
     ap.add_argument("--served", action="store_true", help="also search the merged server's slots and streams")
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
+                    help="traversal format of the scenes (mt_scene_set_bvh_precision; the bench's is 1)")
     args = ap.parse_args()
     build.build()
     ctx = api.Context(0)
     sc = scenes.soup(args.triangles, seed=1, width=args.width, height=args.height)
     S = api.Scene(ctx, sc)
     S.build_bvh_device(want_arrays=False)
+    S.set_precision(args.precision)
     S.set_env(scenes.sky_env(2048, 1024), 2048, 1024)
     S.grid_config(1600, 1600, 16, 32, enable=2)
+    records = {0: "FP32 records", 1: "FP16 records", 2: "wide BVH"}[args.precision]
     workload = (f"soup {args.triangles} triangles, {args.width}x{args.height}, depth 8, RR from 3, 2048x1024 sky, "
-                "1600x1600 light grid (FP64 cell SATs), 6 frames in flight")
+                f"1600x1600 light grid (FP64 cell SATs), 6 frames in flight, {records}")
     log = lambda m: print(m, flush=True)  # noqa: E731
     key = f"soup{args.triangles}_{args.width}x{args.height}"
     res = autotune(ctx, S, sc.camera, args.width, args.height, workload, out=args.out, rounds=args.rounds,
@@ -233,6 +237,7 @@ def main():
         st = scenes.stadium(width=args.width, height=args.height)
         S2 = api.Scene(ctx, st)
         S2.build_bvh_device(want_arrays=False)
+        S2.set_precision(args.precision)
         S2.set_env(scenes.sky_env(2048, 1024), 2048, 1024)
         reqs = served_requests()
         served_measure(ctx, [S, S2], reqs[:4])({"lanes": 4, "merge_streams": 2})  # warm-up
