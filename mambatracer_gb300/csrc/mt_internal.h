@@ -166,8 +166,9 @@ struct JobSlot {
   cudaStream_t side = nullptr;  // shadow rays beside the next bounce's extension rays
   cudaEvent_t sfork = nullptr, sjoin = nullptr;
   cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr, done = nullptr;
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graphs[2] = {nullptr, nullptr};  // per shading form: one launch, two launches
   unsigned graph_version = 0;  // scene version the graph was captured against
+  bool ran = false;            // a frame has run on this slot (its control blocks hold its counts)
 };
 
 struct mt_job {
@@ -206,6 +207,9 @@ struct mt_job {
   // adaptive light grid (mode 1, scene grid on, environment present)
   unsigned scene_version = 0;
   unsigned tune_version = 0;  // launch-shape version the graphs were captured with
+  // benchmark-semantics shading form of the next frames (1 two launches, 0 one),
+  // chosen from the last finished frame's bounce-1 survivors; -1 not yet known
+  int shade_split = -1;
   int grid_on = 0, grid_fp64 = 0;
   int nu = 0, nv = 0, rx = 0, ry = 0;
   float* d_grid_func = nullptr;

@@ -108,8 +108,10 @@ void free_slot(JobSlot& s) {
   dfree(s.d_pp);
   if (s.h_pp) cudaFreeHost(s.h_pp);
   s.h_pp = nullptr;
-  if (s.graph) cudaGraphExecDestroy(s.graph);
-  s.graph = nullptr;
+  for (cudaGraphExec_t& g : s.graphs) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
   for (cudaEvent_t* e : {&s.fork, &s.ev0, &s.ev1, &s.done, &s.sfork, &s.sjoin}) {
     if (*e) cudaEventDestroy(*e);
     *e = nullptr;
@@ -386,7 +388,7 @@ int enqueue_frame(mt_job* j, JobSlot& s) {
     cudaEvent_t* ev = j->kev.empty() ? nullptr : j->kev.data() + per_pass_events * p;
     if (launch_pass(s.stream, S, E, s.d_pp + p, c.mode, c.max_depth, c.film_kahan, c.width, c.height, s.d_ctrl + p,
                     s.fb, s.d_status + j->status_stride * (size_t)c.max_depth * p, j->status_stride, ctx->num_sms,
-                    ev, j->d_totals, j->nslots > 1, s.side, s.sfork, s.sjoin))
+                    ev, j->d_totals, j->nslots > 1, s.side, s.sfork, s.sjoin, j->shade_split))
       return fail(MT_ERR_CUDA, "pass launch: %s", cudaGetErrorString(cudaGetLastError()));
   }
   return MT_OK;
@@ -405,10 +407,11 @@ extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_coun
     // The scene's arrays or grid configuration changed (the change waited for
     // every frame): recapture the graphs and set the light grid up again.
     for (JobSlot& t : j->slots)
-      if (t.graph) {
-        cudaGraphExecDestroy(t.graph);
-        t.graph = nullptr;
-      }
+      for (cudaGraphExec_t& g : t.graphs)
+        if (g) {
+          cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
     int r = setup_grid(j);
     if (r) return r;
     j->scene_version = j->scene->version;
@@ -416,17 +419,40 @@ extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_coun
   if (j->tune_version != tuning_version()) {
     // new launch shapes: capture the frames' graphs again, once their frames ran
     for (JobSlot& t : j->slots)
-      if (t.graph) {
-        CU(cudaStreamSynchronize(t.stream));
-        cudaGraphExecDestroy(t.graph);
-        t.graph = nullptr;
-      }
+      for (cudaGraphExec_t& g : t.graphs)
+        if (g) {
+          CU(cudaStreamSynchronize(t.stream));
+          cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
     j->tune_version = tuning_version();
   }
   JobSlot& s = j->slots[j->next];
   // The slot's previous frame must have consumed its pinned parameters; frames
   // on the other slots keep running meanwhile.
   CU(cudaEventSynchronize(s.done));
+  const int split_setting = shade_split_setting();
+  if (split_setting >= 0) {
+    j->shade_split = split_setting;
+  } else if (c.mode == 1 && c.max_depth >= 2) {
+    // One launch or two for the shading of the next frames: a finished frame's
+    // share of bounce-1 paths that went on decides (shade_split_for): this slot's
+    // last frame, or, while nothing is decided yet, the job's latest frame once it
+    // has finished. Both forms render the same film, and each slot holds a graph
+    // of each (both captured at its first frame), so a change costs nothing.
+    JobSlot* src = s.ran ? &s : nullptr;
+    if (!src && j->shade_split < 0 && j->last >= 0 && j->slots[j->last].ran) {
+      const cudaError_t q = cudaEventQuery(j->slots[j->last].done);
+      if (q == cudaSuccess) src = &j->slots[j->last];
+      else if (q != cudaErrorNotReady) return fail(MT_ERR_CUDA, "frame event: %s", cudaGetErrorString(q));
+    }
+    if (src) {
+      int counts[3] = {0, 0, 0};
+      CU(cudaMemcpyAsync(counts, src->d_ctrl, sizeof(counts), cudaMemcpyDeviceToHost, src->stream));
+      CU(cudaStreamSynchronize(src->stream));
+      j->shade_split = shade_split_for(counts[1], counts[2], j->shade_split < 0 ? 1 : j->shade_split);
+    }
+  }
   // CDeviceGI.loop updates the grid after each of its first frames
   // (src/cl/device/CDeviceGI.java:263-264): those frames accumulate.
   const int accumulate = j->grid_on && j->grid_frames < c.grid_updates;
@@ -451,22 +477,29 @@ extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_coun
   if (j->grid_on) CU(cudaStreamWaitEvent(s.stream, j->grid_ev, 0));  // the last grid update
   CU(cudaEventRecord(s.ev0, s.stream));
   if (c.use_graph && !c.profile) {
-    if (!s.graph) {
+    const int form = j->shade_split == 0 ? 0 : 1;
+    const bool both = split_setting < 0 && c.mode == 1;  // the job may switch forms later
+    for (int f = 0; f < 2; ++f) {
+      if (s.graphs[f] || (f != form && !both)) continue;
+      const int keep = j->shade_split;
+      j->shade_split = f;
       cudaGraph_t g;
       CU(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
       int r = enqueue_frame(j, s);
       cudaError_t e = cudaStreamEndCapture(s.stream, &g);
+      j->shade_split = keep;
       if (r) return r;
       if (e != cudaSuccess) return fail(MT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-      e = cudaGraphInstantiate(&s.graph, g, 0);
+      e = cudaGraphInstantiate(&s.graphs[f], g, 0);
       cudaGraphDestroy(g);
       if (e != cudaSuccess) return fail(MT_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
     }
-    CU(cudaGraphLaunch(s.graph, s.stream));
+    CU(cudaGraphLaunch(s.graphs[form], s.stream));
   } else {
     int r = enqueue_frame(j, s);
     if (r) return r;
   }
+  s.ran = true;
   CU(cudaEventRecord(s.ev1, s.stream));
   if (accumulate) {
     // CAdaptiveEnvironment.update (CAdaptiveEnvironment.java:128-137): func = accum,

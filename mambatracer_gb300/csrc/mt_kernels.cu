@@ -416,6 +416,34 @@ __device__ __forceinline__ void shade_continue(const DevScene& S, const DevEnv& 
   fb.flag[P.pixel] = 0;
 }
 
+// Benchmark semantics: a warp appends its survivors to the next queue and its
+// shadow rays to the shadow queue, one atomic per queue (ranks by ballot).
+__device__ __forceinline__ void append_warp(Ctrl* ctrl, int b, const FrameBufs& fb, const PathState& P,
+                                            const ShadeOut& R) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int nq = b & 1;  // queue written for bounce b + 1
+  const unsigned am = __ballot_sync(0xffffffffu, P.alive), sm = __ballot_sync(0xffffffffu, R.has_shadow);
+  int qa = 0, qs = 0;
+  if (lane == 0) {
+    if (am) qa = atomicAdd(&ctrl->count[b + 1], __popc(am));
+    if (sm) qs = atomicAdd(&ctrl->shadow[b], __popc(sm));
+  }
+  qa = __shfl_sync(0xffffffffu, qa, 0);
+  qs = __shfl_sync(0xffffffffu, qs, 0);
+  if (P.alive) {
+    const int slot = qa + __popc(am & lt);
+    fb.q_o[nq][slot] = mk(P.H.p.x, P.H.p.y, P.H.p.z, __int_as_float(P.pixel));
+    fb.q_d[nq][slot] = mk(R.ndir.x, R.ndir.y, R.ndir.z, 0.f);
+  }
+  if (R.has_shadow) {
+    const int sslot = qs + __popc(sm & lt);
+    fb.s_o[sslot] = R.sho;
+    fb.s_d[sslot] = R.shd;
+    fb.s_c[sslot] = R.shc;
+  }
+}
+
 // Reference semantics (mode 0), one 256-path tile per block: survivors are
 // compacted in order (block scan + decoupled look-back) between the two phases,
 // and the light and BSDF samples of a survivor are keyed on its compacted slot
@@ -544,8 +572,6 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade_cont(DevScene S, 
                                                               FrameBufs fb) {
   const int count = ctrl->live[b];
   const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
-  const int nq = b & 1;  // queue written for bounce b + 1
   for (;;) {
     int chunk = 0;
     if (lane == 0) chunk = atomicAdd(&ctrl->tiles2[b], 1);
@@ -560,25 +586,7 @@ __global__ void __launch_bounds__(kShadeThreads, MINB) k_shade_cont(DevScene S, 
       shade_load(S, res, b, fb, __ldg(fb.live + k), P);
       shade_continue<1, TEX, LEAN>(S, E, b, fb, pixel_gid(P.local), P, R);
     }
-    const unsigned am = __ballot_sync(0xffffffffu, P.alive), sm = __ballot_sync(0xffffffffu, R.has_shadow);
-    int qa = 0, qs = 0;
-    if (lane == 0) {
-      if (am) qa = atomicAdd(&ctrl->count[b + 1], __popc(am));
-      if (sm) qs = atomicAdd(&ctrl->shadow[b], __popc(sm));
-    }
-    qa = __shfl_sync(0xffffffffu, qa, 0);
-    qs = __shfl_sync(0xffffffffu, qs, 0);
-    if (P.alive) {
-      const int slot = qa + __popc(am & lt);
-      fb.q_o[nq][slot] = mk(P.H.p.x, P.H.p.y, P.H.p.z, __int_as_float(P.pixel));
-      fb.q_d[nq][slot] = mk(R.ndir.x, R.ndir.y, R.ndir.z, 0.f);
-    }
-    if (R.has_shadow) {
-      const int sslot = qs + __popc(sm & lt);
-      fb.s_o[sslot] = R.sho;
-      fb.s_d[sslot] = R.shd;
-      fb.s_c[sslot] = R.shc;
-    }
+    append_warp(ctrl, b, fb, P, R);
   }
 }
 
@@ -624,10 +632,18 @@ int env_shade_minb() {
   int x = e ? std::atoi(e) : kShadeMinBlocks;
   return (x == 3 || x == 4 || x == 5) ? x : kShadeMinBlocks;
 }
-bool shade_split() {
-  static const bool on = !(std::getenv("MT_SHADE_SPLIT") && std::atoi(std::getenv("MT_SHADE_SPLIT")) == 0);
-  return on;
+// MT_SHADE_SPLIT: unset, render jobs choose one or two shading launches frame by
+// frame (shade_split_for) and other passes take two; 0 always one; 1 always two.
+int shade_split_mode() {
+  static const int m = [] {
+    const char* e = std::getenv("MT_SHADE_SPLIT");
+    if (!e) return -1;
+    return std::atoi(e) == 0 ? 0 : 1;
+  }();
+  return m;
 }
+bool shade_split() { return shade_split_mode() != 0; }
+
 int env_steps() {
   const char* e = std::getenv("MT_REFILL_STEPS");
   int x = e ? std::atoi(e) : kSteps;
@@ -701,6 +717,19 @@ void launch_traces(cudaStream_t st, int grid, const DevScene& S, Ctrl* ctrl, int
 
 Tuning get_tuning() { return tuning_ref(); }
 
+int shade_split_setting() { return shade_split_mode(); }
+
+// Measured with six frames in flight: the 1M soup (53 % of bounce-1 paths go
+// on) 915 Mrays/s in two launches against 861 in one; the stadium (71 % go on)
+// 2588 against 2743. A band around the crossover keeps the current choice.
+int shade_split_for(int queued, int went_on, int current) {
+  if (queued <= 0) return current;
+  const double f = (double)went_on / queued;
+  if (f < 0.58) return 1;
+  if (f > 0.66) return 0;
+  return current;
+}
+
 bool set_tuning(const Tuning& t) {
   auto minb_ok = [](int x) { return x == 8 || x == 12 || x == 16; };
   if (!minb_ok(t.closest_minb) || !minb_ok(t.shadow_minb) || t.closest_grid < 0 || t.closest_grid > 32 ||
@@ -736,7 +765,8 @@ void launch_trace(cudaStream_t st, const DevScene& S, Ctrl* ctrl, int b, int mod
 int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassParams* d_pp, int mode, int max_depth,
                 int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb, unsigned long long* status,
                 size_t status_stride, int num_sms, cudaEvent_t* ev, unsigned long long* totals, bool shared,
-                cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+                cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int shade_split_req) {
+  const bool two_launches = shade_split_req < 0 ? shade_split() : shade_split_req != 0;
   const int N = width * height;
   static int shade_bps[6] = {};
   // shadow rays of bounce b beside the extension rays of bounce b + 1 (no
@@ -764,7 +794,7 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
         k_shade_ref<3, true><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
       else
         k_shade_ref<3><<<tiles, kShadeThreads, 0, st>>>(S, E, d_pp, ctrl, b, fb, stb);
-    } else if (shade_split()) {
+    } else if (two_launches) {
       const int sm = shade_minb();
       if (shade_bps[sm] == 0) shade_bps[sm] = shade_blocks_per_sm(sm);
       const int sgrid = std::max(1, std::min(num_sms * shade_bps[sm], tiles));

@@ -57,7 +57,16 @@ int launch_pass(cudaStream_t st, const DevScene& S, const DevEnv& E, const PassP
                 int max_depth, int kahan, int width, int height, Ctrl* ctrl, FrameBufs fb,
                 unsigned long long* status, size_t status_stride, int num_sms, cudaEvent_t* events,
                 unsigned long long* totals, bool shared = false, cudaStream_t side = nullptr,
-                cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
+                cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr, int shade_split = -1);
+// The process's benchmark-semantics shading setting (MT_SHADE_SPLIT): -1 render
+// jobs choose per frame (shade_split_for) and other passes run two launches; 0
+// always one launch; 1 always two.
+int shade_split_setting();
+// Whether shading in two launches pays for a frame whose bounce-1 queue of
+// `queued` paths left `went_on` going on (two launches pay when many paths end at
+// their first hit: their lanes would idle through the light and BSDF samples);
+// current: the choice so far, kept near the crossover.
+int shade_split_for(int queued, int went_on, int current);
 
 // Closest or any hit of reference-layout rays with the traversal work per ray
 // (interior-node visits, triangle tests), one ray per thread.
