@@ -127,20 +127,31 @@ struct StackEntry<true> {
 // A record's two child boxes as n0 = (L.lo.x, L.hi.x, L.lo.y, L.hi.y),
 // n1 = the same for R, n2 = (L.lo.z, L.hi.z, R.lo.z, R.hi.z), and its child refs.
 // FP16 records: q0 = half2 pairs (L x, L y, R x, R y), q1 = (L z, R z, left, right).
+// 32 bytes in one 256-bit read-only load (records are 32-byte aligned: the
+// arrays start on 256-byte boundaries and records are 32 or 64 bytes).
+__device__ __forceinline__ void ldg32(const void* p, uint4& a, uint4& b) {
+  asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
+      : "l"(p));
+}
+
 template <int PREC>
 __device__ __forceinline__ void load_record(const DevScene& S, int ref, float4& n0, float4& n1, float4& n2, int& left,
                                             int& right) {
   if constexpr (PREC == 0) {
     const float4* p = S.nodes + 4 * (size_t)ref;
-    n0 = __ldg(p + 0);
-    n1 = __ldg(p + 1);
-    n2 = __ldg(p + 2);
-    const float4 n3 = __ldg(p + 3);
-    left = __float_as_int(n3.x);
-    right = __float_as_int(n3.y);
+    uint4 a, b, c, d;
+    ldg32(p, a, b);
+    ldg32(p + 2, c, d);
+    n0 = make_float4(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(a.w));
+    n1 = make_float4(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z), __uint_as_float(b.w));
+    n2 = make_float4(__uint_as_float(c.x), __uint_as_float(c.y), __uint_as_float(c.z), __uint_as_float(c.w));
+    left = (int)d.x;
+    right = (int)d.y;
   } else {
     const uint4* p = reinterpret_cast<const uint4*>(S.qnodes) + 2 * (size_t)ref;
-    const uint4 q0 = __ldg(p + 0), q1 = __ldg(p + 1);
+    uint4 q0, q1;
+    ldg32(p, q0, q1);
     auto h2 = [](unsigned u) { return __half22float2(*reinterpret_cast<const __half2*>(&u)); };
     const float2 lx = h2(q0.x), ly = h2(q0.y), rx = h2(q0.z), ry = h2(q0.w), lz = h2(q1.x), rz = h2(q1.y);
     n0 = make_float4(lx.x, lx.y, ly.x, ly.y);
