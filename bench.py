@@ -66,7 +66,7 @@ WORKLOAD = WORKLOADS["soup"]["name"]
 # traversal formats (mt_scene_set_bvh_precision)
 RECORDS = {0: "FP32 child boxes, binary, 64 B records",
            1: "FP16 child boxes rounded outward, binary, 32 B records",
-           2: "wide BVH: up to 8 children with 8-bit child boxes rounded outward, 80 B nodes"}
+           2: "wide BVH: up to 8 children with 8-bit child boxes rounded outward, 96 B nodes"}
 
 
 def make_scene(kind, small, width, height):
@@ -534,8 +534,8 @@ def run_gpu(args):
             prays = check.primary_rays(orc, cam, width, height, frame_no(1))
             _, _, cnt = S.trace_counts(prays)
             v_int, tri = float(cnt[:, 0].mean()), float(cnt[:, 1].mean())
-            alg_bytes = int(width * height * 48 + 80 * int(cnt[:, 0].sum()) + 48 * int(cnt[:, 1].sum()))
-            visit_src = "wide-BVH node visits (80 B) counted on the device (mt_trace_counts)"
+            alg_bytes = int(width * height * 48 + 96 * int(cnt[:, 0].sum()) + 48 * int(cnt[:, 1].sum()))
+            visit_src = "wide-BVH node visits (96 B) counted on the device (mt_trace_counts)"
         else:
             alg_bytes, v_int, tri = algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_no(1),
                                                       threads, rec_bytes=32 if args.precision == 1 else 64)
@@ -964,7 +964,7 @@ def main():
     ap.add_argument("--inflight", type=int, default=6, help="frames kept in flight on separate streams (1..8)")
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
                     help="traversal format: 0 FP32 child boxes (64 B records), 1 FP16 outward-rounded (32 B, the "
-                         "default: the same hits, fastest), 2 wide BVH with 8-bit outward-rounded child boxes (80 B "
+                         "default: the same hits, fastest), 2 wide BVH with 8-bit outward-rounded child boxes (96 B "
                          "nodes)")
     ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS) + ["batched", "served", "plain"])
     ap.add_argument("--lanes", type=int, default=8, help="batched/served: requests in flight, a stream each")

@@ -11,6 +11,7 @@ namespace mt {
 constexpr int kMaxDepth = 32;        // bounces per pass (reference: 15)
 constexpr int kStackDepth = 64;      // traversal stack = the reference's 64-bit bitstack
 constexpr int kWideStack = 32;       // wide-BVH traversal: node groups deferred (<= wide tree depth)
+constexpr int kWideWords = 6;        // uint4 per wide-BVH node: 80 bytes used, padded to 96 (three 32-byte loads)
 constexpr int kTraceThreads = 128;   // threads per traversal CTA
 constexpr int kTraceMinBlocksClosest = 12;  // register bounds of the traversal kernels (CTAs per SM)
 constexpr int kTraceMinBlocksShadow = 8;
@@ -45,7 +46,8 @@ static_assert(sizeof(Material) == 144, "Material layout");
 //     (p2 - p1, 0), (p3 - p1, 0), the edges of the reference's Moller-Trumbore.
 //   qnodes: FP16 child boxes rounded outward (precision 1), 2 x 16 B per record:
 //     (L.x, L.y, R.x, R.y) as (lo, hi) half2 pairs, then (L.z, R.z, left ref, right ref).
-//   wnodes: the wide BVH (precision 2), 5 uint4 = 80 B per node, root 0:
+//   wnodes: the wide BVH (precision 2), kWideWords uint4 = 96 B per node (the
+//     last 16 B unused, so that a node is three aligned 32-byte loads), root 0:
 //     w0 = (origin x, y, z as float bits, ex | ey << 8 | ez << 16 | imask << 24):
 //          per-axis scale 2^(e - 127), imask bit s = slot s holds an interior node
 //     w1 = (first child node, first triangle, lmask, 0): lmask bit s = slot s holds

@@ -242,7 +242,7 @@ __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref,
 // boxes are quantised to 8 bits per plane against the node's FP32 origin and a
 // power-of-two scale per axis, rounded outward (Ylitie, Karras, Laine,
 // "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs",
-// HPG 2017). A node is 80 bytes (see DevScene::wnodes); leaves stay single
+// HPG 2017). A node is 80 bytes, padded to 96 (see DevScene::wnodes); leaves stay single
 // triangles tested by the same FP32 Moller-Trumbore as above, so a hit is the
 // same triangle at the same distance: a quantised box contains the child's
 // FP32 box, so every triangle the binary traversal reaches is reached here.
@@ -307,8 +307,11 @@ __device__ __forceinline__ unsigned xor_permute8(unsigned m, unsigned x) {
 // Intersects the ray with a wide node's eight child boxes; sets the next node
 // and triangle groups from the children hit.
 __device__ __forceinline__ void wide_node(const DevScene& S, const RayT& r, WideState& w, unsigned node) {
-  const uint4* p = S.wnodes + 5 * (size_t)node;
-  const uint4 w0 = __ldg(p + 0), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
+  const uint4* p = S.wnodes + kWideWords * (size_t)node;
+  uint4 w0, w1, w2, w3, w4, w5;
+  ldg32(p, w0, w1);
+  ldg32(p + 2, w2, w3);
+  ldg32(p + 4, w4, w5);
   const unsigned imask = w0.w >> 24, lmask = w1.z & 0xFFu;
   const float ax = __uint_as_float((w0.w & 0xFFu) << 23) * w.jx;
   const float ay = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23) * w.jy;

@@ -41,7 +41,7 @@ struct WChild {
 struct WideBuilder {
   const float4* rec = nullptr;
   const float4* tris = nullptr;
-  std::vector<uint4> nodes;  // 5 per node
+  std::vector<uint4> nodes;  // kWideWords per node
   std::vector<float4> wt;    // 3 per triangle entry
   int max_depth = 0;
   bool bad = false;
@@ -171,8 +171,8 @@ struct WideBuilder {
         lmask |= 1u << s;
       }
     }
-    const unsigned child_base = (unsigned)(nodes.size() / 5);
-    nodes.resize(nodes.size() + 5 * (size_t)ninner);
+    const unsigned child_base = (unsigned)(nodes.size() / kWideWords);
+    nodes.resize(nodes.size() + kWideWords * (size_t)ninner, make_uint4(0u, 0u, 0u, 0u));
     const unsigned tri_base = (unsigned)(wt.size() / 3);
     for (int s = 0; s < 8; ++s) {  // leaf slot s holds triangle tri_base + (leaf slots below s)
       const int i = child_in[s];
@@ -185,7 +185,7 @@ struct WideBuilder {
     auto word = [](const unsigned char* b) {
       return (unsigned)b[0] | ((unsigned)b[1] << 8) | ((unsigned)b[2] << 16) | ((unsigned)b[3] << 24);
     };
-    uint4* o = nodes.data() + 5 * (size_t)w;
+    uint4* o = nodes.data() + kWideWords * (size_t)w;
     unsigned px, py, pz;
     std::memcpy(&px, &org[0], 4);
     std::memcpy(&py, &org[1], 4);
@@ -226,9 +226,9 @@ int refresh_wide(mt_scene* s) {
   b.rec = rec.data();
   b.tris = tris.data();
 
-  b.nodes.reserve(5 * (size_t)(s->ntri / 3 + 8));
+  b.nodes.reserve(kWideWords * (size_t)(s->ntri / 3 + 8));
   b.wt.reserve(3 * (size_t)s->ntri);
-  b.nodes.resize(5);
+  b.nodes.resize(kWideWords, make_uint4(0u, 0u, 0u, 0u));
   if (s->root_ref >= 0) {
     WChild c[8];
     b.children_of(s->root_ref, c);
@@ -259,7 +259,7 @@ int refresh_wide(mt_scene* s) {
   if (r) return r;
   CU(cudaMemcpy(s->d_wnodes, b.nodes.data(), b.nodes.size() * sizeof(uint4), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(s->d_wtris, b.wt.data(), b.wt.size() * sizeof(float4), cudaMemcpyHostToDevice));
-  s->nwide = (int)(b.nodes.size() / 5);
+  s->nwide = (int)(b.nodes.size() / kWideWords);
   s->wdepth = b.max_depth + 1;
   return MT_OK;
 }
