@@ -323,7 +323,7 @@ int mt_trace_any(mt_scene* scene, const void* rays, int n, int32_t* occluded_out
  * 2 ints per ray, interior-node visits and triangle tests, in the scene's
  * record format (FP32 or FP16 binary records: the visits of the reference's
  * stackless traversal, src/cl/kernel/NormalBVH.cl:14-92; the wide BVH: its
- * 80-byte node visits). any != 0: any-hit (t_out unused, prim_out = occluded
+ * 96-byte node visits). any != 0: any-hit (t_out unused, prim_out = occluded
  * flags). No reference counterpart: it measures the algorithm's memory work
  * (the roofline's algorithmic bytes). */
 int mt_trace_counts(mt_scene* scene, const void* rays, int n, int any, float* t_out, int32_t* prim_out,

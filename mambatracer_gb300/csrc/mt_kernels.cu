@@ -679,7 +679,7 @@ int trace_blocks_per_sm() {
   return n > 0 ? n : 1;
 }
 // The wide-BVH kernels are built for 8 resident blocks per SM whatever the
-// tuning's bound (at 12 or 16 their 80-byte node tests spill registers), and
+// tuning's bound (at 12 or 16 their wide node tests spill registers), and
 // refill after an eighth of the binary kernels' steps (a wide step tests eight
 // child boxes; measured on the 1M soup at 1080p, refill every 4, 8, 12, 16, 32,
 // 64 wide steps: bounce-1 closest hits 1.73, 1.76, 1.81, 1.86, 2.02, 2.21 ms).
@@ -930,7 +930,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_query(DevScene S, const fl
 // Traversal work per ray: the same traversal as k_query, one step at a time,
 // counting interior-node visits and triangle tests (counts[2 i], counts[2 i + 1]).
 // Binary records: the visits the reference's algorithm makes (a step is one or
-// the other, classified before it runs); the wide BVH: its 80-byte node visits.
+// the other, classified before it runs); the wide BVH: its node visits (96-byte nodes).
 template <int PREC, bool ANY>
 __global__ void __launch_bounds__(kTraceThreads) k_count(DevScene S, const float4* __restrict__ rays, int n,
                                                          float* __restrict__ t_out, int* __restrict__ prim_out,

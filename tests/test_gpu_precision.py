@@ -7,7 +7,7 @@
    at exactly the same distance is kept, when the changed visit order meets them
    the other way round.
 2. The wide BVH: the same tree collapsed into nodes of up to eight children with
-   8-bit child boxes rounded outward (80-byte nodes). Its boxes contain the FP32
+   8-bit child boxes rounded outward (96-byte nodes). Its boxes contain the FP32
    boxes, and its triangle test is the same FP32 Moller-Trumbore, so any-hit
    answers are the same and so is every closest hit, except where two triangles
    are hit within a few ulps of each other (coplanar surfaces: the box room's
