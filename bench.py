@@ -66,7 +66,8 @@ WORKLOAD = WORKLOADS["soup"]["name"]
 # traversal formats (mt_scene_set_bvh_precision)
 RECORDS = {0: "FP32 child boxes, binary, 64 B records",
            1: "FP16 child boxes rounded outward, binary, 32 B records",
-           2: "wide BVH: up to 8 children with 8-bit child boxes rounded outward, 96 B nodes"}
+           2: "wide BVH: up to 8 children with 8-bit child boxes rounded outward, 96 B nodes",
+           3: "4-wide: a record's grandchildren with FP16 boxes rounded outward, 64 B nodes"}
 
 
 def make_scene(kind, small, width, height):
@@ -318,7 +319,7 @@ def bench_scene(ctx, kind, small, width, height, precision):
     nodes, bounds = S.build_bvh_device()  # CNormalBVH.build's tree, built level by level on the GPU
     bvh_build_ms = (time.perf_counter() - t_bvh) * 1e3
     if precision:
-        S.set_precision(precision)  # 1: FP16 child boxes, 32-byte records; 2: wide BVH, 8-bit child boxes
+        S.set_precision(precision)  # 1: FP16 records; 2: wide BVH, 8-bit boxes; 3: 4-wide, FP16 boxes
     if ENV_ON:
         S.set_env(env, ENV_W, ENV_H)
         S.grid_config(*GRID, enable=2)  # grid-guided environment sampling, FP64 per-cell SATs
@@ -449,10 +450,12 @@ def run_gpu(args):
     ctx.finish()
     clocks = ClockSampler(local)
     clocks.start()
+    launches0 = job.launches()
     ctx.record(0)
     for i in range(args.steps):
         job.render(None, frame_no(args.warmup + i))
     ctx.record(1)
+    gpu_launches = job.launches() - launches0
     ctx.finish()
     barrier()
     ms = ctx.elapsed_ms(0, 1)
@@ -527,15 +530,17 @@ def run_gpu(args):
         orc = Oracle()
         threads = os.cpu_count() or 1
         t_alg = time.perf_counter()
-        if args.precision == 2:
-            # the wide BVH has no oracle traversal: its node visits are counted on
-            # the device by the same traversal one ray per thread (mt_trace_counts)
+        if args.precision in (2, 3):
+            # the wide formats have no oracle traversal: their node visits are counted
+            # on the device by the same traversal one ray per thread (mt_trace_counts)
             from oracle import check
             prays = check.primary_rays(orc, cam, width, height, frame_no(1))
             _, _, cnt = S.trace_counts(prays)
             v_int, tri = float(cnt[:, 0].mean()), float(cnt[:, 1].mean())
-            alg_bytes = int(width * height * 48 + 96 * int(cnt[:, 0].sum()) + 48 * int(cnt[:, 1].sum()))
-            visit_src = "wide-BVH node visits (96 B) counted on the device (mt_trace_counts)"
+            nb = 96 if args.precision == 2 else 64
+            alg_bytes = int(width * height * 48 + nb * int(cnt[:, 0].sum()) + 48 * int(cnt[:, 1].sum()))
+            visit_src = (f"{'wide-BVH' if args.precision == 2 else '4-wide'} node visits ({nb} B) counted on the "
+                         "device (mt_trace_counts)")
         else:
             alg_bytes, v_int, tri = algorithmic_bytes(orc, sc, nodes, bounds, cam, width, height, frame_no(1),
                                                       threads, rec_bytes=32 if args.precision == 1 else 64)
@@ -552,8 +557,11 @@ def run_gpu(args):
         traffic, traffic_src = None, None
         kp = os.path.join(ROOT, "profiles", "kernels_soup1M_1080p.json")
         kprof = None
-        if not args.small and args.workload == "soup" and args.precision == 1 and os.path.exists(kp):
+        if not args.small and args.workload == "soup" and os.path.exists(kp):
             kprof = json.load(open(kp))
+            if kprof.get("precision") != args.precision:
+                kprof = None  # captured with another traversal format
+        if kprof is not None:
             traffic = kprof["kernels"]["k_trace_closest"]["dram_bytes"]
             traffic_src = "profiles/kernels_soup1M_1080p.json (" + kprof["source"] + ")"
         achieved = alg_bytes / (t_b1 * 1e-3) / 1e9
@@ -594,7 +602,7 @@ def run_gpu(args):
             "config": config_dict(args.workload, width, height, ntri, world, args.inflight, args.small),
             "rays_per_step": round(total_rays / args.steps / world), "rays_split": rays.tolist(),
             "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e,
-            "gpu_launches": args.steps * (spp * (2 + 3 * DEPTH) + (1 if args.inflight > 1 else 0)), "clocks": clk,
+            "gpu_launches": gpu_launches, "clocks": clk,
             "inflight_frames": args.inflight,
             "msamples_per_s": round(width * height * spp * args.steps * world / (ms * 1e-3) / 1e6, 2),
             "bvh_depth": S.depth, "bvh_build_ms": round(bvh_build_ms, 2), "bvh_build": "GPU, level-synchronous",
@@ -962,10 +970,11 @@ def main():
     ap.add_argument("--no-check", action="store_true", help="skip the image-error check against the oracle")
     ap.add_argument("--no-arms", action="store_true", help="skip the batched and plain-wavefront arms")
     ap.add_argument("--inflight", type=int, default=6, help="frames kept in flight on separate streams (1..8)")
-    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
-                    help="traversal format: 0 FP32 child boxes (64 B records), 1 FP16 outward-rounded (32 B, the "
-                         "default: the same hits, fastest), 2 wide BVH with 8-bit outward-rounded child boxes (96 B "
-                         "nodes)")
+    ap.add_argument("--precision", type=int, default=3, choices=[0, 1, 2, 3],
+                    help="traversal format: 0 FP32 child boxes (64 B records), 1 FP16 outward-rounded (32 B), 2 wide "
+                         "BVH with 8-bit outward-rounded child boxes (96 B nodes), 3 4-wide nodes of a record's "
+                         "grandchildren with FP16 outward-rounded boxes (64 B, the default: the same hits up to "
+                         "exact-distance ties, fastest)")
     ap.add_argument("--workload", default="soup", choices=sorted(WORKLOADS) + ["batched", "served", "plain"])
     ap.add_argument("--lanes", type=int, default=8, help="batched/served: requests in flight, a stream each")
     ap.add_argument("--merged-lanes", type=int, default=None,

@@ -133,12 +133,17 @@ int mt_bvh_build_device(mt_scene* scene, int32_t* nodes_out, float* bounds_out, 
 int mt_scene_layout_read(mt_scene* scene, void* records_out, void* tris_out, int* nrec_out, int* root_ref_out);
 /* Use a BVH built elsewhere (the Java builder's nodes/bounds buffers). */
 int mt_bvh_import(mt_scene* scene, const int32_t* nodes, const float* bounds, int nnodes);
-/* Traversal record format: 0 = FP32 child boxes (default, 64-byte records),
- * 1 = FP16 child boxes rounded outward (32-byte records, kept beside the FP32
- * ones and rebuilt with every BVH build or import). Outward rounding keeps every
- * node the FP32 traversal enters, so closest hits are the same triangles at the
- * same distances; only which of two triangles hit at exactly the same distance
- * is reported can change with the visit order. */
+/* Traversal format: 0 = FP32 child boxes (default, 64-byte records, the
+ * reference's visit order); 1 = FP16 child boxes rounded outward (32-byte
+ * records); 2 = a wide BVH of up to eight children with 8-bit boxes rounded
+ * outward (96-byte nodes); 3 = 4-wide nodes holding a record's grandchildren with
+ * FP16 boxes rounded outward (64-byte nodes, leaves tested in warp-wide batches).
+ * Formats 1-3 are kept beside the FP32 records and rebuilt with every BVH build
+ * or import. Outward-rounded boxes contain the FP32 boxes, so closest hits are
+ * the same triangles at the same distances; only which of two triangles hit at
+ * exactly the same distance is reported can change with the visit order (and
+ * for 2 and 3, of coplanar triangles hit within a few ulps the nearer is kept).
+ * Any-hit answers are the same in every format. */
 int mt_scene_set_bvh_precision(mt_scene* scene, int precision);
 /* Replace the material table (TracerAPI material edits, src/cl/ui/fx/main/TracerAPI.java:371). */
 int mt_scene_set_materials(mt_scene* scene, const void* materials, int nmaterials);
@@ -249,6 +254,11 @@ int mt_job_stats(mt_job* job, int64_t* rays3, int32_t* counts);
 int mt_job_total_rays(mt_job* job, int64_t* rays3);
 /* Device time of the last mt_render_frame, in ms (CUDA events on the job's stream). */
 int mt_job_last_ms(mt_job* job, float* ms);
+/* Kernels the job's frames have launched (graph nodes included): per pass the
+ * ray generation, per bounce the closest-hit traversal, shading (one launch or
+ * two) and the shadow rays, and the ray totals; per frame the film merge of
+ * jobs with frames in flight. Light-grid updates are not counted. */
+int mt_job_launches(mt_job* job, int64_t* n);
 /* Profiled jobs: device time of each launch of the last frame, in ms, pass by
  * pass: [raygen, then per bounce trace_closest, shade, trace_shadow] =
  * spp * (1 + 3 * max_depth) floats. */

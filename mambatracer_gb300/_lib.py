@@ -121,6 +121,7 @@ SIGNATURES = {
     "mt_film_clear": (I, [P]),
     "mt_job_stats": (I, [P, P, P]),
     "mt_job_last_ms": (I, [P, C.POINTER(C.c_float)]),
+    "mt_job_launches": (I, [P, C.POINTER(C.c_int64)]),
     "mt_job_kernel_ms": (I, [P, P]),
     "mt_job_total_rays": (I, [P, P]),
     "mt_ctx_event_record": (I, [P, I]),

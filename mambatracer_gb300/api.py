@@ -258,6 +258,12 @@ class Job:
         check(lib().mt_job_last_ms(self.h, C.byref(ms)))
         return ms.value
 
+    def launches(self) -> int:
+        """Kernels the job's frames have launched (mt_job_launches)."""
+        n = C.c_int64()
+        check(lib().mt_job_launches(self.h, C.byref(n)))
+        return n.value
+
     def kernel_ms(self) -> np.ndarray:
         """Per-launch device times of the last frame (profiled jobs): spp x (1 + 3 * max_depth)."""
         out = np.zeros(self.cfg.spp * (1 + 3 * self.cfg.max_depth), np.float32)

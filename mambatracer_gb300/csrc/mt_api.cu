@@ -259,6 +259,7 @@ void free_scene(mt_scene* s) {
   dfree(s->d_qnodes);
   dfree(s->d_wnodes);
   dfree(s->d_wtris);
+  dfree(s->d_quad);
   dfree(s->d_env_rgb);
   dfree(s->d_env_lum);
   dfree(s->d_env_sat);
@@ -701,8 +702,8 @@ extern "C" int mt_bvh_import(mt_scene* s, const int32_t* nodes, const float* bou
 
 extern "C" int mt_scene_set_bvh_precision(mt_scene* s, int precision) {
   if (!s) return fail(MT_ERR_INVALID, "NULL scene");
-  if (precision < 0 || precision > 2)
-    return fail(MT_ERR_INVALID, "BVH precision %d (0 FP32, 1 FP16, 2 wide 8-bit)", precision);
+  if (precision < 0 || precision > 3)
+    return fail(MT_ERR_INVALID, "BVH precision %d (0 FP32, 1 FP16, 2 wide 8-bit, 3 4-wide FP16)", precision);
   std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CU(cudaSetDevice(s->ctx->device));
   int q = quiesce(s->ctx);

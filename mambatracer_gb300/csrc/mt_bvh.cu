@@ -373,6 +373,58 @@ __global__ void k_quantize_fp16(const float4* __restrict__ recs, int nrec, uint4
   q[2 * (size_t)i + 1] = make_uint4(pair(n2.x, n2.y), pair(n2.z, n2.w), __float_as_uint(n3.x), __float_as_uint(n3.y));
 }
 
+// 4-wide FP16 nodes from FP32 records: node r holds, for each child of record r,
+// that child's two children when it is interior, else the child (a leaf), with
+// the same outward rounding as the FP16 records.
+__global__ void k_quad_fp16(const float4* __restrict__ recs, int nrec, uint4* q) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrec) return;
+  auto pair = [](float lo, float hi) {
+    __half2 h = __halves2half2(__float2half_rd(lo), __float2half_ru(hi));
+    return *reinterpret_cast<unsigned*>(&h);
+  };
+  // a record's children: boxes (lo/hi per axis) and refs
+  auto kids = [&](int r, float box[2][6], int ref[2]) {
+    const float4* p = recs + 4 * (size_t)r;
+    const float4 n0 = p[0], n1 = p[1], n2 = p[2], n3 = p[3];
+    const float b[2][6] = {{n0.x, n0.y, n0.z, n0.w, n2.x, n2.y}, {n1.x, n1.y, n1.z, n1.w, n2.z, n2.w}};
+    for (int c = 0; c < 2; ++c)
+      for (int k = 0; k < 6; ++k) box[c][k] = b[c][k];
+    ref[0] = __float_as_int(n3.x);
+    ref[1] = __float_as_int(n3.y);
+  };
+  float box[2][6];
+  int ref[2];
+  kids(i, box, ref);
+  unsigned w[16];
+  int n = 0;
+  const unsigned empty_box = pair(INFINITY, -INFINITY);
+  for (int c = 0; c < 2; ++c) {
+    if (ref[c] >= 0) {
+      float gb[2][6];
+      int gr[2];
+      kids(ref[c], gb, gr);
+      for (int g = 0; g < 2; ++g, ++n) {
+        for (int a = 0; a < 3; ++a) w[3 * n + a] = pair(gb[g][2 * a], gb[g][2 * a + 1]);
+        w[12 + n] = (unsigned)gr[g];
+      }
+    } else {
+      for (int a = 0; a < 3; ++a) w[3 * n + a] = pair(box[c][2 * a], box[c][2 * a + 1]);
+      w[12 + n] = (unsigned)ref[c];
+      ++n;
+    }
+  }
+  for (; n < 4; ++n) {
+    for (int a = 0; a < 3; ++a) w[3 * n + a] = empty_box;
+    w[12 + n] = (unsigned)kQuadEmpty;
+  }
+  uint4* o = q + 4 * (size_t)i;
+  o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+  o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+  o[2] = make_uint4(w[8], w[9], w[10], w[11]);
+  o[3] = make_uint4(w[12], w[13], w[14], w[15]);
+}
+
 __global__ void k_seed(Seg* segs, int n) {
   if (blockIdx.x == 0 && threadIdx.x == 0) segs[0] = Seg{0, 0, n, 1, 0, -1, 0, 0};
 }
@@ -511,7 +563,19 @@ extern "C" int mt_bvh_build_device(mt_scene* s, int32_t* nodes_out, float* bound
 
 int refresh_qnodes(mt_scene* s) {
   dfree(s->d_qnodes);
+  dfree(s->d_quad);
   if (int w = refresh_wide(s)) return w;
+  if (s->precision == 3 && s->has_bvh && s->nrec > 0) {
+    int r = dalloc(&s->d_quad, 4 * (size_t)s->nrec);
+    if (r) return r;
+    cudaStream_t st = s->ctx->stream;
+    k_quad_fp16<<<blocks(s->nrec), kT, 0, st>>>(s->d_nodes, s->nrec, s->d_quad);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+      dfree(s->d_quad);
+      return fail(MT_ERR_CUDA, "4-wide FP16 nodes: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    return MT_OK;
+  }
   if (s->precision != 1 || !s->has_bvh || s->nrec == 0) return MT_OK;
   int r = dalloc(&s->d_qnodes, 2 * (size_t)s->nrec);
   if (r) return r;

@@ -11,6 +11,10 @@ namespace mt {
 constexpr int kMaxDepth = 32;        // bounces per pass (reference: 15)
 constexpr int kStackDepth = 64;      // traversal stack = the reference's 64-bit bitstack
 constexpr int kWideStack = 32;       // wide-BVH traversal: node groups deferred (<= wide tree depth)
+constexpr int kQuadEmpty = (int)0x80000000;  // an unused child slot of a 4-wide node
+// 4-wide traversal stack: a 4-wide node spans two binary levels and defers at
+// most three children, so a tree within the 64-level bound needs 3 * 32 entries.
+constexpr int kQuadStack = 3 * (kStackDepth / 2);
 constexpr int kWideWords = 6;        // uint4 per wide-BVH node: 80 bytes used, padded to 96 (three 32-byte loads)
 constexpr int kTraceThreads = 128;   // threads per traversal CTA
 constexpr int kTraceMinBlocksClosest = 12;  // register bounds of the traversal kernels (CTAs per SM)
@@ -58,16 +62,23 @@ static_assert(sizeof(Material) == 144, "Material layout");
 //     w4 = (hi.y .., hi.z ..): one quantised plane per byte, plane = origin + q 2^(e-127);
 //          an empty slot holds lo = 255, hi = 0 (never hit)
 //   wtris: the triangles in wide-leaf order, 3 float4 each as in tris.
+//   quad: 4-wide FP16 nodes (precision 3), 4 uint4 = 64 B, indexed like nodes: the
+//     node of record r holds the grandchildren of r where a child of r is
+//     interior and the child itself where it is a leaf, in the order left's
+//     children, right's children; words 3c .. 3c + 2 = child c's x, y, z extents
+//     as (lo rounded down, hi rounded up) half2 pairs, words 12 + c = child c's
+//     ref (a record index, ~triangle slot, or kQuadEmpty: no child).
 struct DevScene {
   const float4* nodes;
   const float4* qnodes;
   const float4* tris;
   const uint4* wnodes;
   const float4* wtris;
+  const uint4* quad;
   int root_ref;
   int ntri;
   int nrec;
-  int precision;  // traversal format: 0 FP32 records, 1 FP16 records, 2 the wide BVH
+  int precision;  // traversal format: 0 FP32 records, 1 FP16 records, 2 the wide BVH, 3 4-wide FP16 nodes
   // shading data in the reference layout
   const float4* points;
   const float2* uvs;

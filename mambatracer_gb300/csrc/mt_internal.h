@@ -92,6 +92,7 @@ struct mt_scene {
   float4* d_tris = nullptr;
   uint4* d_qnodes = nullptr;  // FP16 records (precision 1)
   uint4* d_wnodes = nullptr;  // wide BVH with 8-bit child boxes (precision 2)
+  uint4* d_quad = nullptr;    // 4-wide FP16 nodes (precision 3)
   float4* d_wtris = nullptr;
   int nwide = 0, wdepth = 0;
   int nrec = 0, root_ref = 0, depth = 0, has_bvh = 0, precision = 0;
@@ -126,7 +127,11 @@ struct mt_scene {
     s.nrec = nrec;
     s.wnodes = d_wnodes;
     s.wtris = d_wtris;
-    s.precision = (precision == 1 && d_qnodes) ? 1 : (precision == 2 && d_wnodes) ? 2 : 0;
+    s.quad = d_quad;
+    s.precision = (precision == 1 && d_qnodes) ? 1
+                  : (precision == 2 && d_wnodes) ? 2
+                  : (precision == 3 && d_quad)   ? 3
+                                                 : 0;
     s.points = d_points;
     s.uvs = d_uvs;
     s.normals = d_normals;
@@ -210,6 +215,7 @@ struct mt_job {
   // benchmark-semantics shading form of the next frames (1 two launches, 0 one),
   // chosen from the last finished frame's bounce-1 survivors; -1 not yet known
   int shade_split = -1;
+  int64_t launches = 0;  // kernels of the render passes and film merges issued (mt_job_launches)
   int grid_on = 0, grid_fp64 = 0;
   int nu = 0, nv = 0, rx = 0, ry = 0;
   float* d_grid_func = nullptr;
@@ -244,8 +250,9 @@ void join_jobs(mt_context* ctx);
 int quiesce(mt_context* ctx);
 // Waits for the requests running on the context's servers' lanes.
 void servers_sync(mt_context* ctx);
-// Rebuild (precision 1) or drop the scene's FP16 records from its FP32 records,
-// and the wide BVH (precision 2, refresh_wide).
+// Rebuild or drop the scene's derived traversal formats from its FP32 records:
+// FP16 records (precision 1), 4-wide FP16 nodes (precision 3), and the wide BVH
+// (precision 2, refresh_wide).
 int refresh_qnodes(mt_scene* s);
 int refresh_wide(mt_scene* s);
 // MT_CDF_TABLES=0 turns the CDF tables of environment sampling off (the samplers

@@ -500,6 +500,12 @@ extern "C" int mt_render_frame(mt_job* j, const int32_t* seeds, float frame_coun
     if (r) return r;
   }
   s.ran = true;
+  {
+    // per pass: raygen, per bounce closest hits + shading (one launch or two) +
+    // shadow rays, the ray totals; then the film merge
+    const int two = c.mode == 1 && (j->shade_split < 0 ? shade_split_setting() != 0 : j->shade_split != 0);
+    j->launches += (int64_t)c.spp * (2 + (int64_t)c.max_depth * (3 + two)) + (j->nslots > 1 ? 1 : 0);
+  }
   CU(cudaEventRecord(s.ev1, s.stream));
   if (accumulate) {
     // CAdaptiveEnvironment.update (CAdaptiveEnvironment.java:128-137): func = accum,
@@ -549,6 +555,12 @@ extern "C" int mt_job_total_rays(mt_job* j, int64_t* rays3) {
   CU(cudaStreamSynchronize(j->ctx->stream));
   for (int k = 0; k < 3; ++k) rays3[k] = (int64_t)t[k];
   if (t[3]) return fail(MT_ERR_DEVICE, "device error %llu latched", t[3]);
+  return MT_OK;
+}
+
+extern "C" int mt_job_launches(mt_job* j, int64_t* n) {
+  if (!j || !n) return fail(MT_ERR_INVALID, "NULL argument");
+  *n = j->launches;
   return MT_OK;
 }
 

@@ -147,7 +147,8 @@ constexpr int kSteps = 64;
 // MINB: resident blocks per SM the register allocation is bounded for (the
 // traversal is latency-bound: more resident warps hide more load latency, at
 // the price of registers).
-// PREC: the BVH record format (0 FP32 child boxes, 1 FP16 outward-rounded).
+// PREC: the BVH format (0 FP32 child boxes, 1 FP16 outward-rounded, 2 the wide
+// BVH with 8-bit boxes, 3 4-wide FP16 nodes).
 template <int MINB, int PREC>
 __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_closest(DevScene S, Ctrl* ctrl, int b, FrameBufs fb,
                                                                        int steps) {
@@ -690,13 +691,18 @@ int wide_blocks_per_sm() {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_closest<kWideMinBlocks, 2>, kTraceThreads, 0);
   return n > 0 ? n : 1;
 }
+// 4-wide FP16 nodes (built for the tuning's bound like the binary kernels): a
+// step visits a node of four child boxes (two binary levels) or tests a triangle.
+int quad_steps_of(int steps) { return std::max(2, steps / 2); }
 template <int MINB>
 void launch_traces(cudaStream_t st, int grid, const DevScene& S, Ctrl* ctrl, int b, int mode, FrameBufs fb, int kahan,
                    bool closest) {
   const int steps = tuning_ref().refill_steps;
   if (closest) {
     const int f = S.precision;
-    if (f == 2)
+    if (f == 3)
+      k_trace_closest<MINB, 3><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, quad_steps_of(steps));
+    else if (f == 2)
       k_trace_closest<kWideMinBlocks, 2><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, wide_steps_of(steps));
     else if (f == 1)
       k_trace_closest<MINB, 1><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, steps);
@@ -704,7 +710,9 @@ void launch_traces(cudaStream_t st, int grid, const DevScene& S, Ctrl* ctrl, int
       k_trace_closest<MINB, 0><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, steps);
   } else {
     const int f = S.precision;
-    if (f == 2)
+    if (f == 3)
+      k_trace_shadow<MINB, 3><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan, quad_steps_of(steps));
+    else if (f == 2)
       k_trace_shadow<kWideMinBlocks, 2><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan,
                                                                         wide_steps_of(steps));
     else if (f == 1)
@@ -752,8 +760,7 @@ void launch_trace(cudaStream_t st, const DevScene& S, Ctrl* ctrl, int b, int mod
   if (bps[minb] == 0)
     bps[minb] = minb == 16 ? trace_blocks_per_sm<16>() : minb == 12 ? trace_blocks_per_sm<12>() : trace_blocks_per_sm<8>();
   if (wide_bps == 0) wide_bps = wide_blocks_per_sm();
-  const bool wide = S.precision == 2;
-  const int fit = wide ? wide_bps : bps[minb];
+  const int fit = S.precision == 2 ? wide_bps : bps[minb];
   const int want = closest ? trace_grid_bps() : shadow_grid_bps();
   const int per_sm = !shared ? fit : want > 0 ? std::min(want, fit) : std::max(1, fit / 2);
   const int grid = std::max(1, std::min(num_sms * per_sm, (N + kTraceThreads - 1) / kTraceThreads));
@@ -917,7 +924,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_query(DevScene S, const fl
                                                             float* __restrict__ t_out, int* __restrict__ prim_out,
                                                             int* work, int* err) {
   bool overflow = false;
-  const int steps = PREC == 2 ? kSteps / 8 : kSteps;
+  const int steps = PREC == 2 ? kSteps / 8 : PREC == 3 ? kSteps / 2 : kSteps;
   if (any)
     tr::trace_persistent<true, kSteps, RefRays, QueryOut, PREC>(S, n, work, RefRays{rays}, QueryOut{1, t_out, prim_out},
                                                                 &overflow, steps);
@@ -930,7 +937,8 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_query(DevScene S, const fl
 // Traversal work per ray: the same traversal as k_query, one step at a time,
 // counting interior-node visits and triangle tests (counts[2 i], counts[2 i + 1]).
 // Binary records: the visits the reference's algorithm makes (a step is one or
-// the other, classified before it runs); the wide BVH: its node visits (96-byte nodes).
+// the other, classified before it runs); the wide BVH: its node visits (96-byte
+// nodes); 4-wide FP16 nodes: their node visits (64-byte nodes).
 template <int PREC, bool ANY>
 __global__ void __launch_bounds__(kTraceThreads) k_count(DevScene S, const float4* __restrict__ rays, int n,
                                                          float* __restrict__ t_out, int* __restrict__ prim_out,
@@ -950,15 +958,23 @@ __global__ void __launch_bounds__(kTraceThreads) k_count(DevScene S, const float
     visits = cnt[0];
     tests = cnt[1];
   } else {
-    typename tr::StackEntry<ANY>::type stack[kStackDepth], top;
+    typename tr::StackEntry<ANY>::type stack[PREC == 3 ? kQuadStack : kStackDepth], top;
     int ref = S.root_ref;
     const bool finite = tr::ray_is_finite(r);
-    for (;;) {
-      const bool node = ref >= 0;
-      const bool done = tr::trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, top, 1, &overflow);
-      visits += node;
-      tests += !node;
-      if (done) break;
+    if constexpr (PREC == 3) {
+      int leaf = kQuadEmpty, cnt[2] = {0, 0};
+      while (!tr::quad_steps<ANY>(S, r, ref, leaf, sp, hit, finite, stack, top, 1, &overflow, cnt)) {
+      }
+      visits = cnt[0];
+      tests = cnt[1];
+    } else {
+      for (;;) {
+        const bool node = ref >= 0;
+        const bool done = tr::trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, top, 1, &overflow);
+        visits += node;
+        tests += !node;
+        if (done) break;
+      }
     }
   }
   if (overflow) atomicExch(err, kDevErrStack);
@@ -975,7 +991,9 @@ int launch_count(cudaStream_t st, const DevScene& S, const float4* rays, int n, 
   if (any) k_count<P, true><<<g, kTraceThreads, 0, st>>>(S, rays, n, t_out, prim_out, counts, err); \
   else k_count<P, false><<<g, kTraceThreads, 0, st>>>(S, rays, n, t_out, prim_out, counts, err);
   const int f = S.precision;
-  if (f == 2) {
+  if (f == 3) {
+    MT_COUNT(3)
+  } else if (f == 2) {
     MT_COUNT(2)
   } else if (f == 1) {
     MT_COUNT(1)
@@ -992,7 +1010,9 @@ int launch_query(cudaStream_t st, const DevScene& S, const float4* rays, int n, 
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_query<0>, kTraceThreads, 0);
   if (bps < 1) bps = 1;
   const int f = S.precision;
-  if (f == 2)
+  if (f == 3)
+    k_query<3><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
+  else if (f == 2)
     k_query<2><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
   else if (f == 1)
     k_query<1><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);

@@ -10,7 +10,7 @@
 // the same order without re-reading parents. Identical order and identical
 // arithmetic give identical hit ids, including ties.
 //
-// Two record formats (DevScene::precision): 0 = FP32 child boxes, 64 bytes per
+// Binary record formats (DevScene::precision): 0 = FP32 child boxes, 64 bytes per
 // record; 1 = FP16 child boxes rounded outward (lower bounds down, upper bounds
 // up), 32 bytes per record: the half-size record halves the bytes a visit
 // moves through L1/L2. An outward-rounded box contains the FP32 box, and the
@@ -237,6 +237,148 @@ __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref,
   return false;
 }
 
+// ------------------------------------------------------------------ 4-wide FP16
+// Precision 3: the node of record r holds the children of r's two children
+// (a leaf child stands for itself), so one 64-byte node read replaces the two
+// dependent record reads of two binary levels. The boxes are the FP32 records'
+// child boxes rounded outward to FP16 as in precision 1, tested with the same
+// slab arithmetic, so the boxes entered contain those the binary traversal
+// enters (a grandchild's box nests in its parent's) and every triangle it tests
+// is tested here with the same FP32 Moller-Trumbore: the closest hit is the same
+// triangle at the same distance, except that of two triangles hit at exactly the
+// same distance the one tested first is kept. Children hit are taken nearest
+// first; the others are deferred with their entry distance (closest hits cull
+// deferred interior nodes as above).
+__device__ __forceinline__ float2 half2_bits(unsigned u) {
+  return __half22float2(*reinterpret_cast<const __half2*>(&u));
+}
+
+// Leaves wait in a one-entry slot (leaf) while the lane goes on with interior
+// nodes; the warp tests the waiting leaves together when one of its lanes can
+// go no further (its slot is taken and its next entry is a leaf too, or its
+// stack is empty), so node visits run on converged lanes and triangle tests on
+// many lanes at once instead of a few lanes interleaving the two (Aila, Laine,
+// "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009, postponed
+// leaves). A closest-hit ray's waiting triangle shortens its interval only when
+// tested, so culling is then looser, never tighter.
+// ref: the next entry (a node >= 0, a leaf < 0, kQuadEmpty: nothing left);
+// leaf: the waiting leaf or kQuadEmpty. cnt (or NULL): [0] += node visits,
+// [1] += triangle tests.
+template <bool ANY>
+__device__ __forceinline__ bool quad_steps(const DevScene& S, RayT& r, int& ref, int& leaf, int& sp, int& hit_face,
+                                           bool finite, typename StackEntry<ANY>::type* stack,
+                                           typename StackEntry<ANY>::type& top, int steps, bool* overflow,
+                                           int* cnt = nullptr) {
+  const float4* __restrict__ tris = S.tris;
+  // (lo, hi) half pairs swapped to (near, far) by the direction's sign
+  const unsigned selx = r.sx ? 0x1032u : 0x3210u, sely = r.sy ? 0x1032u : 0x3210u, selz = r.sz ? 0x1032u : 0x3210u;
+  // the next deferred entry, or kQuadEmpty
+  auto pop = [&]() -> int {
+    if constexpr (ANY) {
+      if (sp == 0) return kQuadEmpty;
+      const int e = top;
+      if (--sp > 0) top = stack[sp - 1];
+      return e;
+    } else {
+      for (;;) {
+        if (sp == 0) return kQuadEmpty;
+        const int2 e = stack[--sp];
+        if (!finite || e.x < 0 || __int_as_float(e.y) < r.tmax) return e.x;
+      }
+    }
+  };
+  for (int it = 0; it < steps; ++it) {
+    if (ref < 0 && ref != kQuadEmpty && leaf == kQuadEmpty) {
+      leaf = ref;
+      ref = pop();
+    }
+    if (ref == kQuadEmpty && leaf == kQuadEmpty) return true;
+    if (__any_sync(__activemask(), ref < 0)) {
+      // triangle tests: every lane with a waiting leaf
+      if (leaf != kQuadEmpty) {
+        if (cnt) ++cnt[1];
+        const float4* tp = tris + 3 * (size_t)(~leaf);
+        const float4 p1 = __ldg(tp + 0), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+        leaf = kQuadEmpty;
+        const float t = tri_t(r, p1, e1, e2);
+        if ((r.tmin < t) && (t < r.tmax)) {
+          hit_face = __float_as_int(p1.w);
+          if (ANY) return true;
+          r.tmax = t;
+        }
+      }
+      continue;
+    }
+    // node visit: ref >= 0 on every lane here
+    if (cnt) ++cnt[0];
+    const uint4* p = S.quad + 4 * (size_t)ref;
+    uint4 a, b, c, d;
+    ldg32(p, a, b);
+    ldg32(p + 2, c, d);
+    const unsigned wv[12] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+    const int cr[4] = {(int)d.x, (int)d.y, (int)d.z, (int)d.w};
+    float key[4];
+    int kid[4];
+    int n = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      float tn;
+      bool h;
+      if (finite) {
+        const float2 x = half2_bits(__byte_perm(wv[3 * k], 0u, selx));
+        const float2 y = half2_bits(__byte_perm(wv[3 * k + 1], 0u, sely));
+        const float2 z = half2_bits(__byte_perm(wv[3 * k + 2], 0u, selz));
+        h = slab_fast(r, x.x, x.y, y.x, y.y, z.x, z.y, &tn);
+      } else {
+        const float2 x = half2_bits(wv[3 * k]), y = half2_bits(wv[3 * k + 1]), z = half2_bits(wv[3 * k + 2]);
+        h = slab(r, x.x, x.y, y.x, y.y, z.x, z.y, &tn);
+        if (tn != tn) tn = -INFINITY;  // order only: a NaN entry distance sorts first
+      }
+      h = h && cr[k] != kQuadEmpty;
+      key[k] = h ? tn : INFINITY;
+      kid[k] = cr[k];
+      n += h;
+    }
+    if (n == 0) {
+      ref = pop();
+      continue;
+    }
+    // nearest first (children missed carry +inf and sort last)
+    auto cx = [&](int i, int j) {
+      const bool s = key[j] < key[i];
+      const float ki = key[i], kj = key[j];
+      const int ri = kid[i], rj = kid[j];
+      key[i] = s ? kj : ki;
+      key[j] = s ? ki : kj;
+      kid[i] = s ? rj : ri;
+      kid[j] = s ? ri : rj;
+    };
+    cx(0, 1);
+    cx(2, 3);
+    cx(0, 2);
+    cx(1, 3);
+    cx(1, 2);
+    if (sp + n - 1 > kQuadStack) {
+      *overflow = true;
+      return true;
+    }
+#pragma unroll
+    for (int k = 3; k >= 1; --k) {
+      if (k < n) {
+        if constexpr (ANY) {
+          if (sp > 0) stack[sp - 1] = top;
+          top = kid[k];
+          ++sp;
+        } else {
+          stack[sp++] = make_int2(kid[k], __float_as_int(key[k]));
+        }
+      }
+    }
+    ref = kid[0];
+  }
+  return false;
+}
+
 // ------------------------------------------------------------------ wide BVH
 // Precision 2: the same tree collapsed into nodes of up to eight children whose
 // boxes are quantised to 8 bits per plane against the node's FP32 origin and a
@@ -436,11 +578,11 @@ template <bool ANY, int STEPS, class Src, class Dst, int PREC>
 __device__ __forceinline__ void trace_persistent_binary(const DevScene& S, int count, int* work, Src src, Dst dst,
                                                         bool* overflow, int steps) {
   const int lane = threadIdx.x & 31;
-  typename StackEntry<ANY>::type stack[kStackDepth], top;
+  typename StackEntry<ANY>::type stack[PREC == 3 ? kQuadStack : kStackDepth], top;
   int i = -1;
   bool exhausted = false;
   RayT r;
-  int ref = 0, sp = 0, hit = -1;
+  int ref = 0, sp = 0, hit = -1, leaf = kQuadEmpty;
   bool finite = true;
   for (;;) {
     const bool need = (i < 0) && !exhausted;
@@ -457,6 +599,7 @@ __device__ __forceinline__ void trace_persistent_binary(const DevScene& S, int c
           r = src(i);
           finite = ray_is_finite(r);
           ref = S.root_ref;
+          leaf = kQuadEmpty;
           sp = 0;
           hit = -1;
         }
@@ -465,7 +608,14 @@ __device__ __forceinline__ void trace_persistent_binary(const DevScene& S, int c
     }
     const bool active = i >= 0;
     if (!__any_sync(0xffffffffu, active)) break;
-    if (active && trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, top, steps, overflow)) {
+    bool done = false;
+    if (active) {
+      if constexpr (PREC == 3)
+        done = quad_steps<ANY>(S, r, ref, leaf, sp, hit, finite, stack, top, steps, overflow);
+      else
+        done = trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, top, steps, overflow);
+    }
+    if (done) {
       dst(i, r, hit);
       i = -1;
     }
@@ -473,7 +623,7 @@ __device__ __forceinline__ void trace_persistent_binary(const DevScene& S, int c
 }
 
 // PREC: 0 FP32 records, 1 FP16 records (binary, the reference's visit order),
-// 2 the wide BVH with 8-bit child boxes.
+// 2 the wide BVH with 8-bit child boxes, 3 4-wide FP16 nodes.
 template <bool ANY, int STEPS, class Src, class Dst, int PREC = 0>
 __device__ __forceinline__ void trace_persistent(const DevScene& S, int count, int* work, Src src, Dst dst,
                                                  bool* overflow, int steps = STEPS) {

@@ -214,8 +214,8 @@ def main():
     ap.add_argument("--frames", type=int, default=24)
     ap.add_argument("--rounds", type=int, default=2)
     ap.add_argument("--served", action="store_true", help="also search the merged server's slots and streams")
-    ap.add_argument("--precision", type=int, default=1, choices=[0, 1, 2],
-                    help="traversal format of the scenes (mt_scene_set_bvh_precision; the bench's is 1)")
+    ap.add_argument("--precision", type=int, default=3, choices=[0, 1, 2, 3],
+                    help="traversal format of the scenes (mt_scene_set_bvh_precision; the bench's is 3)")
     args = ap.parse_args()
     build.build()
     ctx = api.Context(0)
@@ -225,7 +225,7 @@ def main():
     S.set_precision(args.precision)
     S.set_env(scenes.sky_env(2048, 1024), 2048, 1024)
     S.grid_config(1600, 1600, 16, 32, enable=2)
-    records = {0: "FP32 records", 1: "FP16 records", 2: "wide BVH"}[args.precision]
+    records = {0: "FP32 records", 1: "FP16 records", 2: "wide BVH", 3: "4-wide FP16"}[args.precision]
     workload = (f"soup {args.triangles} triangles, {args.width}x{args.height}, depth 8, RR from 3, 2048x1024 sky, "
                 f"1600x1600 light grid (FP64 cell SATs), 6 frames in flight, {records}")
     log = lambda m: print(m, flush=True)  # noqa: E731

@@ -12,8 +12,8 @@ The 1M-triangle soup and the 3.3M-triangle stadium of the benchmark:
   * the traversal work of the FP32 records (mt_trace_counts): the oracle's
     triangle tests exactly, and no more interior visits than the oracle (deferred
     nodes beyond the closest hit are dropped);
-  * FP16 records and the wide BVH with 8-bit boxes give the same distances as
-    FP32 records, and the wide BVH visits fewer nodes.
+  * FP16 records, the wide BVH with 8-bit boxes and the 4-wide FP16 nodes give
+    the same distances as FP32 records, and the wide formats visit fewer nodes.
 """
 import numpy as np
 import pytest
@@ -61,16 +61,19 @@ def _check_scene(ctx, orc, sc, nrays, nsample):
     past["tMax"] = t[hit] * np.float32(1.001) + np.float32(1e-6)
     assert S.trace_any(past).all()
 
-    # FP16 records, the wide BVH: the same distances
-    for prec in (1, 2):
+    # FP16 records, the wide BVH, 4-wide FP16 nodes: the same distances
+    wc = {}
+    for prec in (1, 2, 3):
         S.set_precision(prec)
         tq, pq = S.trace_closest(rays)
         assert tq.tobytes() == t.tobytes()
         assert (pq != p).sum() <= max(2, nrays // 10000)
-    _, _, wc = S.trace_counts(sub)
+        wc[prec] = S.trace_counts(sub)[2]
     print(f"interior visits per ray: oracle {oc[:, 0].mean():.1f}, FP32 records {gc[:, 0].mean():.1f}, "
-          f"wide BVH {wc[:, 0].mean():.1f}; triangle tests {oc[:, 1].mean():.2f} / {wc[:, 1].mean():.2f}")
-    assert wc[:, 0].mean() < 0.6 * gc[:, 0].mean()
+          f"wide BVH {wc[2][:, 0].mean():.1f}, 4-wide {wc[3][:, 0].mean():.1f}; triangle tests "
+          f"{oc[:, 1].mean():.2f} / {wc[2][:, 1].mean():.2f} / {wc[3][:, 1].mean():.2f}")
+    assert wc[2][:, 0].mean() < 0.6 * gc[:, 0].mean()
+    assert wc[3][:, 0].mean() < 0.6 * gc[:, 0].mean()
     S.close()
 
 

@@ -24,8 +24,9 @@ only last-ulp branch flips of CUDA's transcendentals move them), and the primary
 rays' hit ids against the FP32 oracle traversal with the rays within 1e-6
 barycentric of a triangle edge counted apart (Moller-Trumbore,
 src/cl/kernel/Primitive.cl:3-29). FP32 records: every hit id equal, every hit
-distance bit-identical. FP16 outward-rounded records and the wide BVH with
-8-bit boxes: any differing id must be an exact-distance tie.
+distance bit-identical. FP16 outward-rounded records, the wide BVH with 8-bit
+boxes and the 4-wide FP16 nodes (the bench's format): any differing id must be
+an exact-distance tie.
 """
 import json
 
@@ -75,6 +76,10 @@ def test_soup_1080p_fp16_records(ctx, orc):
 
 def test_soup_1080p_wide_bvh(ctx, orc):
     _check(_run(ctx, orc, "soup", 2), exact_ids=False)
+
+
+def test_soup_1080p_quad_nodes(ctx, orc):
+    _check(_run(ctx, orc, "soup", 3), exact_ids=False)
 
 
 def test_stadium_1080p(ctx, orc):

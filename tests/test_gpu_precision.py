@@ -14,6 +14,8 @@
    boxes stand on its floor): the reference's slab test on a flat triangle box
    then sometimes skips the nearer one, which the wide traversal tests. Those
    rays are counted, and the wide traversal's distance is never the larger.
+3. 4-wide FP16 nodes: a record's grandchildren with the FP16 records' boxes, so
+   the same hits as 2 (the intermediate level's boxes are not tested).
 
 Frames in benchmark semantics are compared with the FP32 records' frames."""
 import numpy as np
@@ -32,7 +34,7 @@ CASES = {
 }
 
 
-@pytest.mark.parametrize("prec", [1, 2])
+@pytest.mark.parametrize("prec", [1, 2, 3])
 @pytest.mark.parametrize("which", list(CASES))
 def test_quantised_formats_trace_the_same_hits(ctx, which, prec):
     sc = CASES[which]()
@@ -99,7 +101,7 @@ def test_fp16_records_render(ctx):
 def test_precision_argument_checked(ctx):
     S = api.Scene(ctx, scenes.box_room(8, 8))
     with pytest.raises(MTError):
-        S.set_precision(3)
+        S.set_precision(4)
     S.close()
 
 

@@ -78,6 +78,7 @@ for f in range(4):
 np.save({out!r}, J.film())
 rays = J.total_rays()
 np.save({out!r} + ".rays.npy", rays)
+np.save({out!r} + ".launches.npy", np.array([J.launches()]))
 J.close(); S.close(); ctx.close()
 """
 
@@ -99,7 +100,10 @@ def test_two_launch_shading_equals_one_launch(ctx, soup_scene, tmp_path, grid):
         env = dict(os.environ, MT_SHADE_SPLIT=split)
         subprocess.run([sys.executable, "-c", _SINGLE_LAUNCH.format(root=root, out=out, grid=grid)], env=env,
                        check=True, timeout=600)
-        films.append((np.load(out), np.load(out + ".rays.npy")))
+        films.append((np.load(out), np.load(out + ".rays.npy"), int(np.load(out + ".launches.npy")[0])))
+    # launches (mt_job_launches): 4 frames x (raygen + 6 bounces x (closest hits,
+    # shading in 2 or 1 launches, shadow rays) + ray totals) + 4 film merges
+    assert films[0][2] == 4 * (2 + 6 * 4) + 4 and films[1][2] == 4 * (2 + 6 * 3) + 4
     assert films[0][0].tobytes() == films[1][0].tobytes()
     assert np.array_equal(films[0][1], films[1][1])
     assert films[0][0][:, :3].sum() > 0
