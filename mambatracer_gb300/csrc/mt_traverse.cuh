@@ -249,8 +249,33 @@ __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref,
 // same distance the one tested first is kept. Children hit are taken nearest
 // first; the others are deferred with their entry distance (closest hits cull
 // deferred interior nodes as above).
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
 __device__ __forceinline__ float2 half2_bits(unsigned u) {
   return __half22float2(*reinterpret_cast<const __half2*>(&u));
+}
+__device__ __forceinline__ unsigned long long pack2(float a, float b) {
+  unsigned long long v;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(v) : "f"(a), "f"(b));
+  return v;
+}
+// (p - o) * i on both lanes, each lane rounded as the scalar subtraction and
+// multiplication are (add/mul .rn on f32x2: two IEEE operations per instruction)
+__device__ __forceinline__ float2 sub_mul2(unsigned long long p, unsigned long long o, unsigned long long i) {
+  unsigned long long t;
+  float2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t) : "l"(p), "l"(o));
+  asm("mul.rn.f32x2 %0, %0, %1;" : "+l"(t) : "l"(i));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(t));
+  return r;
 }
 
 // Leaves wait in a one-entry slot (leaf) while the lane goes on with interior
@@ -272,6 +297,7 @@ __device__ __forceinline__ bool quad_steps(const DevScene& S, RayT& r, int& ref,
   const float4* __restrict__ tris = S.tris;
   // (lo, hi) half pairs swapped to (near, far) by the direction's sign
   const unsigned selx = r.sx ? 0x1032u : 0x3210u, sely = r.sy ? 0x1032u : 0x3210u, selz = r.sz ? 0x1032u : 0x3210u;
+  const unsigned long long oxy = pack2(r.ox, r.oy), ixy = pack2(r.ix, r.iy);
   // the next deferred entry, or kQuadEmpty
   auto pop = [&]() -> int {
     if constexpr (ANY) {
@@ -325,16 +351,20 @@ __device__ __forceinline__ bool quad_steps(const DevScene& S, RayT& r, int& ref,
       float tn;
       bool h;
       if (finite) {
+        // slab_fast on (near, far) planes; an empty slot's (+inf, -inf) box
+        // gives an entry distance of +inf and never passes
         const float2 x = half2_bits(__byte_perm(wv[3 * k], 0u, selx));
         const float2 y = half2_bits(__byte_perm(wv[3 * k + 1], 0u, sely));
         const float2 z = half2_bits(__byte_perm(wv[3 * k + 2], 0u, selz));
-        h = slab_fast(r, x.x, x.y, y.x, y.y, z.x, z.y, &tn);
+        const float2 nxy = sub_mul2(pack2(x.x, y.x), oxy, ixy), fxy = sub_mul2(pack2(x.y, y.y), oxy, ixy);
+        tn = max3f(nxy.x, nxy.y, (z.x - r.oz) * r.iz);
+        const float tf = min3f(fxy.x, fxy.y, (z.y - r.oz) * r.iz);
+        h = (tn <= tf) && (tn < r.tmax) && (tf * 1.00000024f > r.tmin);
       } else {
         const float2 x = half2_bits(wv[3 * k]), y = half2_bits(wv[3 * k + 1]), z = half2_bits(wv[3 * k + 2]);
-        h = slab(r, x.x, x.y, y.x, y.y, z.x, z.y, &tn);
+        h = slab(r, x.x, x.y, y.x, y.y, z.x, z.y, &tn) && cr[k] != kQuadEmpty;
         if (tn != tn) tn = -INFINITY;  // order only: a NaN entry distance sorts first
       }
-      h = h && cr[k] != kQuadEmpty;
       key[k] = h ? tn : INFINITY;
       kid[k] = cr[k];
       n += h;
@@ -427,16 +457,6 @@ __device__ __forceinline__ void wide_init(const RayT& r, WideState& w) {
 // 2^23 + (byte k of w), exactly: the byte placed in the mantissa of 2^23.
 __device__ __forceinline__ float qbyte(unsigned w, int k) {
   return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + k));
-}
-__device__ __forceinline__ float max3f(float a, float b, float c) {
-  float r;
-  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-  return r;
-}
-__device__ __forceinline__ float min3f(float a, float b, float c) {
-  float r;
-  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-  return r;
 }
 // The 8-bit slot mask m with slot s moved to slot s ^ x (x in 0..7).
 __device__ __forceinline__ unsigned xor_permute8(unsigned m, unsigned x) {
