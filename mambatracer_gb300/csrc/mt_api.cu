@@ -260,6 +260,7 @@ void free_scene(mt_scene* s) {
   dfree(s->d_wnodes);
   dfree(s->d_wtris);
   dfree(s->d_quad);
+  dfree(s->d_up);
   dfree(s->d_env_rgb);
   dfree(s->d_env_lum);
   dfree(s->d_env_sat);

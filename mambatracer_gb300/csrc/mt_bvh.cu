@@ -33,6 +33,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "mt_internal.h"
@@ -425,6 +427,17 @@ __global__ void k_quad_fp16(const float4* __restrict__ recs, int nrec, uint4* q)
   o[3] = make_uint4(w[12], w[13], w[14], w[15]);
 }
 
+// Parent links: up[c] = (r, the other child of r) for each record child c of record r.
+__global__ void k_up_links(const float4* __restrict__ recs, int nrec, int root, int2* up) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrec) return;
+  const float4 n3 = recs[4 * (size_t)i + 3];
+  const int l = __float_as_int(n3.x), r = __float_as_int(n3.y);
+  if (l >= 0) up[l] = make_int2(i, r);
+  if (r >= 0) up[r] = make_int2(i, l);
+  if (i == root) up[i] = make_int2(-1, -1);
+}
+
 __global__ void k_seed(Seg* segs, int n) {
   if (blockIdx.x == 0 && threadIdx.x == 0) segs[0] = Seg{0, 0, n, 1, 0, -1, 0, 0};
 }
@@ -561,9 +574,28 @@ extern "C" int mt_bvh_build_device(mt_scene* s, int32_t* nodes_out, float* bound
   return refresh_qnodes(s);
 }
 
+bool traversal_bitstack() {
+  static const bool on = [] {
+    const char* e = std::getenv("MT_TRAVERSAL");
+    return e && std::strcmp(e, "bitstack") == 0;
+  }();
+  return on;
+}
+
 int refresh_qnodes(mt_scene* s) {
   dfree(s->d_qnodes);
   dfree(s->d_quad);
+  dfree(s->d_up);
+  if (traversal_bitstack() && s->has_bvh && s->nrec > 0) {
+    int r = dalloc(&s->d_up, (size_t)s->nrec);
+    if (r) return r;
+    cudaStream_t st = s->ctx->stream;
+    k_up_links<<<blocks(s->nrec), kT, 0, st>>>(s->d_nodes, s->nrec, s->root_ref, s->d_up);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+      dfree(s->d_up);
+      return fail(MT_ERR_CUDA, "parent links: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+  }
   if (int w = refresh_wide(s)) return w;
   if (s->precision == 3 && s->has_bvh && s->nrec > 0) {
     int r = dalloc(&s->d_quad, 4 * (size_t)s->nrec);

@@ -68,6 +68,8 @@ static_assert(sizeof(Material) == 144, "Material layout");
 //     children, right's children; words 3c .. 3c + 2 = child c's x, y, z extents
 //     as (lo rounded down, hi rounded up) half2 pairs, words 12 + c = child c's
 //     ref (a record index, ~triangle slot, or kQuadEmpty: no child).
+//   up: per record (parent record, the record's sibling ref), the root (-1, -1):
+//     the links of the stackless traversal (bitstack_steps).
 struct DevScene {
   const float4* nodes;
   const float4* qnodes;
@@ -75,6 +77,8 @@ struct DevScene {
   const uint4* wnodes;
   const float4* wtris;
   const uint4* quad;
+  const int2* up;
+  int bitstack;  // binary formats: 1 = the stackless traversal (bitstack and parent links)
   int root_ref;
   int ntri;
   int nrec;

@@ -74,6 +74,10 @@ struct mt_buffer {
   size_t bytes;
 };
 
+// MT_TRAVERSAL=bitstack (read once per process): the binary formats traverse
+// without a deferred-node stack, as the reference does (bitstack_steps).
+bool traversal_bitstack();
+
 struct mt_scene {
   mt_context* ctx;
   int npoints = 0, nuvs = 0, nnormals = 0, ntri = 0, nmat = 0;
@@ -93,6 +97,7 @@ struct mt_scene {
   uint4* d_qnodes = nullptr;  // FP16 records (precision 1)
   uint4* d_wnodes = nullptr;  // wide BVH with 8-bit child boxes (precision 2)
   uint4* d_quad = nullptr;    // 4-wide FP16 nodes (precision 3)
+  int2* d_up = nullptr;       // parent links of the records (the stackless traversal)
   float4* d_wtris = nullptr;
   int nwide = 0, wdepth = 0;
   int nrec = 0, root_ref = 0, depth = 0, has_bvh = 0, precision = 0;
@@ -128,6 +133,8 @@ struct mt_scene {
     s.wnodes = d_wnodes;
     s.wtris = d_wtris;
     s.quad = d_quad;
+    s.up = d_up;
+    s.bitstack = d_up && traversal_bitstack();
     s.precision = (precision == 1 && d_qnodes) ? 1
                   : (precision == 2 && d_wnodes) ? 2
                   : (precision == 3 && d_quad)   ? 3

@@ -698,6 +698,16 @@ template <int MINB>
 void launch_traces(cudaStream_t st, int grid, const DevScene& S, Ctrl* ctrl, int b, int mode, FrameBufs fb, int kahan,
                    bool closest) {
   const int steps = tuning_ref().refill_steps;
+  if (S.bitstack && S.precision <= 1) {
+    if (closest) {
+      if (S.precision == 1) k_trace_closest<MINB, 5><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, steps);
+      else k_trace_closest<MINB, 4><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, fb, steps);
+    } else {
+      if (S.precision == 1) k_trace_shadow<MINB, 5><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan, steps);
+      else k_trace_shadow<MINB, 4><<<grid, kTraceThreads, 0, st>>>(S, ctrl, b, mode, fb, kahan, steps);
+    }
+    return;
+  }
   if (closest) {
     const int f = S.precision;
     if (f == 3)
@@ -924,7 +934,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_query(DevScene S, const fl
                                                             float* __restrict__ t_out, int* __restrict__ prim_out,
                                                             int* work, int* err) {
   bool overflow = false;
-  const int steps = PREC == 2 ? kSteps / 8 : PREC == 3 ? kSteps / 2 : kSteps;
+  const int steps = PREC == 2 ? kSteps / 8 : PREC == 3 ? kSteps / 2 : kSteps;  // 4, 5: stackless binary
   if (any)
     tr::trace_persistent<true, kSteps, RefRays, QueryOut, PREC>(S, n, work, RefRays{rays}, QueryOut{1, t_out, prim_out},
                                                                 &overflow, steps);
@@ -961,7 +971,17 @@ __global__ void __launch_bounds__(kTraceThreads) k_count(DevScene S, const float
     typename tr::StackEntry<ANY>::type stack[PREC == 3 ? kQuadStack : kStackDepth], top;
     int ref = S.root_ref;
     const bool finite = tr::ray_is_finite(r);
-    if constexpr (PREC == 3) {
+    if constexpr (PREC >= 4) {
+      unsigned long long bits = 0;
+      int par = -1, sib = -1;
+      for (;;) {
+        const bool node = ref >= 0;
+        const bool done = tr::bitstack_steps<ANY, PREC - 4>(S, r, ref, bits, par, sib, hit, finite, 1);
+        visits += node;
+        tests += !node;
+        if (done) break;
+      }
+    } else if constexpr (PREC == 3) {
       int leaf = kQuadEmpty, cnt[2] = {0, 0};
       while (!tr::quad_steps<ANY>(S, r, ref, leaf, sp, hit, finite, stack, top, 1, &overflow, cnt)) {
       }
@@ -990,8 +1010,12 @@ int launch_count(cudaStream_t st, const DevScene& S, const float4* rays, int n, 
 #define MT_COUNT(P)                                                                              \
   if (any) k_count<P, true><<<g, kTraceThreads, 0, st>>>(S, rays, n, t_out, prim_out, counts, err); \
   else k_count<P, false><<<g, kTraceThreads, 0, st>>>(S, rays, n, t_out, prim_out, counts, err);
-  const int f = S.precision;
-  if (f == 3) {
+  const int f = S.bitstack && S.precision <= 1 ? 4 + S.precision : S.precision;
+  if (f == 5) {
+    MT_COUNT(5)
+  } else if (f == 4) {
+    MT_COUNT(4)
+  } else if (f == 3) {
     MT_COUNT(3)
   } else if (f == 2) {
     MT_COUNT(2)
@@ -1010,7 +1034,10 @@ int launch_query(cudaStream_t st, const DevScene& S, const float4* rays, int n, 
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_query<0>, kTraceThreads, 0);
   if (bps < 1) bps = 1;
   const int f = S.precision;
-  if (f == 3)
+  if (S.bitstack && f <= 1) {
+    if (f == 1) k_query<5><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
+    else k_query<4><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
+  } else if (f == 3)
     k_query<3><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);
   else if (f == 2)
     k_query<2><<<num_sms * bps, kTraceThreads, 0, st>>>(S, rays, n, any, t_out, prim_out, work, err);

@@ -237,6 +237,69 @@ __device__ __forceinline__ bool trav_steps(const DevScene& S, RayT& r, int& ref,
   return false;
 }
 
+// ------------------------------------------------------------ stackless (binary)
+// The reference's own traversal (NormalBVH.cl:14-92): no deferred-node stack.
+// Each descent pushes one bit on a 64-bit bitstack, 1 when both children were
+// hit and the farther one remains; to backtrack, zero bits are popped while
+// climbing to the parent (parent links: DevScene::up), and at the first 1 the
+// traversal moves to the sibling and clears it. The visit order is the
+// reference's and the one of trav_steps, without its culling of deferred nodes
+// beyond the closest hit (the sibling's entry distance is not kept). par / sib:
+// the current node's parent record and sibling ref, carried in registers from
+// the descent, so a backtrack reads a link only per level it climbs.
+template <bool ANY, int PREC>
+__device__ __forceinline__ bool bitstack_steps(const DevScene& S, RayT& r, int& ref, unsigned long long& bits,
+                                               int& par, int& sib, int& hit_face, bool finite, int steps) {
+  const float4* __restrict__ tris = S.tris;
+  for (int it = 0; it < steps; ++it) {
+    if (ref >= 0) {
+      float4 n0, n1, n2;
+      int left, right;
+      load_record<PREC>(S, ref, n0, n1, n2, left, right);
+      float tl, trr;
+      bool hl, hr;
+      if (finite) {
+        hl = slab_fast(r, r.sx ? n0.y : n0.x, r.sx ? n0.x : n0.y, r.sy ? n0.w : n0.z, r.sy ? n0.z : n0.w,
+                       r.sz ? n2.y : n2.x, r.sz ? n2.x : n2.y, &tl);
+        hr = slab_fast(r, r.sx ? n1.y : n1.x, r.sx ? n1.x : n1.y, r.sy ? n1.w : n1.z, r.sy ? n1.z : n1.w,
+                       r.sz ? n2.w : n2.z, r.sz ? n2.z : n2.w, &trr);
+      } else {
+        hl = slab(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, &tl);
+        hr = slab(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, &trr);
+      }
+      if (hl || hr) {
+        const bool both = hl && hr;
+        const bool rfirst = both ? trr < tl : hr;
+        bits = (bits << 1) | (both ? 1ull : 0ull);
+        par = ref;
+        sib = rfirst ? left : right;
+        ref = rfirst ? right : left;
+        continue;
+      }
+    } else {
+      const float4* tp = tris + 3 * (size_t)(~ref);
+      const float4 p1 = __ldg(tp + 0), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+      const float t = tri_t(r, p1, e1, e2);
+      if ((r.tmin < t) && (t < r.tmax)) {
+        hit_face = __float_as_int(p1.w);
+        if (ANY) return true;
+        r.tmax = t;
+      }
+    }
+    // backtrack: climb past the levels with nothing left, then take the sibling
+    while ((bits & 1ull) == 0ull) {
+      if (bits == 0ull) return true;
+      const int2 u = __ldg(S.up + par);
+      par = u.x;
+      sib = u.y;
+      bits >>= 1;
+    }
+    ref = sib;
+    bits ^= 1ull;
+  }
+  return false;
+}
+
 // ------------------------------------------------------------------ 4-wide FP16
 // Precision 3: the node of record r holds the children of r's two children
 // (a leaf child stands for itself), so one 64-byte node read replaces the two
@@ -598,11 +661,12 @@ template <bool ANY, int STEPS, class Src, class Dst, int PREC>
 __device__ __forceinline__ void trace_persistent_binary(const DevScene& S, int count, int* work, Src src, Dst dst,
                                                         bool* overflow, int steps) {
   const int lane = threadIdx.x & 31;
-  typename StackEntry<ANY>::type stack[PREC == 3 ? kQuadStack : kStackDepth], top;
+  typename StackEntry<ANY>::type stack[PREC == 3 ? kQuadStack : PREC >= 4 ? 1 : kStackDepth], top;
   int i = -1;
   bool exhausted = false;
   RayT r;
-  int ref = 0, sp = 0, hit = -1, leaf = kQuadEmpty;
+  int ref = 0, sp = 0, hit = -1, leaf = kQuadEmpty, par = -1, sib = -1;
+  unsigned long long bits = 0;
   bool finite = true;
   for (;;) {
     const bool need = (i < 0) && !exhausted;
@@ -621,6 +685,8 @@ __device__ __forceinline__ void trace_persistent_binary(const DevScene& S, int c
           ref = S.root_ref;
           leaf = kQuadEmpty;
           sp = 0;
+          bits = 0;
+          par = sib = -1;
           hit = -1;
         }
       }
@@ -632,6 +698,8 @@ __device__ __forceinline__ void trace_persistent_binary(const DevScene& S, int c
     if (active) {
       if constexpr (PREC == 3)
         done = quad_steps<ANY>(S, r, ref, leaf, sp, hit, finite, stack, top, steps, overflow);
+      else if constexpr (PREC >= 4)
+        done = bitstack_steps<ANY, PREC - 4>(S, r, ref, bits, par, sib, hit, finite, steps);
       else
         done = trav_steps<ANY, PREC>(S, r, ref, sp, hit, finite, stack, top, steps, overflow);
     }
@@ -643,7 +711,8 @@ __device__ __forceinline__ void trace_persistent_binary(const DevScene& S, int c
 }
 
 // PREC: 0 FP32 records, 1 FP16 records (binary, the reference's visit order),
-// 2 the wide BVH with 8-bit child boxes, 3 4-wide FP16 nodes.
+// 2 the wide BVH with 8-bit child boxes, 3 4-wide FP16 nodes, 4 / 5 FP32 / FP16
+// records traversed without a stack (bitstack_steps).
 template <bool ANY, int STEPS, class Src, class Dst, int PREC = 0>
 __device__ __forceinline__ void trace_persistent(const DevScene& S, int count, int* work, Src src, Dst dst,
                                                  bool* overflow, int steps = STEPS) {

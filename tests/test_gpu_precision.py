@@ -78,6 +78,70 @@ def test_quantised_formats_trace_the_same_hits(ctx, which, prec):
     S.close()
 
 
+def _same_or_nearer(t0, p0, t1, p1, coplanar_ok):
+    tdiff = t0.view(np.uint32) != t1.view(np.uint32)
+    if not coplanar_ok:
+        assert not tdiff.any()
+        return
+    ulps = np.abs(t0.view(np.int32).astype(np.int64) - t1.view(np.int32).astype(np.int64))
+    assert np.all(t1[tdiff] < t0[tdiff]) and (ulps.max() if tdiff.any() else 0) <= 8
+    assert np.all((p0 != p1) | ~tdiff)
+
+
+@pytest.mark.parametrize("prec", [1, 2, 3])
+def test_quantised_formats_axis_aligned_rays(ctx, prec):
+    """Zero direction components (infinite 1/d, NaN slab terms: the traversal takes
+    the reference's comparison chain, Util.cl:707-732) and origins on box planes:
+    the quantised formats give the FP32 records' distances and any-hit answers."""
+    sc = scenes.box_room(8, 8)
+    S = api.Scene(ctx, sc)
+    S.build_bvh_device(want_arrays=False)
+    rng = np.random.default_rng(3)
+    n = 20000
+    o = rng.uniform(-0.2, 1.2, size=(n, 3)).astype(np.float32)
+    o[: n // 4, 0] = 0.5
+    o[n // 4: n // 2, 1] = 0.0
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d = d.astype(np.float32)
+    d[::3, 0] = 0.0
+    d[1::3, 1] = 0.0
+    d[2::5, 2] = 0.0
+    d[::7] = np.array([0.0, 0.0, -1.0], np.float32)
+    rays = layout.make_rays(o, d)
+    srays = layout.make_rays(o, d, tmin=1e-4, tmax=0.3)
+    t0, p0 = S.trace_closest(rays)
+    a0 = S.trace_any(srays)
+    S.set_precision(prec)
+    t1, p1 = S.trace_closest(rays)
+    assert np.array_equal(S.trace_any(srays), a0)
+    assert (p0 >= 0).sum() > n // 4
+    # the box room's coplanar triangles: the wide formats may keep the nearer of two
+    _same_or_nearer(t0, p0, t1, p1, coplanar_ok=prec != 1)
+    S.close()
+
+
+@pytest.mark.parametrize("prec", [1, 2, 3])
+@pytest.mark.parametrize("ntri", [1, 2, 3, 5])
+def test_quantised_formats_tiny_trees(ctx, prec, ntri):
+    """A root that is a leaf, and nodes with fewer than four (eight) children."""
+    room = scenes.box_room(8, 8)
+    sc = scenes.Scene(points=room.points.copy(), faces=room.faces[:ntri].copy(), materials=room.materials)
+    S = api.Scene(ctx, sc)
+    S.build_bvh_device(want_arrays=False)
+    o, d = scenes.random_rays(room, 20000, seed=5, inside=True)
+    rays = layout.make_rays(o, d)
+    t0, p0 = S.trace_closest(rays)
+    a0 = S.trace_any(rays)
+    S.set_precision(prec)
+    t1, p1 = S.trace_closest(rays)
+    assert np.array_equal(S.trace_any(rays), a0)
+    assert (p0 >= 0).sum() > 0
+    _same_or_nearer(t0, p0, t1, p1, coplanar_ok=prec != 1)
+    assert np.array_equal(p0 >= 0, p1 >= 0)
+    S.close()
+
+
 def test_fp16_records_render(ctx):
     sc = scenes.soup(100000, seed=3, extent=0.8, edge_sigma=0.01)
     env = scenes.sky_env(512, 256)
