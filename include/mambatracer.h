@@ -294,10 +294,9 @@ void* mt_buf_device_ptr(mt_buffer* buf);
  * context unless the host made another one current). Its first call on a
  * device looks up the scratch array's device address in that context, and
  * looks it up again whenever a different context is current there (another
- * context, or a new primary context after cudaDeviceReset); make that first
- * call before any stream capture. Every call uses the same array: calls that
- * overlap on the GPU (other streams, other host threads) race. Errors read
- * through mt_last_error(). */
+ * context, or a new primary context after cudaDeviceReset). Every call uses
+ * the same array: calls that overlap on the GPU (other streams, other host
+ * threads) race. Errors read through mt_last_error(). */
 int mt_compact_isects_noalloc(void* stream, const void* isects_in, const int32_t* pixels_in, int n,
                               void* isects_out, int32_t* pixels_out, int32_t* count_io);
 
