@@ -14,8 +14,10 @@
    boxes stand on its floor): the reference's slab test on a flat triangle box
    then sometimes skips the nearer one, which the wide traversal tests. Those
    rays are counted, and the wide traversal's distance is never the larger.
-3. 4-wide FP16 nodes: a record's grandchildren with the FP16 records' boxes, so
-   the same hits as 2 (the intermediate level's boxes are not tested).
+3. 4-wide FP16 nodes: a record's grandchildren with FP16 boxes rounded outward
+   after a margin of 2^-16 of the scene's extent (the intermediate level's boxes
+   are not tested): the same hits as 2; of two triangles hit at exactly the same
+   distance, the one kept may change between runs (leaf tests wait for the warp).
 
 Frames in benchmark semantics are compared with the FP32 records' frames."""
 import numpy as np
@@ -66,7 +68,13 @@ def test_quantised_formats_trace_the_same_hits(ctx, which, prec):
     # a rebuild keeps the format; going back to FP32 gives the FP32 answers
     S.build_bvh_device(want_arrays=False)
     t2, p2 = S.trace_closest(rays)
-    assert t2.tobytes() == t1.tobytes() and np.array_equal(p2, p1)
+    assert t2.tobytes() == t1.tobytes()
+    if prec == 3:
+        # which of two triangles at exactly the same distance is kept depends on
+        # when the warp tests its waiting leaves, so it may change between runs
+        assert (p2 != p1).sum() <= 1e-4 * len(p1)
+    else:
+        assert np.array_equal(p2, p1)
     # the traversal work: the FP32 records' triangle tests are the oracle's
     # (deferred leaves are always tested); the quantised formats test fewer or
     # more boxes but reach every triangle the FP32 records do
