@@ -141,9 +141,11 @@ int mt_bvh_import(mt_scene* scene, const int32_t* nodes, const float* bounds, in
  * Formats 1-3 are kept beside the FP32 records and rebuilt with every BVH build
  * or import. Outward-rounded boxes contain the FP32 boxes, so closest hits are
  * the same triangles at the same distances; only which of two triangles hit at
- * exactly the same distance is reported can change with the visit order (and
- * for 2 and 3, of coplanar triangles hit within a few ulps the nearer is kept).
- * Any-hit answers are the same in every format. */
+ * exactly the same distance is reported can change with the visit order, and
+ * among coplanar triangles hit within a few ulps of each other format 2 keeps
+ * the nearer and format 3 either (its choice may change between runs, since
+ * its leaf tests wait for the warp). Any-hit answers are the same in every
+ * format. */
 int mt_scene_set_bvh_precision(mt_scene* scene, int precision);
 /* Replace the material table (TracerAPI material edits, src/cl/ui/fx/main/TracerAPI.java:371). */
 int mt_scene_set_materials(mt_scene* scene, const void* materials, int nmaterials);

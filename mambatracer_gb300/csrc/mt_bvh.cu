@@ -377,16 +377,12 @@ __global__ void k_quantize_fp16(const float4* __restrict__ recs, int nrec, uint4
 
 // 4-wide FP16 nodes from FP32 records: node r holds, for each child of record r,
 // that child's two children when it is interior, else the child (a leaf), with
-// the same outward rounding as the FP16 records after widening every box by eps
-// on each side (eps = 2^-16 of the scene's extent, against FP32 rounding of the
-// slab and triangle distances of about 2^-23 of the extent for rays starting in
-// the scene): a box holding a triangle hit before the current closest hit then
-// always passes, whatever the order in which the boxes are met.
-__global__ void k_quad_fp16(const float4* __restrict__ recs, int nrec, float eps, uint4* q) {
+// the same outward rounding as the FP16 records.
+__global__ void k_quad_fp16(const float4* __restrict__ recs, int nrec, uint4* q) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nrec) return;
-  auto pair = [eps](float lo, float hi) {
-    __half2 h = __halves2half2(__float2half_rd(lo - eps), __float2half_ru(hi + eps));
+  auto pair = [](float lo, float hi) {
+    __half2 h = __halves2half2(__float2half_rd(lo), __float2half_ru(hi));
     return *reinterpret_cast<unsigned*>(&h);
   };
   // a record's children: boxes (lo/hi per axis) and refs
@@ -601,23 +597,11 @@ int refresh_qnodes(mt_scene* s) {
     }
   }
   if (int w = refresh_wide(s)) return w;
-  if (s->precision == 3 && s->has_bvh && s->nrec > 0 && s->root_ref >= 0) {
+  if (s->precision == 3 && s->has_bvh && s->nrec > 0) {
     int r = dalloc(&s->d_quad, 4 * (size_t)s->nrec);
     if (r) return r;
     cudaStream_t st = s->ctx->stream;
-    float4 root[4];
-    if (cudaMemcpyAsync(root, s->d_nodes + 4 * (size_t)s->root_ref, sizeof(root), cudaMemcpyDeviceToHost, st) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess) {
-      dfree(s->d_quad);
-      return fail(MT_ERR_CUDA, "4-wide FP16 nodes: %s", cudaGetErrorString(cudaGetLastError()));
-    }
-    // the scene's extent: the root record's two child boxes
-    const float ext = std::max({std::max(root[0].y, root[1].y) - std::min(root[0].x, root[1].x),
-                                std::max(root[0].w, root[1].w) - std::min(root[0].z, root[1].z),
-                                std::max(root[2].y, root[2].w) - std::min(root[2].x, root[2].z)});
-    const float eps = std::isfinite(ext) && ext > 0.f ? std::ldexp(ext, -16) : 0.f;
-    k_quad_fp16<<<blocks(s->nrec), kT, 0, st>>>(s->d_nodes, s->nrec, eps, s->d_quad);
+    k_quad_fp16<<<blocks(s->nrec), kT, 0, st>>>(s->d_nodes, s->nrec, s->d_quad);
     if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
       dfree(s->d_quad);
       return fail(MT_ERR_CUDA, "4-wide FP16 nodes: %s", cudaGetErrorString(cudaGetLastError()));

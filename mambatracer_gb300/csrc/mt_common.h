@@ -66,8 +66,7 @@ static_assert(sizeof(Material) == 144, "Material layout");
 //     node of record r holds the grandchildren of r where a child of r is
 //     interior and the child itself where it is a leaf, in the order left's
 //     children, right's children; words 3c .. 3c + 2 = child c's x, y, z extents
-//     widened by 2^-16 of the scene's extent, as (lo rounded down, hi rounded up)
-//     half2 pairs, words 12 + c = child c's
+//     as (lo rounded down, hi rounded up) half2 pairs, words 12 + c = child c's
 //     ref (a record index, ~triangle slot, or kQuadEmpty: no child).
 //   up: per record (parent record, the record's sibling ref), the root (-1, -1):
 //     the links of the stackless traversal (bitstack_steps).

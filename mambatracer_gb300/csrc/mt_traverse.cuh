@@ -304,16 +304,17 @@ __device__ __forceinline__ bool bitstack_steps(const DevScene& S, RayT& r, int& 
 // Precision 3: the node of record r holds the children of r's two children
 // (a leaf child stands for itself), so one 64-byte node read replaces the two
 // dependent record reads of two binary levels. The boxes are the FP32 records'
-// child boxes widened by a margin far above the FP32 rounding of the slab and
-// triangle distances (2^-16 of the scene's extent) and rounded outward to FP16,
-// tested with the same slab arithmetic, so a box holding a triangle hit before
-// the current closest hit always passes and every triangle the binary traversal
-// tests is tested here with the same FP32 Moller-Trumbore: the closest hit is the
-// same triangle at the same distance, except that of two triangles hit at
-// exactly the same distance the one tested first is kept, and of triangles hit
-// within a few ulps of each other (coplanar) the nearer is kept, where the
-// reference's tight boxes can skip it. Children hit are taken nearest first; the
-// others are deferred with their entry distance (closest hits cull deferred
+// child boxes rounded outward to FP16 as in precision 1, tested with the same
+// slab arithmetic, so the boxes entered contain those the binary traversal
+// enters (a grandchild's box nests in its parent's) and every triangle it tests
+// is tested here with the same FP32 Moller-Trumbore: the closest hit is the same
+// triangle at the same distance, except among triangles hit at exactly or within
+// a few ulps of the same distance (coplanar surfaces), where the order in which
+// the boxes are met decides (a box test compares its entry distance with the
+// closest hit so far, and a box plane that FP16 represents exactly keeps no
+// slack against the triangle's own rounding); with leaves waiting for the warp
+// that order can change from run to run. Children hit are taken nearest first;
+// the others are deferred with their entry distance (closest hits cull deferred
 // interior nodes as above).
 __device__ __forceinline__ float max3f(float a, float b, float c) {
   float r;

@@ -14,10 +14,11 @@
    boxes stand on its floor): the reference's slab test on a flat triangle box
    then sometimes skips the nearer one, which the wide traversal tests. Those
    rays are counted, and the wide traversal's distance is never the larger.
-3. 4-wide FP16 nodes: a record's grandchildren with FP16 boxes rounded outward
-   after a margin of 2^-16 of the scene's extent (the intermediate level's boxes
-   are not tested): the same hits as 2; of two triangles hit at exactly the same
-   distance, the one kept may change between runs (leaf tests wait for the warp).
+3. 4-wide FP16 nodes: a record's grandchildren with the FP16 records' boxes (the
+   intermediate level's boxes are not tested): the same hits, except among
+   triangles hit at exactly or within a few ulps of the same distance, where
+   either may be kept, and the one kept may change between runs (leaf tests
+   wait for the warp).
 
 Frames in benchmark semantics are compared with the FP32 records' frames."""
 import numpy as np
@@ -58,23 +59,26 @@ def test_quantised_formats_trace_the_same_hits(ctx, which, prec):
         assert not tdiff.any()
         assert differ.sum() <= 1e-4 * len(p0), differ.sum()   # exact-distance ties only
     else:
-        # coplanar triangles hit within a few ulps: the wide traversal keeps the nearer
+        # coplanar triangles hit within a few ulps: the wide BVH keeps the nearer;
+        # the 4-wide nodes keep either
         ulps = np.abs(t0.view(np.int32).astype(np.int64) - t1.view(np.int32).astype(np.int64))
-        print(f"room, wide BVH: {differ.sum()} of {len(p0)} hit ids differ, {tdiff.sum()} distances "
-              f"(at most {ulps.max()} ulps, never farther)")
-        assert np.all(t1[tdiff] < t0[tdiff]) and ulps.max() <= 8
+        print(f"room, format {prec}: {differ.sum()} of {len(p0)} hit ids differ, {tdiff.sum()} distances "
+              f"(at most {ulps.max()} ulps, {(t1[tdiff] > t0[tdiff]).sum()} farther)")
+        assert ulps.max() <= 8
+        assert prec == 3 or np.all(t1[tdiff] < t0[tdiff])
         assert differ.sum() <= 0.01 * len(p0)
         assert np.all(differ | ~tdiff)
     # a rebuild keeps the format; going back to FP32 gives the FP32 answers
     S.build_bvh_device(want_arrays=False)
     t2, p2 = S.trace_closest(rays)
-    assert t2.tobytes() == t1.tobytes()
     if prec == 3:
-        # which of two triangles at exactly the same distance is kept depends on
-        # when the warp tests its waiting leaves, so it may change between runs
-        assert (p2 != p1).sum() <= 1e-4 * len(p1)
+        # among coplanar triangles the one kept depends on when the warp tests
+        # its waiting leaves, so it may change between runs (by a few ulps)
+        ulps2 = np.abs(t2.view(np.int32).astype(np.int64) - t1.view(np.int32).astype(np.int64))
+        assert ulps2.max() <= (8 if which == "room" else 0)
+        assert (p2 != p1).sum() <= (0.01 if which == "room" else 1e-4) * len(p1)
     else:
-        assert np.array_equal(p2, p1)
+        assert t2.tobytes() == t1.tobytes() and np.array_equal(p2, p1)
     # the traversal work: the FP32 records' triangle tests are the oracle's
     # (deferred leaves are always tested); the quantised formats test fewer or
     # more boxes but reach every triangle the FP32 records do
@@ -86,13 +90,16 @@ def test_quantised_formats_trace_the_same_hits(ctx, which, prec):
     S.close()
 
 
-def _same_or_nearer(t0, p0, t1, p1, coplanar_ok):
+def _same_or_nearer(t0, p0, t1, p1, prec):
+    """Format 1: the same distances; the wide BVH (2): the same, or the nearer of
+    coplanar triangles hit within a few ulps; the 4-wide nodes (3): either."""
     tdiff = t0.view(np.uint32) != t1.view(np.uint32)
-    if not coplanar_ok:
+    if prec == 1:
         assert not tdiff.any()
         return
     ulps = np.abs(t0.view(np.int32).astype(np.int64) - t1.view(np.int32).astype(np.int64))
-    assert np.all(t1[tdiff] < t0[tdiff]) and (ulps.max() if tdiff.any() else 0) <= 8
+    assert (ulps.max() if tdiff.any() else 0) <= 8
+    assert prec == 3 or np.all(t1[tdiff] < t0[tdiff])
     assert np.all((p0 != p1) | ~tdiff)
 
 
@@ -124,8 +131,8 @@ def test_quantised_formats_axis_aligned_rays(ctx, prec):
     t1, p1 = S.trace_closest(rays)
     assert np.array_equal(S.trace_any(srays), a0)
     assert (p0 >= 0).sum() > n // 4
-    # the box room's coplanar triangles: the wide formats may keep the nearer of two
-    _same_or_nearer(t0, p0, t1, p1, coplanar_ok=prec != 1)
+    # the box room's coplanar triangles
+    _same_or_nearer(t0, p0, t1, p1, prec)
     S.close()
 
 
@@ -145,7 +152,7 @@ def test_quantised_formats_tiny_trees(ctx, prec, ntri):
     t1, p1 = S.trace_closest(rays)
     assert np.array_equal(S.trace_any(rays), a0)
     assert (p0 >= 0).sum() > 0
-    _same_or_nearer(t0, p0, t1, p1, coplanar_ok=prec != 1)
+    _same_or_nearer(t0, p0, t1, p1, prec)
     assert np.array_equal(p0 >= 0, p1 >= 0)
     S.close()
 
