@@ -130,11 +130,27 @@ extern "C" int mt_batch_render(mt_context* ctx, mt_scene* s, const mt_batch_fram
   if (e != cudaSuccess) return done(fail(MT_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e)));
   const DevScene S = s->view();
   const DevEnv E = s->env_view();  // full-map environment sampling
-  for (int p = 0; p < max_spp; ++p)
-    if (launch_batch_pass(st, S, E, d_start + (size_t)p * (nframes + 1), d_film + (size_t)p * nframes,
-                          d_pp + (size_t)p * nframes, nact[p], tot[p], max_depth, film_kahan, d_ctrl + p, fb,
-                          ctx->num_sms, d_totals))
-      return done(fail(MT_ERR_CUDA, "batch pass launch: %s", cudaGetErrorString(cudaGetLastError())));
+  // every pass of the batch (per pass: raygen, per bounce closest hits, shading
+  // and shadow rays, ray totals) captured into one CUDA graph and launched once
+  e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return done(fail(MT_ERR_CUDA, "batch capture: %s", cudaGetErrorString(e)));
+  int lr = 0;
+  for (int p = 0; p < max_spp && !lr; ++p)
+    lr = launch_batch_pass(st, S, E, d_start + (size_t)p * (nframes + 1), d_film + (size_t)p * nframes,
+                           d_pp + (size_t)p * nframes, nact[p], tot[p], max_depth, film_kahan, d_ctrl + p, fb,
+                           ctx->num_sms, d_totals);
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(st, &graph);
+  if (lr || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return done(fail(MT_ERR_CUDA, "batch pass capture: %s", cudaGetErrorString(lr ? cudaGetLastError() : e)));
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+  if (exec) cudaGraphExecDestroy(exec);  // released once the launch completes
+  if (e != cudaSuccess) return done(fail(MT_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e)));
   unsigned long long h_tot[4] = {0, 0, 0, 0};
   e = cudaMemcpyAsync(films_out, fb.film, total * 16, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(h_tot, d_totals, 32, cudaMemcpyDeviceToHost, st);

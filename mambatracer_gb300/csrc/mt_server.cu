@@ -108,6 +108,8 @@ struct MergeGroup {
   Round rounds[kRounds];
   int next_round = 0;
   int inflight = 0;  // rounds whose end callback has not run (server lock)
+  // per scene: the executable graph of its merged pass, updated every round
+  std::vector<std::pair<const mt_scene*, cudaGraphExec_t>> graphs;
 };
 
 }  // namespace
@@ -287,6 +289,9 @@ void free_merged(mt_server* s) {
       if (Rd.done) cudaEventDestroy(Rd.done);
       Rd.done = nullptr;
     }
+    for (auto& g : G.graphs)
+      if (g.second) cudaGraphExecDestroy(g.second);
+    G.graphs.clear();
     if (G.stream) cudaStreamDestroy(G.stream);
     G.stream = nullptr;
   }
@@ -427,13 +432,46 @@ int issue_round(mt_server* s, MergeGroup& G, const std::vector<int>& work, const
     CU(cudaMemsetAsync(Rd.d_ctrl, 0, sizeof(Ctrl) * groups.size(), st));
   }
   for (size_t g = 0; g < groups.size(); ++g) {
+    // The scene group's merged pass (raygen, per bounce closest hits, shading and
+    // shadow rays, ray totals) as one CUDA graph: captured every round, since
+    // its path total sizes the grids and its tables move through the ring, and
+    // applied to the stream's executable graph of that scene by an update (the
+    // same kernels every round), instantiated again only when an update fails.
     const Group& Gr = groups[g];
     const DevScene S = Gr.scene->view();
     const DevEnv E = Gr.scene->env_view();  // full-map environment sampling
-    if (launch_batch_pass(st, S, E, Rd.d_tab + Gr.tab, Rd.d_tab + Gr.tab + Gr.n + 1, Rd.d_pp + Gr.pp, Gr.n,
-                          Gr.total, c.max_depth, c.film_kahan, Rd.d_ctrl + g, G.fb, s->ctx->num_sms, s->d_totals,
-                          s->groups.size() > 1))
-      return fail(MT_ERR_CUDA, "merged pass launch: %s", cudaGetErrorString(cudaGetLastError()));
+    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int lr = launch_batch_pass(st, S, E, Rd.d_tab + Gr.tab, Rd.d_tab + Gr.tab + Gr.n + 1, Rd.d_pp + Gr.pp,
+                                     Gr.n, Gr.total, c.max_depth, c.film_kahan, Rd.d_ctrl + g, G.fb,
+                                     s->ctx->num_sms, s->d_totals, s->groups.size() > 1);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (lr || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return fail(MT_ERR_CUDA, "merged pass capture: %s", cudaGetErrorString(lr ? cudaGetLastError() : e));
+    }
+    cudaGraphExec_t* ex = nullptr;
+    for (auto& kv : G.graphs)
+      if (kv.first == Gr.scene) ex = &kv.second;
+    if (!ex) {
+      G.graphs.emplace_back(Gr.scene, nullptr);
+      ex = &G.graphs.back().second;
+    }
+    if (*ex) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(*ex, graph, &info) != cudaSuccess) {
+        cudaGetLastError();  // an update that does not apply is not an error: instantiate again
+        cudaGraphExecDestroy(*ex);
+        *ex = nullptr;
+      }
+    }
+    if (!*ex) e = cudaGraphInstantiate(ex, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      *ex = nullptr;
+      return fail(MT_ERR_CUDA, "merged pass graph: %s", cudaGetErrorString(e));
+    }
+    CU(cudaGraphLaunch(*ex, st));
   }
   for (int k : go) {
     Lane& L = s->lanes[k];
