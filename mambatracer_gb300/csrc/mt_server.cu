@@ -98,6 +98,7 @@ struct Round {
 
 constexpr size_t kPathBytesPerPixel = 200;
 constexpr int kRounds = 3;
+constexpr size_t kGraphsPerStream = 16;  // scenes whose merged-pass graph a merge stream keeps
 
 // One merge stream: its slots, its share of the queues, its round ring.
 struct MergeGroup {
@@ -454,6 +455,11 @@ int issue_round(mt_server* s, MergeGroup& G, const std::vector<int>& work, const
     for (auto& kv : G.graphs)
       if (kv.first == Gr.scene) ex = &kv.second;
     if (!ex) {
+      if (G.graphs.size() >= kGraphsPerStream) {
+        // the oldest scene's graph goes (a graph still running is freed when it ends)
+        if (G.graphs.front().second) cudaGraphExecDestroy(G.graphs.front().second);
+        G.graphs.erase(G.graphs.begin());
+      }
       G.graphs.emplace_back(Gr.scene, nullptr);
       ex = &G.graphs.back().second;
     }
