@@ -70,6 +70,8 @@ def test_null_arguments_are_errors():
     assert L.mt_buf_write(None, 0, None, 0) == -1
     assert L.mt_job_stats(None, None, None) == -1
     assert L.mt_trace_closest(None, None, 0, None, None) == -1
+    assert L.mt_job_launches(None, None) == -1
+    assert L.mt_scene_set_bvh_precision(None, 3) == -1
 
 
 def test_single_triangle_bvh():
